@@ -1,0 +1,200 @@
+/*
+ * mx_reion.h — C ABI of the GB300 reionization grid step.
+ *
+ * This library replaces, for one process owning the whole box on one GPU, the
+ * three per-snapshot entry points of the Meraxes reionization step:
+ *
+ *   void find_HII_bubbles(int snapshot, timer_info* timer_total);
+ *        reference: src/core/find_HII_bubbles.h:12, body find_HII_bubbles.c:47-532
+ *   void ComputeTs(int snapshot, timer_info* timer_total);
+ *        reference: src/core/ComputeTs.h:13, body ComputeTs.c:78-1045
+ *   void ComputeBrightnessTemperatureBox(int snapshot);
+ *        reference: src/core/BrightnessTemperature.h:9, body BrightnessTemperature.c:24-549
+ *
+ * The reference reads everything from the global `run_globals`; this ABI takes
+ * the same data explicitly: the run parameters (mx_params, the subset of
+ * run_params_t / physics_params_t / run_units_t the step reads), the snapshot
+ * redshift list (run_globals.ZZ), and the grids (mx_grids, the
+ * run_globals.reion_grids fields) in the reference's own memory layouts:
+ *
+ *   PADDED  float[D][D][2(D/2+1)]  (FFTW in-place r2c layout; misc_tools.c:205)
+ *   REAL    float[D][D][D]                                     (misc_tools.c:208)
+ *
+ * Every entry point returns 0 on success or a negative MX_E* code; the text of
+ * the last error on a context is returned by mx_last_error().  No C++
+ * exception crosses this boundary and nothing calls exit().
+ *
+ * Two families of calls:
+ *   mx_<step>(...)          grids are HOST pointers; inputs are copied to the
+ *                           device, outputs copied back (what the reference's
+ *                           C driver needs as a drop-in).
+ *   mx_<step>_device(...)   grids are DEVICE pointers owned by the caller; no
+ *                           host copies; work is ordered on `stream`
+ *                           (a cudaStream_t, or NULL for the context stream).
+ */
+#ifndef MX_REION_H
+#define MX_REION_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MX_ABI_VERSION 1
+
+/* Status codes. */
+#define MX_OK 0
+#define MX_EINVAL (-1)   /* invalid parameter / argument */
+#define MX_ENOMEM (-2)   /* device or host allocation failed */
+#define MX_ECUDA (-3)    /* CUDA runtime or cuFFT error */
+#define MX_ETABLE (-4)   /* physics table missing or unreadable */
+#define MX_ESTATE (-5)   /* call order / snapshot list error */
+#define MX_ENOTSUP (-6)  /* configuration not supported */
+
+/* Run parameters read by the step.  Field names follow the reference's
+ * parameter names (src/meraxes.h run_params_t / physics_params_t / run_units_t;
+ * defaults in input/params/defaults.par). */
+typedef struct mx_params
+{
+  int32_t grid_dim; /* ReionGridDim */
+  int32_t abi_version; /* must be MX_ABI_VERSION */
+  double box_size;  /* BoxSize [Mpc/h] */
+
+  /* cosmology */
+  double hubble_h;     /* Hubble_h */
+  double omega_m;      /* OmegaM */
+  double omega_lambda; /* OmegaLambda */
+  double omega_r;      /* OmegaR */
+  double omega_k;      /* OmegaK */
+  double baryon_frac;  /* BaryonFrac */
+  double w_lambda;     /* wLambda */
+
+  /* units */
+  double unit_length_cm;     /* UnitLength_in_cm */
+  double unit_mass_g;        /* UnitMass_in_g */
+  double unit_velocity_cm_s; /* UnitVelocity_in_cm_per_s */
+
+  /* switches */
+  int32_t flag_recombinations;    /* Flag_IncludeRecombinations */
+  int32_t flag_spin_temp;         /* Flag_IncludeSpinTemp */
+  int32_t flag_21cm;              /* Flag_Compute21cmBrightTemp */
+  int32_t flag_pecvel;            /* Flag_IncludePecVelsFor21cm (0..3) */
+  int32_t uvb_flag;               /* ReionUVBFlag */
+  int32_t filter_type;            /* ReionFilterType: 0 tophat, 1 sharp-k, 2 Gaussian */
+  int32_t rtom_filter_type;       /* ReionRtoMFilterType: 0 tophat, 1 Gaussian */
+  int32_t ts_heating_filter_type; /* TsHeatingFilterType */
+  int32_t ts_num_filter_steps;    /* TsNumFilterSteps */
+  int32_t trees_id;               /* TreesID: velocity unit convention */
+
+  /* excursion set */
+  double delta_r_factor;      /* ReionDeltaRFactor */
+  double r_bubble_min;        /* ReionRBubbleMin [Mpc/h] */
+  double r_bubble_max;        /* ReionRBubbleMax [Mpc/h] */
+  double r_bubble_max_recomb; /* ReionRBubbleMaxRecomb [Mpc/h] */
+  double reion_efficiency;    /* physics.ReionEfficiency (as set by set_ReionEfficiency) */
+  double nion_phot_per_bary;  /* ReionNionPhotPerBary */
+  double gamma_halo_bias;     /* ReionGammaHaloBias */
+  double alpha_uv;            /* ReionAlphaUV */
+  double y_he;                /* Y_He */
+
+  /* X-ray heating / spin temperature */
+  double max_heating_redshift;  /* ReionMaxHeatingRedshift */
+  double lx_gal;                /* LXrayGal [erg/s per Msun/yr] */
+  double nu_xray_gal_threshold; /* NuXrayGalThreshold [eV] */
+  double spec_index_xray_gal;   /* SpecIndexXrayGal */
+  double nu_xray_soft_cut;      /* NuXraySoftCut [eV] */
+  double nu_xray_max;           /* NuXrayMax [eV] */
+  double reion_sfr_timescale;   /* ReionSfrTimescale (kept for completeness) */
+  double clumping_factor;       /* x_e sink clumping; the reference hard-codes
+                                   CLUMPING_FACTOR = 2 (XRayHeatingFunctions.h:30-32) */
+} mx_params;
+
+/* Grid pointers (all HOST or all DEVICE, depending on the call family).
+ * Fields the configuration does not use may be NULL. */
+typedef struct mx_grids
+{
+  float* deltax;       /* PADDED, in */
+  float* stars;        /* PADDED, in */
+  float* weighted_sfr; /* PADDED, in */
+  float* sfr;          /* PADDED, in; reweighted in place by ComputeTs like the reference */
+  float* sfr_histories; /* n_sfr_histories slices of 2*D*D*(D/2+1) floats, in */
+  float* N_rec;        /* PADDED, in/out (recombinations) */
+  float* x_e_box;      /* PADDED, in (find_HII_bubbles) / out (ComputeTs) */
+  float* x_e_box_prev; /* PADDED, in/out (ComputeTs) */
+  float* Tk_box;       /* REAL, in/out (ComputeTs) */
+  float* TS_box;       /* REAL, out (ComputeTs) */
+  float* xH;           /* REAL, out */
+  float* z_at_ionization;    /* REAL, in/out (init to -1) */
+  float* r_bubble;           /* REAL, out */
+  float* J_21;               /* REAL, out (UVB) */
+  float* J_21_at_ionization; /* REAL, in/out (UVB) */
+  float* Gamma12;            /* REAL, in/out (recombinations) */
+  float* delta_T;            /* REAL, out (21cm) */
+  float* vel;                /* PADDED, in; converted in place like the reference */
+} mx_grids;
+
+/* Global scalars written by the step (run_globals.reion_grids.* and the
+ * file-scope globals of XRayHeatingFunctions.c). */
+typedef struct mx_globals
+{
+  double volume_weighted_global_xH;   /* find_HII_bubbles.c:492 */
+  double volume_weighted_global_J_21; /* find_HII_bubbles.c:493 */
+  double mass_weighted_global_xH;     /* find_HII_bubbles.c:494 */
+  double volume_ave_J_alpha;          /* ComputeTs.c:926 */
+  double volume_ave_xalpha;
+  double volume_ave_Xheat;
+  double volume_ave_Xion;
+  double volume_ave_TS;   /* ComputeTs.c:972 */
+  double volume_ave_TK;
+  double volume_ave_xe;   /* as the reference computes it (ComputeTs.c:957) */
+  double volume_ave_Tb;   /* BrightnessTemperature.c:545 */
+  double x_e_ave;         /* cell mean of x_e_box_prev (ComputeTs.c:475) */
+  double collapse_fraction; /* stored_fcoll[snapshot] (ComputeTs.c:468) */
+  int32_t n_radii;        /* filter radii used by find_HII_bubbles */
+  int32_t gpu_launches;   /* kernels launched by the last call */
+} mx_globals;
+
+typedef struct mx_ctx mx_ctx;
+
+/* Context lifetime.  `tables_dir` is the directory holding the 21cmFAST
+ * tables (recfast_LCDM.dat, stellar_spectra.dat, kappa_*_table.dat,
+ * x_int_tables/); it is only read when flag_spin_temp is set.  The context
+ * owns all device scratch, cuFFT plans and physics tables. */
+int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out);
+void mx_destroy(mx_ctx* ctx);
+const char* mx_last_error(const mx_ctx* ctx); /* ctx may be NULL: last mx_create error */
+
+/* run_globals.ZZ: redshift of every snapshot (descending).  Also computes the
+ * number of stored SFR-history slices (set_sfr_history, ComputeTs.c:32-76). */
+int mx_set_redshifts(mx_ctx* ctx, const double* zz, int32_t n_snaps);
+int32_t mx_n_sfr_histories(const mx_ctx* ctx);
+/* Filter radii of find_HII_bubbles for this configuration (largest first). */
+int32_t mx_filter_radii(const mx_ctx* ctx, double* radii, int32_t cap);
+
+/* Host-pointer entry points (drop-in for the reference functions). */
+int mx_find_HII_bubbles(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out);
+int mx_ComputeTs(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out);
+int mx_ComputeBrightnessTemperatureBox(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out);
+/* ComputeTs (if spin temperature) -> find_HII_bubbles -> brightness
+ * temperature (if flag_21cm), the order of dracarys.c:352-390. */
+int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out);
+
+/* Device-pointer entry points. */
+int mx_find_HII_bubbles_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream);
+int mx_ComputeTs_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream);
+int mx_ComputeBrightnessTemperatureBox_device(mx_ctx* ctx,
+                                              int32_t snapshot,
+                                              const mx_grids* dev,
+                                              mx_globals* out,
+                                              void* stream);
+int mx_step_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream);
+
+/* Build information: returns a static string. */
+const char* mx_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MX_REION_H */

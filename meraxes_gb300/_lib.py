@@ -1,0 +1,75 @@
+"""Loader of the in-tree CUDA library (libmxreion.so) through its C ABI.
+
+The product path has no CPU fallback: if the library cannot be built or
+loaded, `load()` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from .params import MxGlobals, MxGrids, MxParams
+
+_LOCK = threading.Lock()
+_LIB = None
+
+MX_OK = 0
+ERRORS = {-1: "MX_EINVAL", -2: "MX_ENOMEM", -3: "MX_ECUDA", -4: "MX_ETABLE", -5: "MX_ESTATE", -6: "MX_ENOTSUP"}
+
+# every entry point declared in include/mx_reion.h
+EXPORTS = [
+    "mx_create", "mx_destroy", "mx_last_error", "mx_set_redshifts", "mx_n_sfr_histories", "mx_filter_radii",
+    "mx_find_HII_bubbles", "mx_ComputeTs", "mx_ComputeBrightnessTemperatureBox", "mx_step",
+    "mx_find_HII_bubbles_device", "mx_ComputeTs_device", "mx_ComputeBrightnessTemperatureBox_device",
+    "mx_step_device", "mx_build_info",
+]
+
+
+class MxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib_path() -> str:
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libmxreion.so")
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = lib_path()
+        if build_if_missing:
+            from .build import build
+
+            build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"CUDA library missing: {path} (run meraxes_gb300/build.py)")
+        L = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        L.mx_create.argtypes = [ctypes.POINTER(MxParams), ctypes.c_char_p, ctypes.POINTER(P)]
+        L.mx_create.restype = ctypes.c_int
+        L.mx_destroy.argtypes = [P]
+        L.mx_destroy.restype = None
+        L.mx_last_error.argtypes = [P]
+        L.mx_last_error.restype = ctypes.c_char_p
+        L.mx_set_redshifts.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int32]
+        L.mx_set_redshifts.restype = ctypes.c_int
+        L.mx_n_sfr_histories.argtypes = [P]
+        L.mx_n_sfr_histories.restype = ctypes.c_int32
+        L.mx_filter_radii.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int32]
+        L.mx_filter_radii.restype = ctypes.c_int32
+        for fn in ("mx_find_HII_bubbles", "mx_ComputeTs", "mx_ComputeBrightnessTemperatureBox", "mx_step"):
+            getattr(L, fn).argtypes = [P, ctypes.c_int32, ctypes.POINTER(MxGrids), ctypes.POINTER(MxGlobals)]
+            getattr(L, fn).restype = ctypes.c_int
+        for fn in ("mx_find_HII_bubbles_device", "mx_ComputeTs_device", "mx_ComputeBrightnessTemperatureBox_device",
+                   "mx_step_device"):
+            getattr(L, fn).argtypes = [P, ctypes.c_int32, ctypes.POINTER(MxGrids), ctypes.POINTER(MxGlobals), P]
+            getattr(L, fn).restype = ctypes.c_int
+        L.mx_build_info.argtypes = []
+        L.mx_build_info.restype = ctypes.c_char_p
+        _LIB = L
+        return L

@@ -1,0 +1,119 @@
+"""High-level interface of the reionization grid step.
+
+`ReionGridStep` mirrors the reference's entry points (src/core/find_HII_bubbles.c
+find_HII_bubbles, src/core/ComputeTs.c ComputeTs,
+src/core/BrightnessTemperature.c ComputeBrightnessTemperatureBox): one object
+per run holds the parameters, the snapshot redshift list and the device
+context; each call takes the grids of one snapshot.
+
+Grids are passed as a dict name -> array in the reference layouts (PADDED for
+deltax, stars, weighted_sfr, sfr, N_rec, x_e_box, x_e_box_prev, vel; REAL for
+the rest; sfr_histories as [n_slices, padded]).  numpy arrays select the
+host-pointer entry points (host<->device copies inside the call); CUDA torch
+tensors select the device entry points on torch's current stream.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .params import GRID_NAMES, MxGlobals, MxGrids, ReionParams
+from .synthetic import TABLES_DIR
+
+
+def _is_torch_cuda(a) -> bool:
+    return hasattr(a, "is_cuda") and bool(a.is_cuda)
+
+
+class ReionGridStep:
+    def __init__(self, params: ReionParams, redshifts: Sequence[float], tables_dir: str = TABLES_DIR):
+        self.lib = _lib.load()
+        self.params = params
+        self._pc = params.to_ctypes()
+        self.ctx = ctypes.c_void_p()
+        rc = self.lib.mx_create(ctypes.byref(self._pc), tables_dir.encode(), ctypes.byref(self.ctx))
+        if rc != 0:
+            raise _lib.MxError(rc, self.lib.mx_last_error(None).decode())
+        zz = (ctypes.c_double * len(redshifts))(*[float(z) for z in redshifts])
+        self._check(self.lib.mx_set_redshifts(self.ctx, zz, len(redshifts)))
+        self.redshifts = list(redshifts)
+        self.n_sfr_histories = int(self.lib.mx_n_sfr_histories(self.ctx))
+        self.last_launches = 0
+
+    # ------------------------------------------------------------------ utils
+    def _check(self, rc: int):
+        if rc != 0:
+            raise _lib.MxError(rc, self.lib.mx_last_error(self.ctx).decode())
+
+    def close(self):
+        if self.ctx:
+            self.lib.mx_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def filter_radii(self):
+        buf = (ctypes.c_double * 1024)()
+        n = self.lib.mx_filter_radii(self.ctx, buf, 1024)
+        return list(buf[:n])
+
+    def _grids(self, grids: Dict[str, object]):
+        g = MxGrids()
+        device = None
+        for name in GRID_NAMES:
+            a = grids.get(name)
+            if a is None:
+                continue
+            if _is_torch_cuda(a):
+                if device is False:
+                    raise ValueError("mixing host and device grids")
+                device = True
+                import torch
+
+                if a.dtype != torch.float32 or not a.is_contiguous():
+                    raise ValueError(f"{name}: need contiguous float32")
+                setattr(g, name, a.data_ptr())
+            else:
+                if device is True:
+                    raise ValueError("mixing host and device grids")
+                device = False
+                if not isinstance(a, np.ndarray) or a.dtype != np.float32 or not a.flags.c_contiguous:
+                    raise ValueError(f"{name}: need C-contiguous float32 numpy array")
+                setattr(g, name, a.ctypes.data)
+        return g, bool(device)
+
+    def _call(self, name: str, snapshot: int, grids) -> Dict[str, float]:
+        g, device = self._grids(grids)
+        out = MxGlobals()
+        if device:
+            import torch
+
+            stream = torch.cuda.current_stream().cuda_stream
+            rc = getattr(self.lib, name + "_device")(self.ctx, snapshot, ctypes.byref(g), ctypes.byref(out),
+                                                    ctypes.c_void_p(stream))
+        else:
+            rc = getattr(self.lib, name)(self.ctx, snapshot, ctypes.byref(g), ctypes.byref(out))
+        self._check(rc)
+        self.last_launches = out.gpu_launches
+        return out.as_dict()
+
+    # --------------------------------------------------------- entry points
+    def find_HII_bubbles(self, snapshot: int, grids) -> Dict[str, float]:
+        return self._call("mx_find_HII_bubbles", snapshot, grids)
+
+    def ComputeTs(self, snapshot: int, grids) -> Dict[str, float]:
+        return self._call("mx_ComputeTs", snapshot, grids)
+
+    def ComputeBrightnessTemperatureBox(self, snapshot: int, grids) -> Dict[str, float]:
+        return self._call("mx_ComputeBrightnessTemperatureBox", snapshot, grids)
+
+    def step(self, snapshot: int, grids) -> Dict[str, float]:
+        """ComputeTs -> find_HII_bubbles -> brightness temperature."""
+        return self._call("mx_step", snapshot, grids)

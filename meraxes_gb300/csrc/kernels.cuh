@@ -1,0 +1,181 @@
+// Device kernels of the reionization grid step and their launch helpers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mx {
+
+// Reduction blocks used by every deterministic two-stage FP64 reduction.
+constexpr int RED_BLOCKS = 608;  // 4 x 152 SMs
+constexpr int RED_THREADS = 256;
+constexpr int MAX_FIELDS = 5;
+constexpr int MAX_SHELLS = 64;
+constexpr int MAX_RADII = 256;
+
+struct GridDims
+{
+  int D;       // cells per side
+  int H;       // D/2 + 1
+  long long C; // complex elements D*D*H
+  long long N; // cells D^3
+  long long P; // padded reals 2*C
+};
+
+// ------------------------------------------------------------ k-space filter
+// Per-radius parameters of a filtered batch.
+struct FilterBatch
+{
+  int n;                   // radii in the batch
+  int filter_type;         // 0 tophat, 1 sharp-k, 2 Gaussian
+  int scale_mode;          // 0: (float)((double)v / N); 1: v / (float)N
+  float R[MAX_RADII];      // (float)R per radius
+  int apply[MAX_RADII];    // 0 on the unfiltered last step
+};
+
+// out[(r*G + g)] = filter_r(scale(in[g])) for every complex element.
+void launch_filter(const float2* const* in, int G, float2* out, long long out_field_stride, const FilterBatch& fb,
+                   const GridDims& gd, float box_size, cudaStream_t s);
+
+// ---------------------------------------------------------- threshold loop
+struct RadiusParams
+{
+  double R, M_mean, R_cubed, J21_const, Gamma_pref;
+  int last;
+};
+struct ThresholdArgs
+{
+  const float* fields;   // batch base: field (r*G + g) at fields + (r*G+g)*P
+  long long P;
+  int G;                 // fields per radius: dx, stars, wsfr, [x_e], [N_rec]
+  int idx_xe, idx_nr;    // field slot or -1
+  int n_r;               // radii in this batch
+  const RadiusParams* rp; // device array, n_r entries
+  float* xH;
+  float* z_at_ion;
+  float* r_bubble;
+  float* J21;
+  float* J21_at_ion;
+  float* Gamma12;
+  double pixel_volume, eff, redshift;
+  float gamma_halo_bias;
+  int uvb, recomb, spin;
+};
+void launch_threshold(const ThresholdArgs& a, const GridDims& gd, cudaStream_t s);
+
+// ---------------------------------------------------------------- reductions
+struct FhbReduceArgs
+{
+  const float* xH;
+  const float* J21;
+  const float* deltax;  // PADDED, unfiltered input
+  const float* Gamma12;
+  float* N_rec;         // PADDED, updated when recomb
+  const double* rr_y;   // recombination table (device)
+  const double* rr_c;
+  const double* rr_x;
+  double redshift;
+  float fabs_dtdz, zstep;
+  int uvb, recomb;
+  double* partials;     // RED_BLOCKS x 4
+};
+void launch_fhb_reduce(const FhbReduceArgs& a, const GridDims& gd, cudaStream_t s);
+// Sums `nvals` columns of a RED_BLOCKS x nvals partials array in fixed order.
+void launch_finalize(const double* partials, int nvals, double* out, cudaStream_t s);
+
+// ------------------------------------------------------------ grid helpers
+void launch_fill(float* p, long long n, float v, cudaStream_t s);
+void launch_fill_real_in_padded(float* p, const GridDims& gd, float v, cudaStream_t s);
+
+// ---------------------------------------------------------------- ComputeTs
+// SFR-history operations on the PADDED sfr grid (ComputeTs.c:288-377).
+void launch_sfr_scale_half(float* sfr, long long nhalf, double w, cudaStream_t s);
+void launch_sfr_zero_half(float* sfr, long long nhalf, cudaStream_t s);
+void launch_sfr_load(float* sfr, const float* slice, float w, int accumulate, const GridDims& gd, cudaStream_t s);
+
+// Shell value extraction: shells[r*N + real] = max(filtered_real, 0).
+void launch_shell_extract(const float* filtered, long long P, int n, int r0, float* shells, const GridDims& gd,
+                          cudaStream_t s);
+
+// Collapse fraction and mean x_e of the unsmoothed fields (ComputeTs.c:413-475).
+struct CfArgs
+{
+  const float* stars;
+  const float* deltax;
+  const float* x_e_prev;
+  double RtoM_h2;  // RtoM(R) * h * h
+  double R3;       // pow(R, 3.0)
+  double pixel_volume;
+  double* partials; // RED_BLOCKS x 2
+};
+void launch_cf_xe(const CfArgs& a, const GridDims& gd, cudaStream_t s);
+
+// Per-cell constants of the spin-temperature update.
+struct TsDevConst
+{
+  int S, no_light;
+  float zp;
+  double zpd;
+  double dzp, dt_dzp, growth, dgrowth, prefactor, conv, p2, p3, n_b0, f_h, f_he, no;
+  double pixel_volume, sfr_a, sfr_b, clumping;
+  double hubble_z, hubble0_h, h;  // hubble((float)zp), HUBBLE*h, h
+  double a[MAX_SHELLS], b[MAX_SHELLS], zpp1[MAX_SHELLS], sum_lyn[MAX_SHELLS], dt_dzpp[MAX_SHELLS],
+    dzpp[MAX_SHELLS];
+  double tab[3][14][MAX_SHELLS];
+  float xhii[14];
+  // kappa splines (ln T -> ln kappa)
+  int nk[3];
+  double kx[3][27], ky[3][27], kc[3][27];
+};
+
+struct EvolveArgs
+{
+  const float* shells;  // S x N
+  const float* deltax;  // PADDED
+  float* x_e_prev;      // PADDED
+  float* Tk;            // REAL
+  float* TS;            // REAL
+  const TsDevConst* cst;  // device copy
+  double* partials;       // RED_BLOCKS x 4 (J_alpha, xalpha, Xheat, Xion)
+  unsigned int* err;      // error word (iteration cap)
+};
+void launch_evolve(const EvolveArgs& a, const GridDims& gd, cudaStream_t s);
+
+// Homogeneous branch: fill x_e, T_K and compute T_S with J_alpha = 0.
+struct HomogArgs
+{
+  const float* deltax;
+  const float* stars;
+  float* x_e_prev;
+  float* Tk;
+  float* TS;
+  float xe0, tk0;
+  const TsDevConst* cst;
+  double RtoM_h2, R3, pixel_volume;
+  double* partials;  // RED_BLOCKS x 1 (collapse fraction)
+  unsigned int* err;
+};
+void launch_homog(const HomogArgs& a, const GridDims& gd, cudaStream_t s);
+
+// Means of T_S and T_K (ComputeTs.c:942-974).
+void launch_ts_means(const float* TS, const float* Tk, double* partials, const GridDims& gd, cudaStream_t s);
+
+// --------------------------------------------------- brightness temperature
+struct DeltaTArgs
+{
+  const float* deltax;
+  const float* xH;
+  const float* TS;
+  float* delta_T;
+  float const_factor;
+  double T_rad;
+  float redshift;
+  int spin, pecvel;
+  double* partials;  // RED_BLOCKS x 1
+};
+void launch_delta_T(const DeltaTArgs& a, const GridDims& gd, cudaStream_t s);
+
+int kernel_launch_count();
+void reset_kernel_launch_count();
+
+}  // namespace mx

@@ -1,0 +1,996 @@
+// C ABI of the GB300 reionization grid step (include/mx_reion.h):
+// context, device memory plan, cuFFT plans and the orchestration of
+// find_HII_bubbles, ComputeTs and the brightness-temperature box.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <future>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "host_physics.h"
+#include "kernels.cuh"
+#include "mx_reion.h"
+
+using namespace mx;
+
+namespace {
+thread_local std::string g_create_error;
+
+struct CudaError
+{
+  int code;
+  std::string msg;
+};
+
+#define MX_CUDA(call)                                                                                                  \
+  do {                                                                                                                 \
+    cudaError_t e_ = (call);                                                                                           \
+    if (e_ != cudaSuccess)                                                                                             \
+      throw CudaError{ MX_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_) };                                \
+  } while (0)
+#define MX_CUFFT(call)                                                                                                 \
+  do {                                                                                                                 \
+    cufftResult r_ = (call);                                                                                           \
+    if (r_ != CUFFT_SUCCESS)                                                                                           \
+      throw CudaError{ MX_ECUDA, std::string(#call) + ": cufft status " + std::to_string((int)r_) };                  \
+  } while (0)
+
+int hw_threads()
+{
+  unsigned n = std::thread::hardware_concurrency();
+  return n ? (int)n : 4;
+}
+}  // namespace
+
+struct mx_ctx
+{
+  mx_params p;
+  Derived d;
+  GridDims gd;
+  std::string err;
+  std::string tables_dir;
+  std::vector<double> zz;
+  int n_hist = 0;
+  double stored_fcoll[1000];
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int nthreads = 4;
+
+  RecombTable rr;
+  HeatTables ht;
+  double *d_rr_x = nullptr, *d_rr_y = nullptr, *d_rr_c = nullptr;
+
+  // scratch
+  float2* d_unf = nullptr;      // MAX_FIELDS x C
+  float2* d_work = nullptr;     // batch x C
+  long long work_fields = 0;    // capacity in spectra
+  float2** d_in_ptrs = nullptr; // device array of MAX_FIELDS pointers
+  double* d_partials = nullptr; // RED_BLOCKS x 8
+  double* d_sums = nullptr;     // 16
+  double* h_sums = nullptr;     // pinned, 16
+  RadiusParams* d_rp = nullptr;
+  TsDevConst* d_tsc = nullptr;
+  TsDevConst* h_tsc = nullptr;  // pinned
+  float* d_shells = nullptr;    // S x N (spin temperature)
+  unsigned int* d_err = nullptr;
+  float* d_xe_last = nullptr;
+  // device mirror used by the host-pointer entry points
+  mx_grids mirror{};
+  std::vector<void*> mirror_allocs;
+  std::map<long long, cufftHandle> c2r_plans;  // keyed by batch
+  cufftHandle r2c_plan = 0;
+  int launches = 0;
+
+  ~mx_ctx();
+  void alloc_scratch();
+  cufftHandle c2r_plan(long long batch);
+  void ensure_mirror();
+};
+
+mx_ctx::~mx_ctx()
+{
+  for (auto& kv : c2r_plans)
+    cufftDestroy(kv.second);
+  if (r2c_plan)
+    cufftDestroy(r2c_plan);
+  cudaFree(d_unf);
+  cudaFree(d_work);
+  cudaFree(d_in_ptrs);
+  cudaFree(d_partials);
+  cudaFree(d_sums);
+  cudaFreeHost(h_sums);
+  cudaFree(d_rp);
+  cudaFree(d_tsc);
+  cudaFreeHost(h_tsc);
+  cudaFree(d_shells);
+  cudaFree(d_err);
+  cudaFree(d_xe_last);
+  cudaFree(d_rr_x);
+  cudaFree(d_rr_y);
+  cudaFree(d_rr_c);
+  for (void* q : mirror_allocs)
+    cudaFree(q);
+  if (stream)
+    cudaStreamDestroy(stream);
+}
+
+static int n_fields(const mx_params& p) { return 3 + (p.flag_spin_temp ? 1 : 0) + (p.flag_recombinations ? 1 : 0); }
+
+void mx_ctx::alloc_scratch()
+{
+  const int G = n_fields(p);
+  MX_CUDA(cudaMalloc(&d_unf, sizeof(float2) * gd.C * MAX_FIELDS));
+  // Radius batch: as many (radius, field) spectra as the memory plan allows,
+  // up to all radii of the snapshot.
+  const std::vector<double> radii = filter_radii(p);
+  size_t free_b = 0, total_b = 0;
+  MX_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double spectrum = (double)sizeof(float2) * gd.C;
+  const long long want = (long long)radii.size() * G;
+  long long fit = (long long)(0.45 * (double)free_b / spectrum);
+  if (const char* env = std::getenv("MX_MAX_BATCH_SPECTRA"))
+    fit = std::min(fit, (long long)std::atoll(env));
+  long long cap = std::max<long long>(G, std::min(want, fit));
+  cap = std::max<long long>(G, (cap / G) * G);
+  if (p.flag_spin_temp)
+    cap = std::max<long long>(cap, 1);
+  work_fields = cap;
+  MX_CUDA(cudaMalloc(&d_work, spectrum * cap));
+  MX_CUDA(cudaMalloc(&d_in_ptrs, sizeof(float2*) * MAX_FIELDS));
+  MX_CUDA(cudaMalloc(&d_partials, sizeof(double) * RED_BLOCKS * 8));
+  MX_CUDA(cudaMalloc(&d_sums, sizeof(double) * 16));
+  MX_CUDA(cudaMallocHost(&h_sums, sizeof(double) * 16));
+  MX_CUDA(cudaMalloc(&d_rp, sizeof(RadiusParams) * MAX_RADII));
+  MX_CUDA(cudaMalloc(&d_err, sizeof(unsigned int)));
+  MX_CUDA(cudaMemset(d_err, 0, sizeof(unsigned int)));
+  MX_CUDA(cudaMalloc(&d_xe_last, sizeof(float)));
+  if (p.flag_spin_temp) {
+    MX_CUDA(cudaMalloc(&d_tsc, sizeof(TsDevConst)));
+    MX_CUDA(cudaMallocHost(&h_tsc, sizeof(TsDevConst)));
+    MX_CUDA(cudaMalloc(&d_shells, sizeof(float) * gd.N * (size_t)p.ts_num_filter_steps));
+  }
+  // forward transform: padded real input -> half spectrum (out of place)
+  int n[3] = { gd.D, gd.D, gd.D };
+  int inembed[3] = { gd.D, gd.D, 2 * gd.H };
+  int onembed[3] = { gd.D, gd.D, gd.H };
+  MX_CUFFT(cufftPlanMany(&r2c_plan, 3, n, inembed, 1, (int)gd.P, onembed, 1, (int)gd.C, CUFFT_R2C, 1));
+  MX_CUFFT(cufftSetStream(r2c_plan, stream));
+}
+
+cufftHandle mx_ctx::c2r_plan(long long batch)
+{
+  auto it = c2r_plans.find(batch);
+  if (it != c2r_plans.end())
+    return it->second;
+  cufftHandle h;
+  int n[3] = { gd.D, gd.D, gd.D };
+  int inembed[3] = { gd.D, gd.D, gd.H };
+  int onembed[3] = { gd.D, gd.D, 2 * gd.H };
+  MX_CUFFT(cufftPlanMany(&h, 3, n, inembed, 1, (int)gd.C, onembed, 1, (int)gd.P, CUFFT_C2R, (int)batch));
+  MX_CUFFT(cufftSetStream(h, stream));
+  c2r_plans[batch] = h;
+  return h;
+}
+
+void mx_ctx::ensure_mirror()
+{
+  if (mirror.deltax)
+    return;
+  float** f[] = { &mirror.deltax, &mirror.stars, &mirror.weighted_sfr, &mirror.sfr, &mirror.N_rec, &mirror.x_e_box,
+                  &mirror.x_e_box_prev, &mirror.vel };
+  for (float** q : f) {
+    MX_CUDA(cudaMalloc((void**)q, sizeof(float) * gd.P));
+    MX_CUDA(cudaMemset(*q, 0, sizeof(float) * gd.P));
+    mirror_allocs.push_back(*q);
+  }
+  float** r[] = { &mirror.Tk_box, &mirror.TS_box, &mirror.xH, &mirror.z_at_ionization, &mirror.r_bubble,
+                  &mirror.J_21, &mirror.J_21_at_ionization, &mirror.Gamma12, &mirror.delta_T };
+  for (float** q : r) {
+    MX_CUDA(cudaMalloc((void**)q, sizeof(float) * gd.N));
+    MX_CUDA(cudaMemset(*q, 0, sizeof(float) * gd.N));
+    mirror_allocs.push_back(*q);
+  }
+  if (p.flag_spin_temp && n_hist > 0) {
+    MX_CUDA(cudaMalloc((void**)&mirror.sfr_histories, sizeof(float) * gd.P * n_hist));
+    mirror_allocs.push_back(mirror.sfr_histories);
+  }
+}
+
+// ======================================================================
+// find_HII_bubbles (src/core/find_HII_bubbles.c:47-495)
+// ======================================================================
+static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s)
+{
+  const mx_params& p = c->p;
+  const GridDims& gd = c->gd;
+  const int uvb = p.uvb_flag, recomb = p.flag_recombinations, spin = p.flag_spin_temp;
+  const double redshift = c->zz[snapshot];
+  const double prev_z = snapshot == 0 ? c->zz[snapshot] : c->zz[snapshot - 1];
+  const float zstep = (float)(prev_z - redshift);
+  const float fabs_dtdz = (float)std::fabs(dtdz(p, (float)redshift) / p.hubble_h);
+  const double pixel_volume = std::pow(p.box_size / (double)gd.D, 3);
+  const int launches0 = kernel_launch_count();
+
+  if (!g->deltax || !g->stars || !g->weighted_sfr || !g->xH || !g->z_at_ionization || !g->r_bubble ||
+      (uvb && (!g->J_21 || !g->J_21_at_ionization)) || (recomb && (!g->N_rec || !g->Gamma12)) ||
+      (spin && !g->x_e_box))
+    throw CudaError{ MX_EINVAL, "find_HII_bubbles: a required grid pointer is NULL" };
+
+  // initial state (find_HII_bubbles.c:102-116)
+  if (uvb)
+    launch_fill(g->J_21, gd.N, 0.0f, s);
+  launch_fill(g->xH, gd.N, 1.0f, s);
+  launch_fill(g->r_bubble, gd.N, 0.0f, s);
+
+  // forward transforms of the G fields (find_HII_bubbles.c:118-163)
+  const float* src[MAX_FIELDS];
+  int G = 0, idx_xe = -1, idx_nr = -1;
+  src[G++] = g->deltax;
+  src[G++] = g->stars;
+  src[G++] = g->weighted_sfr;
+  if (spin) {
+    idx_xe = G;
+    src[G++] = g->x_e_box;
+  }
+  if (recomb) {
+    idx_nr = G;
+    src[G++] = g->N_rec;
+  }
+  float2* unf_ptrs[MAX_FIELDS];
+  for (int f = 0; f < G; f++) {
+    unf_ptrs[f] = c->d_unf + (long long)f * gd.C;
+    MX_CUFFT(cufftSetStream(c->r2c_plan, s));
+    MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)src[f], (cufftComplex*)unf_ptrs[f]));
+  }
+  MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, unf_ptrs, sizeof(float2*) * G, cudaMemcpyHostToDevice, s));
+
+  // radius schedule (find_HII_bubbles.c:184-207)
+  const std::vector<double> radii = filter_radii(p);
+  const int nR = (int)radii.size();
+  if (nR > MAX_RADII)
+    throw CudaError{ MX_ENOTSUP, "too many filter radii" };
+  std::vector<RadiusParams> rps(nR);
+  for (int r = 0; r < nR; r++) {
+    const double R = radii[r];
+    RadiusParams& q = rps[r];
+    q.R = R;
+    q.last = (r == nR - 1);
+    q.M_mean = RtoM(p, c->d, R);
+    q.R_cubed = R * R * R;
+    q.J21_const = (1.0 + redshift) * (1.0 + redshift) / (4.0 * k::PI) * p.alpha_uv * k::PLANCK * 1e21 * R *
+                  p.unit_length_cm * p.nion_phot_per_bary / k::PROTONMASS * p.unit_mass_g /
+                  std::pow(p.unit_length_cm, 3) / c->d.unit_time_s;
+    q.Gamma_pref = 0;
+    if (recomb) {
+      q.Gamma_pref = (1.0 + redshift) * (1.0 + redshift) * R * (p.unit_length_cm / p.hubble_h) * k::SIGMA_HI *
+                     p.alpha_uv / (p.alpha_uv + 2.75) / 1.0e-12;
+      q.Gamma_pref *= (p.unit_mass_g / c->d.unit_time_s) * std::pow(p.unit_length_cm / p.hubble_h, -3.) *
+                      p.nion_phot_per_bary / k::PROTONMASS;
+    }
+  }
+  MX_CUDA(cudaMemcpyAsync(c->d_rp, rps.data(), sizeof(RadiusParams) * nR, cudaMemcpyHostToDevice, s));
+
+  // batched filter -> C2R -> threshold over chunks of radii, largest first
+  const int per_batch = (int)std::max<long long>(1, c->work_fields / G);
+  for (int r0 = 0; r0 < nR; r0 += per_batch) {
+    const int nb = std::min(per_batch, nR - r0);
+    FilterBatch fb;
+    fb.n = nb;
+    fb.filter_type = p.filter_type;
+    fb.scale_mode = 0;
+    for (int r = 0; r < nb; r++) {
+      fb.R[r] = (float)radii[r0 + r];
+      fb.apply[r] = (r0 + r) != nR - 1;
+    }
+    launch_filter((const float2* const*)c->d_in_ptrs, G, c->d_work, gd.C, fb, gd, (float)p.box_size, s);
+    // one radius (G fields) per cuFFT execution keeps the cuFFT work area at
+    // the size of one radius' spectra
+    const cufftHandle plan = c->c2r_plan(G);
+    for (int r = 0; r < nb; r++) {
+      cufftComplex* w = (cufftComplex*)(c->d_work + (long long)r * G * gd.C);
+      MX_CUFFT(cufftExecC2R(plan, w, (cufftReal*)w));
+    }
+    ThresholdArgs ta;
+    ta.fields = (const float*)c->d_work;
+    ta.P = gd.P;
+    ta.G = G;
+    ta.idx_xe = idx_xe;
+    ta.idx_nr = idx_nr;
+    ta.n_r = nb;
+    ta.rp = c->d_rp + r0;
+    ta.xH = g->xH;
+    ta.z_at_ion = g->z_at_ionization;
+    ta.r_bubble = g->r_bubble;
+    ta.J21 = g->J_21;
+    ta.J21_at_ion = g->J_21_at_ionization;
+    ta.Gamma12 = g->Gamma12;
+    ta.pixel_volume = pixel_volume;
+    ta.eff = p.reion_efficiency;
+    ta.redshift = redshift;
+    ta.gamma_halo_bias = (float)p.gamma_halo_bias;
+    ta.uvb = uvb;
+    ta.recomb = recomb;
+    ta.spin = spin;
+    launch_threshold(ta, gd, s);
+  }
+
+  // global means and N_rec (find_HII_bubbles.c:451-494)
+  FhbReduceArgs ra;
+  ra.xH = g->xH;
+  ra.J21 = g->J_21;
+  ra.deltax = g->deltax;
+  ra.Gamma12 = g->Gamma12;
+  ra.N_rec = g->N_rec;
+  ra.rr_x = c->d_rr_x;
+  ra.rr_y = c->d_rr_y;
+  ra.rr_c = c->d_rr_c;
+  ra.redshift = redshift;
+  ra.fabs_dtdz = fabs_dtdz;
+  ra.zstep = zstep;
+  ra.uvb = uvb;
+  ra.recomb = recomb;
+  ra.partials = c->d_partials;
+  launch_fhb_reduce(ra, gd, s);
+  launch_finalize(c->d_partials, 4, c->d_sums, s);
+  MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  MX_CUDA(cudaStreamSynchronize(s));
+  const double total = std::pow((double)gd.D, 3);
+  if (out) {
+    out->volume_weighted_global_xH = c->h_sums[0] / total;
+    out->volume_weighted_global_J_21 = uvb ? c->h_sums[1] / total : 0.0;
+    out->mass_weighted_global_xH = c->h_sums[2] / c->h_sums[3];
+    out->n_radii = nR;
+    out->gpu_launches = kernel_launch_count() - launches0;
+  }
+}
+
+// ======================================================================
+// ComputeTs (src/core/ComputeTs.c:78-1020)
+// ======================================================================
+static void fill_kappa(mx_ctx* c, TsDevConst* t)
+{
+  const NaturalSpline* sp[3] = { &c->ht.kap10, &c->ht.kap_e, &c->ht.kap_p };
+  for (int w = 0; w < 3; w++) {
+    t->nk[w] = (int)sp[w]->x.size();
+    for (int i = 0; i < t->nk[w]; i++) {
+      t->kx[w][i] = sp[w]->x[i];
+      t->ky[w][i] = sp[w]->y[i];
+      t->kc[w][i] = sp[w]->c[i];
+    }
+  }
+}
+
+static void fill_common_ts(mx_ctx* c, TsDevConst* t, double zp)
+{
+  const mx_params& p = c->p;
+  t->zp = (float)zp;
+  t->zpd = zp;
+  t->n_b0 = c->d.n_b0;
+  t->f_h = c->d.f_h;
+  t->f_he = c->d.f_he;
+  t->no = c->d.no;
+  t->hubble_z = hubble(p, (float)zp);
+  t->hubble0_h = k::HUBBLE * p.hubble_h;
+  t->h = p.hubble_h;
+  t->clumping = p.clumping_factor;
+  for (int i = 0; i < 14; i++)
+    t->xhii[i] = c->ht.xhii[i];
+  fill_kappa(c, t);
+}
+
+static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s)
+{
+  const mx_params& p = c->p;
+  const GridDims& gd = c->gd;
+  const int launches0 = kernel_launch_count();
+  if (!p.flag_spin_temp)
+    throw CudaError{ MX_ESTATE, "ComputeTs: flag_spin_temp is off" };
+  if (!g->deltax || !g->stars || !g->sfr || !g->x_e_box || !g->x_e_box_prev || !g->Tk_box || !g->TS_box ||
+      (c->n_hist > 0 && !g->sfr_histories))
+    throw CudaError{ MX_EINVAL, "ComputeTs: a required grid pointer is NULL" };
+  const double box = p.box_size / p.hubble_h;
+  const double pixel_volume = std::pow(box / (double)gd.D, 3);
+  const double total = std::pow((double)gd.D, 3);
+  const double zp = c->zz[snapshot];
+  const double prev_z = snapshot == 0 ? c->zz[snapshot] : c->zz[snapshot - 1];
+  const ShellPlan sp = plan_shells(p, c->zz, snapshot);
+  const int S = p.ts_num_filter_steps;
+  if (S > MAX_SHELLS)
+    throw CudaError{ MX_ENOTSUP, "too many spin-temperature shells" };
+  TsDevConst* t = c->h_tsc;
+  std::memset(t, 0, sizeof(TsDevConst));
+  fill_common_ts(c, t, zp);
+  const double R0 = k::L_FACTOR * box / (float)gd.D;
+  const double RtoM_h2 = RtoM(p, c->d, R0) * p.hubble_h * p.hubble_h;
+  double collapse_fraction = 0.0, x_e_ave = 0.0;
+
+  if (sp.homogeneous) {
+    // ComputeTs.c:189-262
+    MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
+    HomogArgs ha;
+    ha.deltax = g->deltax;
+    ha.stars = g->stars;
+    ha.x_e_prev = g->x_e_box_prev;
+    ha.Tk = g->Tk_box;
+    ha.TS = g->TS_box;
+    ha.xe0 = (float)(float)c->ht.xion_recfast((float)zp);
+    ha.tk0 = (float)(float)c->ht.T_recfast((float)zp);
+    ha.cst = c->d_tsc;
+    ha.RtoM_h2 = RtoM_h2;
+    ha.R3 = std::pow(R0, 3.0);
+    ha.pixel_volume = pixel_volume;
+    ha.partials = c->d_partials;
+    ha.err = c->d_err;
+    launch_homog(ha, gd, s);
+    launch_finalize(c->d_partials, 1, c->d_sums, s);
+    MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double), cudaMemcpyDeviceToHost, s));
+    MX_CUDA(cudaStreamSynchronize(s));
+    collapse_fraction = c->h_sums[0] / total;
+  } else {
+    // collapse fraction and <x_e> of the unsmoothed fields (ComputeTs.c:413-475)
+    CfArgs ca;
+    ca.stars = g->stars;
+    ca.deltax = g->deltax;
+    ca.x_e_prev = g->x_e_box_prev;
+    ca.RtoM_h2 = RtoM_h2;
+    ca.R3 = std::pow(R0, 3.0);
+    ca.pixel_volume = pixel_volume;
+    ca.partials = c->d_partials;
+    launch_cf_xe(ca, gd, s);
+    launch_finalize(c->d_partials, 2, c->d_sums, s);
+    MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+    MX_CUDA(cudaStreamSynchronize(s));
+    collapse_fraction = c->h_sums[0] / total;
+    x_e_ave = c->h_sums[1] / total;
+    c->stored_fcoll[snapshot] = collapse_fraction;
+
+    // X-ray frequency tables on host threads while the shells are smoothed
+    FreqTables ft;
+    std::vector<double> zz = c->zz;
+    std::future<void> tables = std::async(std::launch::async, [&]() {
+      build_freq_tables(p, c->d, c->ht, zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads,
+                        &ft);
+    });
+
+    // shells (ComputeTs.c:276-503): apply the SFR-history operations, forward
+    // transform when the grid changed, then filter + inverse transform in
+    // batches of shells sharing a spectrum.
+    try {
+      float2* sfr_unf = c->d_unf;
+      const long long nhalf = gd.C;
+      int r = 0;
+      while (r < S) {
+        for (const SfrOp& op : sp.ops[r]) {
+          if (op.kind == SfrOp::SCALE_HALF)
+            launch_sfr_scale_half(g->sfr, nhalf, op.dweight, s);
+          else if (op.kind == SfrOp::ZERO_HALF)
+            launch_sfr_zero_half(g->sfr, nhalf, s);
+          else
+            launch_sfr_load(g->sfr, g->sfr_histories + (long long)op.slice * gd.P, op.weight,
+                            op.kind == SfrOp::ADD, gd, s);
+        }
+        MX_CUFFT(cufftSetStream(c->r2c_plan, s));
+        MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)g->sfr, (cufftComplex*)sfr_unf));
+        // shells r..r_end-1 share this spectrum (no operations in between)
+        int r_end = r + 1;
+        while (r_end < S && sp.ops[r_end].empty())
+          r_end++;
+        float2* in_ptr[1] = { sfr_unf };
+        MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, in_ptr, sizeof(float2*), cudaMemcpyHostToDevice, s));
+        for (int q0 = r; q0 < r_end;) {
+          const int nb = (int)std::min<long long>(c->work_fields, r_end - q0);
+          FilterBatch fb;
+          fb.n = nb;
+          fb.filter_type = p.ts_heating_filter_type;
+          fb.scale_mode = 1;
+          for (int q = 0; q < nb; q++) {
+            fb.R[q] = (float)sp.R[q0 + q];
+            fb.apply[q] = (q0 + q) > 0;
+          }
+          launch_filter((const float2* const*)c->d_in_ptrs, 1, c->d_work, gd.C, fb, gd, (float)p.box_size, s);
+          const cufftHandle plan = c->c2r_plan(1);
+          for (int q = 0; q < nb; q++) {
+            cufftComplex* w = (cufftComplex*)(c->d_work + (long long)q * gd.C);
+            MX_CUFFT(cufftExecC2R(plan, w, (cufftReal*)w));
+          }
+          launch_shell_extract((const float*)c->d_work, gd.P, nb, q0, c->d_shells, gd, s);
+          q0 += nb;
+        }
+        r = r_end;
+      }
+    } catch (...) {
+      tables.wait();
+      throw;
+    }
+    tables.get();
+
+    // per-cell constants (ComputeTs.c:666-724, XRayHeatingFunctions.c:1241-1435)
+    const float zpf = (float)zp;
+    t->S = S;
+    t->no_light = (collapse_fraction > 0.0) ? 0 : 1;
+    t->dzp = zp - prev_z;
+    t->dt_dzp = ft.dt_dzp;
+    t->growth = ft.growth_zp;
+    t->dgrowth = ft.dgrowth_dzp;
+    t->prefactor = ft.const_zp_prefactor;
+    t->conv = (k::C / (4. * k::PI)) / (k::PROTONMASS / k::SOLAR_MASS);
+    t->p2 = std::pow((double)(1.0f + zpf), 2);
+    t->p3 = std::pow((double)(1.0f + zpf), 3);
+    t->pixel_volume = pixel_volume;
+    t->sfr_a = p.unit_mass_g / c->d.unit_time_s;
+    t->sfr_b = std::pow(p.unit_length_cm, -3.);
+    for (int q = 0; q < S; q++) {
+      t->a[q] = sp.a_dt_dz[q];
+      t->b[q] = sp.b_pow[q];
+      t->zpp1[q] = sp.zpp1[q];
+      t->sum_lyn[q] = ft.sum_lyn[q];
+      t->dt_dzpp[q] = sp.dt_dzpp[q];
+      t->dzpp[q] = sp.dzpp[q];
+      for (int x = 0; x < 14; x++)
+        for (int w = 0; w < 3; w++)
+          t->tab[w][x][q] = ft.tab[((size_t)w * 14 + x) * S + q];
+    }
+    MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
+    EvolveArgs ea;
+    ea.shells = c->d_shells;
+    ea.deltax = g->deltax;
+    ea.x_e_prev = g->x_e_box_prev;
+    ea.Tk = g->Tk_box;
+    ea.TS = g->TS_box;
+    ea.cst = c->d_tsc;
+    ea.partials = c->d_partials;
+    ea.err = c->d_err;
+    launch_evolve(ea, gd, s);
+    launch_finalize(c->d_partials, 4, c->d_sums + 8, s);
+    MX_CUDA(cudaMemcpyAsync(c->h_sums + 8, c->d_sums + 8, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  }
+
+  // x_e_box <- x_e_box_prev (ComputeTs.c:940) and the means (:942-974)
+  MX_CUDA(cudaMemcpyAsync(g->x_e_box, g->x_e_box_prev, sizeof(float) * gd.P, cudaMemcpyDeviceToDevice, s));
+  launch_ts_means(g->TS_box, g->Tk_box, c->d_partials, gd, s);
+  launch_finalize(c->d_partials, 2, c->d_sums, s);
+  MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+  // the reference's <x_e> reads the last cell's x_e_box_prev (ComputeTs.c:957)
+  const long long last_pad = (long long)(gd.D - 1) + 2LL * gd.H * ((long long)(gd.D - 1) + (long long)gd.D * (gd.D - 1));
+  float xe_last = 0.f;
+  MX_CUDA(cudaMemcpyAsync(c->d_xe_last, g->x_e_box_prev + last_pad, sizeof(float), cudaMemcpyDeviceToDevice, s));
+  unsigned int errw = 0;
+  MX_CUDA(cudaMemcpyAsync(&errw, c->d_err, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+  MX_CUDA(cudaMemcpyAsync(&xe_last, c->d_xe_last, sizeof(float), cudaMemcpyDeviceToHost, s));
+  MX_CUDA(cudaStreamSynchronize(s));
+  if (errw) {
+    MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
+    throw CudaError{ MX_ECUDA, "ComputeTs: spin-temperature iteration did not converge" };
+  }
+  if (out) {
+    if (!sp.homogeneous) {
+      out->volume_ave_J_alpha = c->h_sums[8] / total;
+      out->volume_ave_xalpha = c->h_sums[9] / total;
+      out->volume_ave_Xheat = c->h_sums[10] / total;
+      out->volume_ave_Xion = c->h_sums[11] / total;
+    }
+    out->volume_ave_TS = c->h_sums[0] / total;
+    out->volume_ave_TK = c->h_sums[1] / total;
+    out->volume_ave_xe = (double)xe_last;
+    out->x_e_ave = x_e_ave;
+    out->collapse_fraction = collapse_fraction;
+    out->gpu_launches = kernel_launch_count() - launches0;
+  }
+}
+
+// ======================================================================
+// ComputeBrightnessTemperatureBox (src/core/BrightnessTemperature.c:24-549)
+// ======================================================================
+static void run_delta_T(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s)
+{
+  const mx_params& p = c->p;
+  const GridDims& gd = c->gd;
+  const int launches0 = kernel_launch_count();
+  if (p.flag_spin_temp && p.flag_pecvel > 0)
+    throw CudaError{ MX_ENOTSUP, "peculiar-velocity modes of the brightness temperature are not built" };
+  if (!g->deltax || !g->xH || !g->delta_T || (p.flag_spin_temp && !g->TS_box))
+    throw CudaError{ MX_EINVAL, "ComputeBrightnessTemperatureBox: a required grid pointer is NULL" };
+  const float redshift = (float)(float)c->zz[snapshot];
+  const float Hubble_h = (float)(float)p.hubble_h;
+  const float OmegaM = (float)(float)p.omega_m;
+  const float OmegaB = (float)(OmegaM * p.baryon_frac);
+  DeltaTArgs a;
+  a.const_factor = (float)(27.0 * (OmegaB * Hubble_h * Hubble_h / 0.023) *
+                           std::sqrt((0.15 / OmegaM / Hubble_h / Hubble_h) * (1.0 + redshift) / 10.0));
+  a.T_rad = k::TCMB * (1. + redshift);
+  a.redshift = redshift;
+  a.deltax = g->deltax;
+  a.xH = g->xH;
+  a.TS = g->TS_box;
+  a.delta_T = g->delta_T;
+  a.spin = p.flag_spin_temp;
+  a.pecvel = p.flag_pecvel;
+  a.partials = c->d_partials;
+  launch_delta_T(a, gd, s);
+  launch_finalize(c->d_partials, 1, c->d_sums, s);
+  MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double), cudaMemcpyDeviceToHost, s));
+  MX_CUDA(cudaStreamSynchronize(s));
+  if (out) {
+    out->volume_ave_Tb = c->h_sums[0] / std::pow((double)gd.D, 3);
+    out->gpu_launches = kernel_launch_count() - launches0;
+  }
+}
+
+// ======================================================================
+// C ABI
+// ======================================================================
+template <class F>
+static int guarded(mx_ctx* c, F&& f)
+{
+  if (!c)
+    return MX_EINVAL;
+  try {
+    if (cudaSetDevice(c->device) != cudaSuccess)
+      throw CudaError{ MX_ECUDA, "cudaSetDevice failed" };
+    f();
+    c->err.clear();
+    return MX_OK;
+  } catch (const CudaError& e) {
+    c->err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    c->err = "host allocation failed";
+    return MX_ENOMEM;
+  } catch (const std::exception& e) {
+    c->err = e.what();
+    return MX_EINVAL;
+  }
+}
+
+static void check_snapshot(mx_ctx* c, int snapshot)
+{
+  if (c->zz.empty())
+    throw CudaError{ MX_ESTATE, "mx_set_redshifts has not been called" };
+  if (snapshot < 0 || snapshot >= (int)c->zz.size() || snapshot >= 1000)
+    throw CudaError{ MX_EINVAL, "snapshot out of range" };
+}
+
+static cudaStream_t pick(mx_ctx* c, void* stream) { return stream ? (cudaStream_t)stream : c->stream; }
+
+extern "C" {
+
+const char* mx_build_info(void) { return "meraxes_gb300 reion step, sm_103a, abi 1"; }
+
+int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out)
+{
+  g_create_error.clear();
+  if (!params || !out) {
+    g_create_error = "mx_create: NULL argument";
+    return MX_EINVAL;
+  }
+  *out = nullptr;
+  const mx_params& p = *params;
+  if (p.abi_version != MX_ABI_VERSION) {
+    g_create_error = "mx_create: abi_version mismatch";
+    return MX_EINVAL;
+  }
+  if (p.grid_dim < 2 || p.grid_dim % 2 != 0 || p.grid_dim > 2048 || !(p.box_size > 0) || !(p.delta_r_factor > 1.0) ||
+      p.filter_type < 0 || p.filter_type > 2 || p.rtom_filter_type < 0 || p.rtom_filter_type > 1 ||
+      (p.flag_spin_temp && (p.ts_num_filter_steps < 1 || p.ts_num_filter_steps > MAX_SHELLS ||
+                            p.ts_heating_filter_type < 0 || p.ts_heating_filter_type > 2))) {
+    g_create_error = "mx_create: invalid parameter";
+    return MX_EINVAL;
+  }
+  std::unique_ptr<mx_ctx> c(new (std::nothrow) mx_ctx());
+  if (!c) {
+    g_create_error = "mx_create: host allocation failed";
+    return MX_ENOMEM;
+  }
+  c->p = p;
+  c->d.init(p);
+  c->gd.D = p.grid_dim;
+  c->gd.H = p.grid_dim / 2 + 1;
+  c->gd.C = (long long)p.grid_dim * p.grid_dim * c->gd.H;
+  c->gd.N = (long long)p.grid_dim * p.grid_dim * p.grid_dim;
+  c->gd.P = 2 * c->gd.C;
+  c->tables_dir = tables_dir ? tables_dir : "";
+  std::memset(c->stored_fcoll, 0, sizeof(c->stored_fcoll));
+  c->nthreads = std::max(1, std::min(64, hw_threads()));
+  if (const char* env = std::getenv("MX_HOST_THREADS"))
+    c->nthreads = std::max(1, std::atoi(env));
+  try {
+    if (cudaGetDevice(&c->device) != cudaSuccess)
+      throw CudaError{ MX_ECUDA, "no CUDA device" };
+    MX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    if (p.filter_type != 0 && p.filter_type != 1 && p.filter_type != 2)
+      throw CudaError{ MX_EINVAL, "invalid filter type" };
+    if (p.flag_spin_temp) {
+      std::string e;
+      int rc = c->ht.load(p, c->tables_dir, &e);
+      if (rc)
+        throw CudaError{ rc, e };
+    }
+    if (p.flag_recombinations) {
+      c->rr.build(p, c->d, c->nthreads);
+      const size_t n = c->rr.y.size();
+      MX_CUDA(cudaMalloc(&c->d_rr_x, sizeof(double) * c->rr.lng.size()));
+      MX_CUDA(cudaMalloc(&c->d_rr_y, sizeof(double) * n));
+      MX_CUDA(cudaMalloc(&c->d_rr_c, sizeof(double) * n));
+      MX_CUDA(cudaMemcpy(c->d_rr_x, c->rr.lng.data(), sizeof(double) * c->rr.lng.size(), cudaMemcpyHostToDevice));
+      MX_CUDA(cudaMemcpy(c->d_rr_y, c->rr.y.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+      MX_CUDA(cudaMemcpy(c->d_rr_c, c->rr.c.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    }
+    c->alloc_scratch();
+  } catch (const CudaError& e) {
+    g_create_error = e.msg;
+    return e.code == MX_ECUDA && e.msg.find("memory") != std::string::npos ? MX_ENOMEM : e.code;
+  }
+  *out = c.release();
+  return MX_OK;
+}
+
+void mx_destroy(mx_ctx* ctx)
+{
+  if (!ctx)
+    return;
+  cudaSetDevice(ctx->device);
+  delete ctx;
+}
+
+const char* mx_last_error(const mx_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int mx_set_redshifts(mx_ctx* ctx, const double* zz, int32_t n_snaps)
+{
+  return guarded(ctx, [&]() {
+    if (!zz || n_snaps < 1 || n_snaps > 1000)
+      throw CudaError{ MX_EINVAL, "mx_set_redshifts: bad list" };
+    ctx->zz.assign(zz, zz + n_snaps);
+    ctx->n_hist = ctx->p.flag_spin_temp ? n_sfr_histories(ctx->p, ctx->zz) : 0;
+  });
+}
+
+int32_t mx_n_sfr_histories(const mx_ctx* ctx) { return ctx ? ctx->n_hist : -1; }
+
+int32_t mx_filter_radii(const mx_ctx* ctx, double* radii, int32_t cap)
+{
+  if (!ctx)
+    return MX_EINVAL;
+  const std::vector<double> r = filter_radii(ctx->p);
+  for (int i = 0; i < (int)r.size() && i < cap; i++)
+    radii[i] = r[i];
+  return (int32_t)r.size();
+}
+
+int mx_find_HII_bubbles_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!dev)
+      throw CudaError{ MX_EINVAL, "NULL grids" };
+    run_find_HII_bubbles(ctx, snapshot, dev, out, pick(ctx, stream));
+  });
+}
+
+int mx_ComputeTs_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!dev)
+      throw CudaError{ MX_EINVAL, "NULL grids" };
+    run_ComputeTs(ctx, snapshot, dev, out, pick(ctx, stream));
+  });
+}
+
+int mx_ComputeBrightnessTemperatureBox_device(mx_ctx* ctx,
+                                              int32_t snapshot,
+                                              const mx_grids* dev,
+                                              mx_globals* out,
+                                              void* stream)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!dev)
+      throw CudaError{ MX_EINVAL, "NULL grids" };
+    run_delta_T(ctx, snapshot, dev, out, pick(ctx, stream));
+  });
+}
+
+int mx_step_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!dev)
+      throw CudaError{ MX_EINVAL, "NULL grids" };
+    cudaStream_t s = pick(ctx, stream);
+    int launches = 0;
+    if (ctx->p.flag_spin_temp) {
+      run_ComputeTs(ctx, snapshot, dev, out, s);
+      launches += out ? out->gpu_launches : 0;
+    }
+    run_find_HII_bubbles(ctx, snapshot, dev, out, s);
+    launches += out ? out->gpu_launches : 0;
+    if (ctx->p.flag_21cm) {
+      run_delta_T(ctx, snapshot, dev, out, s);
+      launches += out ? out->gpu_launches : 0;
+    }
+    if (out)
+      out->gpu_launches = launches;
+  });
+}
+
+// ------------------------------------------------------------ host family
+namespace {
+enum Dir { IN = 1, OUT = 2 };
+struct FieldIO
+{
+  float* mx_grids::*member;
+  bool padded;
+  int dir;
+};
+
+void copy_fields(mx_ctx* c, const mx_grids* host, const std::vector<FieldIO>& fields, int dir, cudaStream_t s)
+{
+  for (const FieldIO& f : fields) {
+    if (!(f.dir & dir))
+      continue;
+    float* h = host->*(f.member);
+    float* d = c->mirror.*(f.member);
+    if (!h)
+      continue;
+    const size_t n = f.padded ? (size_t)c->gd.P : (size_t)c->gd.N;
+    if (dir == IN)
+      MX_CUDA(cudaMemcpyAsync(d, h, n * sizeof(float), cudaMemcpyHostToDevice, s));
+    else
+      MX_CUDA(cudaMemcpyAsync(h, d, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+  }
+}
+
+// Device grids for a host call: the mirror, with NULL where the caller passed NULL.
+mx_grids mirror_for(mx_ctx* c, const mx_grids* host)
+{
+  mx_grids m = c->mirror;
+  float* mx_grids::*all[] = { &mx_grids::deltax,   &mx_grids::stars,        &mx_grids::weighted_sfr,
+                              &mx_grids::sfr,      &mx_grids::sfr_histories, &mx_grids::N_rec,
+                              &mx_grids::x_e_box,  &mx_grids::x_e_box_prev, &mx_grids::Tk_box,
+                              &mx_grids::TS_box,   &mx_grids::xH,           &mx_grids::z_at_ionization,
+                              &mx_grids::r_bubble, &mx_grids::J_21,         &mx_grids::J_21_at_ionization,
+                              &mx_grids::Gamma12,  &mx_grids::delta_T,      &mx_grids::vel };
+  for (auto mem : all)
+    if (!(host->*mem))
+      m.*mem = nullptr;
+  return m;
+}
+
+const std::vector<FieldIO>& fhb_fields()
+{
+  static const std::vector<FieldIO> f = {
+    { &mx_grids::deltax, true, IN },           { &mx_grids::stars, true, IN },
+    { &mx_grids::weighted_sfr, true, IN },     { &mx_grids::x_e_box, true, IN },
+    { &mx_grids::N_rec, true, IN | OUT },      { &mx_grids::xH, false, OUT },
+    { &mx_grids::z_at_ionization, false, IN | OUT }, { &mx_grids::r_bubble, false, OUT },
+    { &mx_grids::J_21, false, OUT },           { &mx_grids::J_21_at_ionization, false, IN | OUT },
+    { &mx_grids::Gamma12, false, IN | OUT },
+  };
+  return f;
+}
+const std::vector<FieldIO>& ts_fields()
+{
+  static const std::vector<FieldIO> f = {
+    { &mx_grids::deltax, true, IN },        { &mx_grids::stars, true, IN },
+    { &mx_grids::sfr, true, IN | OUT },     { &mx_grids::x_e_box, true, OUT },
+    { &mx_grids::x_e_box_prev, true, IN | OUT }, { &mx_grids::Tk_box, false, IN | OUT },
+    { &mx_grids::TS_box, false, OUT },
+  };
+  return f;
+}
+const std::vector<FieldIO>& dt_fields()
+{
+  static const std::vector<FieldIO> f = {
+    { &mx_grids::deltax, true, IN },
+    { &mx_grids::xH, false, IN },
+    { &mx_grids::TS_box, false, IN },
+    { &mx_grids::delta_T, false, OUT },
+  };
+  return f;
+}
+
+void copy_histories(mx_ctx* c, const mx_grids* host, cudaStream_t s)
+{
+  if (c->n_hist > 0 && host->sfr_histories)
+    MX_CUDA(cudaMemcpyAsync(c->mirror.sfr_histories, host->sfr_histories, sizeof(float) * c->gd.P * c->n_hist,
+                            cudaMemcpyHostToDevice, s));
+}
+}  // namespace
+
+int mx_find_HII_bubbles(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!host)
+      throw CudaError{ MX_EINVAL, "NULL grids" };
+    ctx->ensure_mirror();
+    cudaStream_t s = ctx->stream;
+    copy_fields(ctx, host, fhb_fields(), IN, s);
+    mx_grids m = mirror_for(ctx, host);
+    run_find_HII_bubbles(ctx, snapshot, &m, out, s);
+    copy_fields(ctx, host, fhb_fields(), OUT, s);
+    MX_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int mx_ComputeTs(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!host)
+      throw CudaError{ MX_EINVAL, "NULL grids" };
+    ctx->ensure_mirror();
+    cudaStream_t s = ctx->stream;
+    copy_fields(ctx, host, ts_fields(), IN, s);
+    copy_histories(ctx, host, s);
+    mx_grids m = mirror_for(ctx, host);
+    run_ComputeTs(ctx, snapshot, &m, out, s);
+    copy_fields(ctx, host, ts_fields(), OUT, s);
+    MX_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int mx_ComputeBrightnessTemperatureBox(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!host)
+      throw CudaError{ MX_EINVAL, "NULL grids" };
+    ctx->ensure_mirror();
+    cudaStream_t s = ctx->stream;
+    copy_fields(ctx, host, dt_fields(), IN, s);
+    mx_grids m = mirror_for(ctx, host);
+    run_delta_T(ctx, snapshot, &m, out, s);
+    copy_fields(ctx, host, dt_fields(), OUT, s);
+    MX_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!host)
+      throw CudaError{ MX_EINVAL, "NULL grids" };
+    ctx->ensure_mirror();
+    cudaStream_t s = ctx->stream;
+    // union of the inputs of the three stages
+    std::vector<FieldIO> all = fhb_fields();
+    if (ctx->p.flag_spin_temp)
+      for (const FieldIO& f : ts_fields())
+        all.push_back(f);
+    copy_fields(ctx, host, all, IN, s);
+    if (ctx->p.flag_spin_temp)
+      copy_histories(ctx, host, s);
+    mx_grids m = mirror_for(ctx, host);
+    int launches = 0;
+    if (ctx->p.flag_spin_temp) {
+      run_ComputeTs(ctx, snapshot, &m, out, s);
+      launches += out ? out->gpu_launches : 0;
+    }
+    run_find_HII_bubbles(ctx, snapshot, &m, out, s);
+    launches += out ? out->gpu_launches : 0;
+    if (ctx->p.flag_21cm) {
+      run_delta_T(ctx, snapshot, &m, out, s);
+      launches += out ? out->gpu_launches : 0;
+    }
+    std::vector<FieldIO> outs = all;
+    if (ctx->p.flag_21cm)
+      outs.push_back({ &mx_grids::delta_T, false, OUT });
+    copy_fields(ctx, host, outs, OUT, s);
+    MX_CUDA(cudaStreamSynchronize(s));
+    if (out)
+      out->gpu_launches = launches;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,51 @@
+/*
+ * CPU oracle of the reionization grid step — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's per-snapshot grid step
+ * (find_HII_bubbles, ComputeTs, ComputeBrightnessTemperatureBox) operating on
+ * explicit host grids in the reference layouts (include/mx_reion.h).  Used by
+ * the tests, the smoke check and the CPU baseline of the benchmark as the
+ * checker; never linked by the product library.
+ *
+ * Parity pinning: this restatement is checked against the reference's own
+ * sources compiled with the shims in oracle/shims (oracle/_ref, built by
+ * `make ref` where the reference tree is present) and against the committed
+ * fixtures in tests/golden/ that were produced by that build.
+ */
+#ifndef MX_ORACLE_H
+#define MX_ORACLE_H
+
+#include "../include/mx_reion.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mxo_ctx mxo_ctx;
+
+int mxo_create(const mx_params* p, const char* tables_dir, mxo_ctx** out);
+void mxo_destroy(mxo_ctx* c);
+int mxo_set_redshifts(mxo_ctx* c, const double* zz, int n_snaps);
+int mxo_n_sfr_histories(const mxo_ctx* c);
+int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out);
+int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out);
+int mxo_delta_T(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out);
+/* Per-cell threshold margin of the last find_HII_bubbles call (REAL layout):
+ * min over radii, up to and including the first crossing, of
+ * |f_coll*eff / (nf*(1+rec)) - 1|.  A cell whose flag, r_bubble or first-crossing
+ * J_21 can legitimately differ between two FP32 FFT implementations has a
+ * small margin.  NULL before a call. */
+const float* mxo_last_margin(const mxo_ctx* c);
+
+/* Table-level helpers (host physics) for tests. */
+double mxo_recombination_rate_splined(mxo_ctx* c, double z_eff, double gamma12);
+double mxo_dtdz(const mxo_ctx* c, float z);
+double mxo_get_Ts(mxo_ctx* c, float z, float delta, float TK, float xe, float Jalpha, float* xalpha);
+/* Frequency-integral tables of the last ComputeTs call: [3][14][n_shells]. */
+const double* mxo_last_freq_tables(const mxo_ctx* c, int* n_shells);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,170 @@
+/*
+ * Driver for the reference's own reionization sources compiled against the
+ * shims (oracle/_ref/libmxref.so) — TEST INFRASTRUCTURE ONLY.
+ *
+ * It sets up `run_globals` the way init_meraxes() / init_storage() do for the
+ * fields the grid step reads (src/core/init.c:184-205 set_units,
+ * init.c:292-313 set_sfr_history / init_MHR, reionization.c:518-952
+ * malloc_reionization_grids), then calls the reference's entry points
+ * find_HII_bubbles(), ComputeTs() and ComputeBrightnessTemperatureBox()
+ * unmodified.  Used only to pin the C restatement in mx_oracle.c and to make
+ * the golden fixtures under tests/golden/.
+ */
+#define _MAIN
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "meraxes.h"
+
+#include "BrightnessTemperature.h"
+#include "ComputeTs.h"
+#include "XRayHeatingFunctions.h"
+#include "find_HII_bubbles.h"
+#include "recombinations.h"
+#include "reionization.h"
+#include "utils.h"
+
+#include "../include/mx_reion.h"
+
+static int g_ready = 0;
+
+int mxref_init(const mx_params* p, const double* zz, int n_snaps, const char* tables_dir)
+{
+  memset(&run_globals, 0, sizeof(run_globals));
+  run_params_t* rp = &run_globals.params;
+  physics_params_t* ph = &rp->physics;
+  run_units_t* u = &run_globals.units;
+
+  run_globals.mpi_comm = MPI_COMM_WORLD;
+  run_globals.mpi_rank = 0;
+  run_globals.mpi_size = 1;
+
+  rp->BoxSize = p->box_size;
+  rp->Hubble_h = p->hubble_h;
+  rp->OmegaM = p->omega_m;
+  rp->OmegaLambda = p->omega_lambda;
+  rp->OmegaR = p->omega_r;
+  rp->OmegaK = p->omega_k;
+  rp->BaryonFrac = p->baryon_frac;
+  rp->wLambda = p->w_lambda;
+  rp->ReionGridDim = p->grid_dim;
+  rp->ReionFilterType = p->filter_type;
+  rp->ReionRtoMFilterType = p->rtom_filter_type;
+  rp->TsHeatingFilterType = p->ts_heating_filter_type;
+  rp->TsNumFilterSteps = p->ts_num_filter_steps;
+  rp->ReionUVBFlag = p->uvb_flag;
+  rp->ReionDeltaRFactor = p->delta_r_factor;
+  rp->TreesID = (enum tree_ids)p->trees_id;
+  rp->Flag_PatchyReion = 1;
+  rp->Flag_IncludeSpinTemp = p->flag_spin_temp;
+  rp->Flag_IncludeRecombinations = p->flag_recombinations;
+  rp->Flag_Compute21cmBrightTemp = p->flag_21cm;
+  rp->Flag_IncludePecVelsFor21cm = p->flag_pecvel;
+  rp->Flag_ComputePS = 0;
+  rp->Flag_ConstructLightcone = 0;
+  rp->ReionSfrTimescale = p->reion_sfr_timescale;
+  strncpy(rp->TablesForXHeatingDir, tables_dir ? tables_dir : ".", STRLEN - 1);
+  rp->FFTW3WisdomDir[0] = '\0';
+
+  ph->ReionEfficiency = p->reion_efficiency;
+  ph->ReionNionPhotPerBary = p->nion_phot_per_bary;
+  ph->ReionGammaHaloBias = p->gamma_halo_bias;
+  ph->ReionAlphaUV = p->alpha_uv;
+  ph->Y_He = p->y_he;
+  ph->ReionRBubbleMin = p->r_bubble_min;
+  ph->ReionRBubbleMax = p->r_bubble_max;
+  ph->ReionRBubbleMaxRecomb = p->r_bubble_max_recomb;
+  ph->ReionMaxHeatingRedshift = p->max_heating_redshift;
+  ph->LXrayGal = p->lx_gal;
+  ph->NuXrayGalThreshold = p->nu_xray_gal_threshold;
+  ph->SpecIndexXrayGal = p->spec_index_xray_gal;
+  ph->NuXraySoftCut = p->nu_xray_soft_cut;
+  ph->NuXrayMax = p->nu_xray_max;
+
+  /* set_units (init.c:184-205) */
+  u->UnitLength_in_cm = p->unit_length_cm;
+  u->UnitMass_in_g = p->unit_mass_g;
+  u->UnitVelocity_in_cm_per_s = p->unit_velocity_cm_s;
+  u->UnitTime_in_s = u->UnitLength_in_cm / u->UnitVelocity_in_cm_per_s;
+  u->UnitTime_in_Megayears = u->UnitTime_in_s / SEC_PER_MEGAYEAR;
+  run_globals.G = GRAVITY / pow(u->UnitLength_in_cm, 3) * u->UnitMass_in_g * pow(u->UnitTime_in_s, 2);
+  run_globals.Hubble = HUBBLE * u->UnitTime_in_s;
+  run_globals.RhoCrit = 3 * run_globals.Hubble * run_globals.Hubble / (8 * M_PI * run_globals.G);
+
+  run_globals.ZZ = (double*)malloc(sizeof(double) * (size_t)n_snaps);
+  memcpy(run_globals.ZZ, zz, sizeof(double) * (size_t)n_snaps);
+  run_globals.ListOutputSnaps = (int*)malloc(sizeof(int));
+  run_globals.ListOutputSnaps[0] = n_snaps - 1;
+  run_globals.NOutputSnaps = 1;
+  run_globals.NStoreSnapshots = 1;
+
+  if (rp->Flag_IncludeSpinTemp)
+    run_globals.NstoreSnapshots_SFR = set_sfr_history();
+  malloc_reionization_grids();
+  if (rp->Flag_IncludeRecombinations)
+    init_MHR();
+  g_ready = 1;
+  return 0;
+}
+
+int mxref_n_sfr_histories(void) { return run_globals.NstoreSnapshots_SFR; }
+
+float* mxref_grid(const char* name)
+{
+  reion_grids_t* g = &run_globals.reion_grids;
+#define G(n)                                                                                                           \
+  if (!strcmp(name, #n))                                                                                               \
+    return (float*)g->n;
+  G(deltax) G(stars) G(weighted_sfr) G(sfr) G(sfr_histories) G(N_rec) G(x_e_box) G(x_e_box_prev) G(Tk_box)
+  G(TS_box) G(xH) G(z_at_ionization) G(r_bubble) G(J_21) G(J_21_at_ionization) G(Gamma12) G(delta_T) G(vel)
+#undef G
+  return NULL;
+}
+
+void mxref_globals(mx_globals* out)
+{
+  reion_grids_t* g = &run_globals.reion_grids;
+  memset(out, 0, sizeof(*out));
+  out->volume_weighted_global_xH = g->volume_weighted_global_xH;
+  out->volume_weighted_global_J_21 = g->volume_weighted_global_J_21;
+  out->mass_weighted_global_xH = g->mass_weighted_global_xH;
+  out->volume_ave_J_alpha = g->volume_ave_J_alpha;
+  out->volume_ave_xalpha = g->volume_ave_xalpha;
+  out->volume_ave_Xheat = g->volume_ave_Xheat;
+  out->volume_ave_Xion = g->volume_ave_Xion;
+  out->volume_ave_TS = g->volume_ave_TS;
+  out->volume_ave_TK = g->volume_ave_TK;
+  out->volume_ave_xe = g->volume_ave_xe;
+  out->volume_ave_Tb = g->volume_ave_Tb;
+  out->x_e_ave = x_e_ave;
+}
+
+double mxref_stored_fcoll(int snapshot) { return stored_fcoll[snapshot]; }
+
+int mxref_find_HII_bubbles(int snapshot)
+{
+  timer_info t;
+  timer_start(&t);
+  find_HII_bubbles(snapshot, &t);
+  return 0;
+}
+
+int mxref_ComputeTs(int snapshot)
+{
+  timer_info t;
+  timer_start(&t);
+  ComputeTs(snapshot, &t);
+  return 0;
+}
+
+int mxref_delta_T(int snapshot)
+{
+  ComputeBrightnessTemperatureBox(snapshot);
+  return 0;
+}
+
+/* Selected physics helpers of the reference, exposed for table-level tests. */
+double mxref_splined_recombination_rate(double z_eff, double gamma12) { return splined_recombination_rate(z_eff, gamma12); }
+double mxref_dtdz(float z) { return dtdz(z); }
+double mxref_RtoM(double R) { return RtoM(R); }

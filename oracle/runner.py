@@ -1,0 +1,216 @@
+"""Python drivers for the oracle libraries — TEST INFRASTRUCTURE ONLY."""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Dict, Optional
+
+import numpy as np
+
+from meraxes_gb300.params import GRID_NAMES, MxGlobals, MxGrids, ReionParams
+
+ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libmxoracle.so")
+REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libmxref.so")
+REF_SRC = os.environ.get("MX_REFERENCE_SRC", "/root/reference/src")
+
+
+def build_oracle(force: bool = False) -> str:
+    if force or not os.path.exists(ORACLE_LIB) or _stale(ORACLE_LIB, ["mx_oracle.c", "mx_numerics.c", "mx_oracle.h"]):
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "oracle"], check=True)
+    return ORACLE_LIB
+
+
+def ref_available() -> bool:
+    return os.path.isdir(os.path.join(REF_SRC, "core"))
+
+
+def build_ref(force: bool = False) -> Optional[str]:
+    if not ref_available():
+        return None
+    if force or not os.path.exists(REF_LIB) or _stale(REF_LIB, ["ref_driver.c", "ref_shims.c", "mx_numerics.c"]):
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref", f"REF_SRC={REF_SRC}"], check=True)
+    return REF_LIB
+
+
+def _stale(lib: str, srcs) -> bool:
+    t = os.path.getmtime(lib)
+    return any(os.path.getmtime(os.path.join(ORACLE_DIR, s)) > t for s in srcs)
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class OracleBackend:
+    """The C restatement, operating in place on a dict of numpy grids."""
+
+    kind = "port"
+
+    def __init__(self, params: ReionParams, redshifts, tables_dir: str):
+        self.lib = ctypes.CDLL(build_oracle())
+        L = self.lib
+        L.mxo_create.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
+        L.mxo_destroy.argtypes = [ctypes.c_void_p]
+        L.mxo_set_redshifts.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        L.mxo_n_sfr_histories.argtypes = [ctypes.c_void_p]
+        for fn in ("mxo_find_HII_bubbles", "mxo_ComputeTs", "mxo_delta_T"):
+            getattr(L, fn).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.mxo_last_margin.argtypes = [ctypes.c_void_p]
+        L.mxo_last_margin.restype = ctypes.POINTER(ctypes.c_float)
+        L.mxo_last_freq_tables.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        L.mxo_last_freq_tables.restype = ctypes.POINTER(ctypes.c_double)
+        L.mxo_recombination_rate_splined.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
+        L.mxo_recombination_rate_splined.restype = ctypes.c_double
+        L.mxo_get_Ts.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                 ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
+        L.mxo_get_Ts.restype = ctypes.c_double
+        self.params = params
+        self._pc = params.to_ctypes()
+        self.ctx = ctypes.c_void_p()
+        rc = L.mxo_create(ctypes.byref(self._pc), tables_dir.encode(), ctypes.byref(self.ctx))
+        if rc != 0:
+            raise RuntimeError(f"mxo_create failed ({rc})")
+        zz = (ctypes.c_double * len(redshifts))(*redshifts)
+        L.mxo_set_redshifts(self.ctx, zz, len(redshifts))
+        self.n_sfr_histories = L.mxo_n_sfr_histories(self.ctx)
+
+    def close(self):
+        if self.ctx:
+            self.lib.mxo_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _grids(state: Dict[str, np.ndarray]) -> MxGrids:
+        g = MxGrids()
+        for n in GRID_NAMES:
+            a = state.get(n)
+            if a is not None:
+                assert a.dtype == np.float32 and a.flags.c_contiguous, n
+                setattr(g, n, a.ctypes.data)
+        return g
+
+    def _call(self, fn: str, snapshot: int, state) -> Dict[str, float]:
+        g = self._grids(state)
+        out = MxGlobals()
+        rc = getattr(self.lib, fn)(self.ctx, snapshot, ctypes.byref(g), ctypes.byref(out))
+        if rc != 0:
+            raise RuntimeError(f"{fn} failed ({rc})")
+        return out.as_dict()
+
+    def find_HII_bubbles(self, snapshot: int, state) -> Dict[str, float]:
+        return self._call("mxo_find_HII_bubbles", snapshot, state)
+
+    def ComputeTs(self, snapshot: int, state) -> Dict[str, float]:
+        return self._call("mxo_ComputeTs", snapshot, state)
+
+    def delta_T(self, snapshot: int, state) -> Dict[str, float]:
+        return self._call("mxo_delta_T", snapshot, state)
+
+    def margin(self) -> np.ndarray:
+        D = self.params.grid_dim
+        p = self.lib.mxo_last_margin(self.ctx)
+        return np.ctypeslib.as_array(p, shape=(D, D, D)).copy()
+
+    def freq_tables(self) -> np.ndarray:
+        n = ctypes.c_int()
+        p = self.lib.mxo_last_freq_tables(self.ctx, ctypes.byref(n))
+        return np.ctypeslib.as_array(p, shape=(3, 14, n.value)).copy()
+
+    def step(self, snapshot: int, state) -> Dict[str, float]:
+        """ComputeTs -> find_HII_bubbles -> delta_T (dracarys.c:352-390)."""
+        out: Dict[str, float] = {}
+        if self.params.flag_spin_temp:
+            out.update(self.ComputeTs(snapshot, state))
+        out.update({k: v for k, v in self.find_HII_bubbles(snapshot, state).items()
+                    if k in ("volume_weighted_global_xH", "volume_weighted_global_J_21", "mass_weighted_global_xH",
+                             "n_radii")})
+        if self.params.flag_21cm:
+            out["volume_ave_Tb"] = self.delta_T(snapshot, state)["volume_ave_Tb"]
+        return out
+
+
+class RefBackend:
+    """The reference's own sources (compiled with shims); one instance per
+    process because the reference keeps its state in globals."""
+
+    kind = "reference"
+    _instance = None
+
+    def __init__(self, params: ReionParams, redshifts, tables_dir: str):
+        lib = build_ref()
+        if lib is None:
+            raise RuntimeError("reference tree not available")
+        self.lib = ctypes.CDLL(lib, mode=ctypes.RTLD_LOCAL)
+        L = self.lib
+        L.mxref_init.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_char_p]
+        L.mxref_grid.argtypes = [ctypes.c_char_p]
+        L.mxref_grid.restype = ctypes.POINTER(ctypes.c_float)
+        L.mxref_globals.argtypes = [ctypes.c_void_p]
+        L.mxref_stored_fcoll.restype = ctypes.c_double
+        L.mxref_splined_recombination_rate.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.mxref_splined_recombination_rate.restype = ctypes.c_double
+        self.params = params
+        self._pc = params.to_ctypes()
+        zz = (ctypes.c_double * len(redshifts))(*redshifts)
+        L.mxref_init(ctypes.byref(self._pc), zz, len(redshifts), tables_dir.encode())
+        self.n_sfr_histories = L.mxref_n_sfr_histories()
+
+    def _view(self, name: str, n: int) -> Optional[np.ndarray]:
+        p = self.lib.mxref_grid(name.encode())
+        if not p:
+            return None
+        return np.ctypeslib.as_array(p, shape=(n,))
+
+    def _sync_in(self, state):
+        for n, a in state.items():
+            if n not in GRID_NAMES or a is None:
+                continue
+            v = self._view(n, a.size)
+            if v is not None:
+                v[:] = a.ravel()
+
+    def _sync_out(self, state):
+        for n, a in state.items():
+            if n not in GRID_NAMES or a is None:
+                continue
+            v = self._view(n, a.size)
+            if v is not None:
+                a.reshape(-1)[:] = v
+
+    def _run(self, fn, snapshot, state):
+        self._sync_in(state)
+        getattr(self.lib, fn)(snapshot)
+        self._sync_out(state)
+        g = MxGlobals()
+        self.lib.mxref_globals(ctypes.byref(g))
+        d = g.as_dict()
+        d["collapse_fraction"] = self.lib.mxref_stored_fcoll(snapshot)
+        return d
+
+    def find_HII_bubbles(self, snapshot, state):
+        return self._run("mxref_find_HII_bubbles", snapshot, state)
+
+    def ComputeTs(self, snapshot, state):
+        return self._run("mxref_ComputeTs", snapshot, state)
+
+    def delta_T(self, snapshot, state):
+        return self._run("mxref_delta_T", snapshot, state)
+
+    def step(self, snapshot, state):
+        out = {}
+        if self.params.flag_spin_temp:
+            out.update(self.ComputeTs(snapshot, state))
+        r = self.find_HII_bubbles(snapshot, state)
+        for k in ("volume_weighted_global_xH", "volume_weighted_global_J_21", "mass_weighted_global_xH"):
+            out[k] = r[k]
+        if self.params.flag_21cm:
+            out["volume_ave_Tb"] = self.delta_T(snapshot, state)["volume_ave_Tb"]
+        return out

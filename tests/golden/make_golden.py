@@ -1,0 +1,68 @@
+"""Regenerates the golden fixtures in tests/golden/ from the reference itself.
+
+The reference's own reionization sources (src/core/*.c of meraxes) are
+compiled unmodified against the shims in oracle/shims/ (`make -C oracle ref`,
+which needs the reference tree) and run on the seeded synthetic cases of
+tests/cases.py.  Each fixture stores the inputs of every snapshot, the final
+grids and the per-snapshot global scalars.
+
+    python tests/golden/make_golden.py            # all cases
+    python tests/golden/make_golden.py full24     # one case
+
+Each case runs in a fresh process because the reference keeps its state in
+globals.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+
+def make_one(name: str):
+    import numpy as np
+
+    from cases import CASES, OUTPUT_GRIDS, initial
+    from meraxes_gb300 import synthetic as syn
+    from oracle import RefBackend
+
+    case = CASES[name]
+    w = case.workload()
+    ref = RefBackend(w.params, w.redshifts, syn.TABLES_DIR)
+    gen = syn.FieldGenerator(w)
+    st = initial(w, ref.n_sfr_histories)
+    arrays = {}
+    for k, v in st.items():
+        arrays["init/" + k] = v.copy()
+    glob = []
+    for s in w.snapshots:
+        inp = gen.inputs(s, ref.n_sfr_histories)
+        for k, v in inp.items():
+            arrays[f"in{s}/{k}"] = v.copy()
+        st.update(inp)
+        glob.append(ref.step(s, st))
+    for k in OUTPUT_GRIDS:
+        if k in st and st[k] is not None:
+            arrays["out/" + k] = st[k]
+    meta = {"case": name, "snapshots": w.snapshots, "redshifts": w.redshifts, "globals": glob,
+            "n_sfr_histories": ref.n_sfr_histories, "grid_dim": w.params.grid_dim}
+    arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
+    print(name, "written")
+
+
+if __name__ == "__main__":
+    from cases import CASES
+
+    names = sys.argv[1:] or list(CASES)
+    if len(names) == 1:
+        make_one(names[0])
+    else:
+        for n in names:
+            subprocess.run([sys.executable, os.path.abspath(__file__), n], check=True)

@@ -1,0 +1,125 @@
+"""CUDA path against the oracle and the reference fixtures (GB300)."""
+import os
+
+import numpy as np
+import pytest
+
+from cases import CASES, Case, OUTPUT_GRIDS, run_case
+from compare import compare
+from test_oracle_golden import golden_inputs, load_golden, run_on
+
+pytestmark = pytest.mark.gpu
+
+
+class GpuBackend:
+    """The product through its host-pointer C ABI entry point mx_step."""
+
+    def __init__(self, params, redshifts):
+        from meraxes_gb300.api import ReionGridStep
+
+        self.step_obj = ReionGridStep(params, redshifts)
+        self.n_sfr_histories = self.step_obj.n_sfr_histories
+        self.launches = []
+
+    def step(self, snapshot, state):
+        g = self.step_obj.step(snapshot, state)
+        self.launches.append(self.step_obj.last_launches)
+        return g
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_gpu_matches_reference_fixture(name):
+    d, meta = load_golden(name)
+    w = CASES[name].workload()
+    init, per, out = golden_inputs(d, meta)
+    gpu = GpuBackend(w.params, meta["redshifts"])
+    assert gpu.n_sfr_histories == meta["n_sfr_histories"]
+    st, glob = run_on(gpu, meta, init, per)
+    assert all(n > 0 for n in gpu.launches)
+    rep = {}
+    compare(out, st, meta["globals"][-1], glob[-1], report=rep)
+    print(name, rep)
+
+
+@pytest.mark.parametrize("name,D", [("plain32_tophat", 64), ("plain32_sharpk", 64), ("plain32_gauss", 48),
+                                    ("full24", 48), ("evolve16", 32)])
+def test_gpu_matches_oracle_with_margins(name, D, tables_dir):
+    from meraxes_gb300 import synthetic as syn
+    from oracle import OracleBackend
+
+    c = CASES[name]
+    case = Case(name, c.base, D, c.overrides, c.fesc, c.snapshots)
+    w = case.workload()
+    orc = OracleBackend(w.params, w.redshifts, tables_dir)
+    gpu = GpuBackend(w.params, w.redshifts)
+    gen = syn.FieldGenerator(w)
+    from cases import initial
+
+    sa = initial(w, orc.n_sfr_histories)
+    sb = {k: v.copy() for k, v in sa.items()}
+    for s in w.snapshots:
+        inp = gen.inputs(s, orc.n_sfr_histories)
+        sa.update({k: v.copy() for k, v in inp.items()})
+        sb.update({k: v.copy() for k, v in inp.items()})
+        ga = orc.step(s, sa)
+        margin = orc.margin()
+        gb = gpu.step(s, sb)
+        rep = {}
+        compare(sa, sb, ga, gb, margin=margin, report=rep)
+    print(name, D, rep)
+
+
+def test_device_entry_points_match_host_entry_points():
+    import torch
+
+    from cases import initial
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+
+    w = CASES["full24"].workload()
+    host = ReionGridStep(w.params, w.redshifts)
+    dev = ReionGridStep(w.params, w.redshifts)
+    gen = syn.FieldGenerator(w)
+    s = w.snapshots[0]
+    st = initial(w, host.n_sfr_histories)
+    st.update(gen.inputs(s, host.n_sfr_histories))
+    tst = {k: torch.from_numpy(v.copy()).cuda() for k, v in st.items()}
+    gh = host.step(s, st)
+    gd = dev.step(s, tst)
+    torch.cuda.synchronize()
+    for k in OUTPUT_GRIDS:
+        if k in st:
+            assert np.array_equal(st[k], tst[k].cpu().numpy()), k
+    for k in ("volume_weighted_global_xH", "volume_ave_TS", "volume_ave_Tb"):
+        assert gh[k] == gd[k]
+
+
+def test_errors_are_reported_not_raised_on_device():
+    from meraxes_gb300 import _lib
+    from meraxes_gb300.api import ReionGridStep
+
+    w = CASES["plain32_tophat"].workload()
+    st = ReionGridStep(w.params, w.redshifts)
+    with pytest.raises(_lib.MxError) as e:
+        st.find_HII_bubbles(99, {"deltax": np.zeros(1, np.float32)})
+    assert e.value.code == -1
+    with pytest.raises(_lib.MxError) as e:
+        st.find_HII_bubbles(1, {})
+    assert e.value.code == -1
+    # the context stays usable after an error
+    from cases import initial
+    from meraxes_gb300 import synthetic as syn
+
+    gen = syn.FieldGenerator(w)
+    s = w.snapshots[0]
+    g = initial(w, 0)
+    g.update(gen.inputs(s, 0))
+    out = st.step(s, g)
+    assert 0.0 <= out["volume_weighted_global_xH"] <= 1.0

@@ -1,0 +1,68 @@
+"""The C restatement (oracle) against the golden fixtures produced by the
+reference's own sources (tests/golden/make_golden.py)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from cases import CASES, OUTPUT_GRIDS
+from compare import compare
+from meraxes_gb300 import synthetic as syn
+from oracle import OracleBackend
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_golden(name):
+    d = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    meta = json.loads(bytes(d["meta"]).decode())
+    return d, meta
+
+
+def golden_inputs(d, meta):
+    init = {k[5:]: np.array(d[k]) for k in d.files if k.startswith("init/")}
+    per = {}
+    for s in meta["snapshots"]:
+        per[s] = {k.split("/", 1)[1]: np.array(d[k]) for k in d.files if k.startswith(f"in{s}/")}
+    out = {k[4:]: np.array(d[k]) for k in d.files if k.startswith("out/")}
+    return init, per, out
+
+
+def run_on(backend, meta, init, per):
+    st = {k: v.copy() for k, v in init.items()}
+    glob = []
+    for s in meta["snapshots"]:
+        st.update({k: v.copy() for k, v in per[s].items()})
+        glob.append(backend.step(s, st))
+    return st, glob
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_oracle_reproduces_reference_fixture(name, tables_dir):
+    d, meta = load_golden(name)
+    w = CASES[name].workload()
+    init, per, out = golden_inputs(d, meta)
+    orc = OracleBackend(w.params, meta["redshifts"], tables_dir)
+    assert orc.n_sfr_histories == meta["n_sfr_histories"]
+    st, glob = run_on(orc, meta, init, per)
+    # same FFT and numerics restatement on both sides: agreement to FP32
+    # rounding of differently compiled arithmetic (bit-exact on the machine
+    # that generated the fixtures)
+    for k in OUTPUT_GRIDS:
+        if k in out:
+            a, b = out[k].astype(np.float64), st[k].astype(np.float64)
+            err = np.abs(a - b) / np.maximum(np.abs(a), 1e-30 + 1e-6 * np.abs(a).max())
+            assert err.max() < 1e-5, (k, err.max())
+    for g_ref, g_orc in zip(meta["globals"], glob):
+        for k, v in g_ref.items():
+            if k in g_orc and k not in ("n_radii", "gpu_launches") and v != 0:
+                assert abs(g_orc[k] - v) <= 1e-6 * abs(v), (k, v, g_orc[k])
+
+
+def test_fixture_cases_cover_the_paths():
+    seen = {CASES[n].workload().params.filter_type for n in CASES}
+    assert seen == {0, 1, 2}
+    assert any(CASES[n].workload().params.flag_recombinations for n in CASES)
+    assert any(CASES[n].workload().params.flag_spin_temp for n in CASES)
+    assert any(len(CASES[n].workload().snapshots) > 1 for n in CASES)

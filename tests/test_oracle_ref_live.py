@@ -1,0 +1,47 @@
+"""Live check of the restatement against the reference's own sources compiled
+with the shims (only where the reference tree is present)."""
+import subprocess
+import sys
+import os
+
+import pytest
+
+from oracle import ref_available
+
+pytestmark = pytest.mark.skipif(not ref_available(), reason="reference tree not present")
+
+SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r}); sys.path.insert(0, {tests!r})
+from cases import Case, run_case, OUTPUT_GRIDS
+from meraxes_gb300 import synthetic as syn
+from oracle import OracleBackend, RefBackend
+c = Case('live', {base!r}, {D}, {ov!r}, fesc={fesc})
+w = c.workload()
+ref = RefBackend(w.params, w.redshifts, syn.TABLES_DIR)
+orc = OracleBackend(w.params, w.redshifts, syn.TABLES_DIR)
+a, ga = run_case(ref, w)
+b, gb = run_case(orc, w)
+bad = []
+for k in OUTPUT_GRIDS:
+    if k in a and a[k] is not None and not np.array_equal(a[k], b[k], equal_nan=True):
+        bad.append(k)
+for x, y in zip(ga, gb):
+    for k in x:
+        if k in y and k not in ('n_radii', 'gpu_launches') and x[k] != y[k] and abs(x[k]-y[k]) > 1e-14*abs(x[k]):
+            bad.append(k)
+print('MISMATCH' if bad else 'OK', bad)
+"""
+
+
+@pytest.mark.parametrize("base,D,ov,fesc", [
+    ("plain_64", 16, {"reion_efficiency": 2000.0, "delta_r_factor": 1.3}, 1.0),
+    ("plain_64", 20, {"reion_efficiency": 5000.0, "filter_type": 1, "uvb_flag": 0}, 1.0),
+    ("full_256", 16, {"reion_efficiency": 31043.0, "clumping_factor": 2.0, "filter_type": 2}, 0.02),
+])
+def test_restatement_bit_exact_against_reference(base, D, ov, fesc):
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = SCRIPT.format(root=os.path.dirname(here), tests=here, base=base, D=D, ov=ov, fesc=fesc)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip().startswith("OK"), r.stdout
