@@ -1,0 +1,482 @@
+#!/usr/bin/env python3
+"""Benchmark of the per-snapshot reionization grid step on GB300.
+
+Workload (evolve_512): 512^3 cells, L = 200 Mpc/h, seed 2, fields grown
+linearly with the growth factor over 20 snapshots z = 15 -> 6; every snapshot
+runs the full step ComputeTs (40 shells) -> find_HII_bubbles (recombinations,
+41 radii, 5 fields) -> 21 cm brightness temperature.  A benchmark "step" is one
+snapshot.  Inputs are seeded synthetic grids (no simulation data).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is ms per snapshot with the inputs resident in
+HBM (device entry points); `e2e` is the same metric through the host-pointer
+entry point mx_step with pinned host buffers (copies inside the timed
+region); `roofline` reports the dominant kernel's achieved HBM bandwidth from
+CUDA events; `cpu_baseline` is the CPU oracle on the host cores.  With N > 1
+(torchrun) the ranks run independent replicas (no data exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "ms/snapshot at 512^3 (ComputeTs + find_HII_bubbles + 21cm box)"
+UNIT = "ms/snapshot"
+REION_EFF = 1.0 / 0.15714 * 4000.0 / (1.0 - 0.75 * 0.24)
+FESC = 0.01
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--grid", type=int, default=512)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample-grid", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload_for(grid: int):
+    from meraxes_gb300.params import workload
+
+    w = workload("evolve_512", grid if grid != 512 else None)
+    w.params.reion_efficiency = REION_EFF
+    w.fesc = FESC
+    return w
+
+
+# ----------------------------------------------------------------- distributed
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world: int, backend: str):
+    import torch.distributed as dist
+
+    if world > 1 and not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- synthetic
+def make_device_fields(w, snapshots, device):
+    """Seeded inputs of the given snapshots, generated on the GPU with the
+    recipe of meraxes_gb300.synthetic (PCG64 white noise, P(k) filtering,
+    growth-factor scaling, stellar mass and SFR grids) in the PADDED layout."""
+    import torch
+
+    from meraxes_gb300.params import growth_factor, sfr_timescale_internal_myr
+
+    p = w.params
+    D, L = p.grid_dim, p.box_size
+    H = D // 2 + 1
+    rng = np.random.default_rng(w.seed)
+    noise = torch.from_numpy(rng.standard_normal((D, D, D))).to(device)
+    fk = torch.fft.rfftn(noise)
+    del noise
+    kf = 2.0 * np.pi / L
+    kx = torch.fft.fftfreq(D, d=1.0 / D, device=device, dtype=torch.float64) * kf
+    kz = torch.fft.rfftfreq(D, d=1.0 / D, device=device, dtype=torch.float64) * kf
+    k2 = kx[:, None, None] ** 2 + kx[None, :, None] ** 2 + kz[None, None, :] ** 2
+    kny = np.pi * D / L
+    pk = torch.where(k2 > 0, torch.exp(-k2 / kny ** 2) / torch.where(k2 > 0, k2, torch.ones_like(k2)),
+                     torch.zeros_like(k2))
+    fk *= torch.sqrt(pk)
+    del pk, k2
+    base = torch.fft.irfftn(fk, s=(D, D, D))
+    del fk
+    base *= 0.6 / base.std()
+    d_norm = growth_factor(w.redshifts[w.snapshots[-1]], p)
+    t20 = sfr_timescale_internal_myr(20.0, p)
+    out = {}
+    for s in snapshots:
+        d = torch.clamp(base * (growth_factor(w.redshifts[s], p) / d_norm), min=-0.99).float()
+        dd = d.double()
+        stars = torch.where(dd > 0.5, 1e-3 * torch.exp(2.0 * dd), torch.zeros_like(dd))
+        sfr = (stars / t20).float()
+        grids = {}
+        for name, val in (("deltax", d), ("stars", (w.fesc * stars.float().double()).float()),
+                          ("weighted_sfr", (w.fesc * sfr.double()).float()), ("sfr", sfr)):
+            t = torch.zeros((D, D, 2 * H), dtype=torch.float32, device=device)
+            t[:, :, :D] = val
+            grids[name] = t
+        out[s] = grids
+        del d, dd, stars
+    del base
+    return out
+
+
+def history_buffer(fields, snapshots, n_hist, D, device):
+    """All SFR grids in reverse snapshot order, so that the contiguous slices
+    [s-0, s-1, ...] for any snapshot are a view (padded with zero slices)."""
+    import torch
+
+    H = D // 2 + 1
+    P = D * D * 2 * H
+    smax = max(snapshots)
+    buf = torch.zeros((smax + 1 + n_hist, P), dtype=torch.float32, device=device)
+    for s in snapshots:
+        buf[smax - s] = fields[s]["sfr"].reshape(-1)
+    return buf, smax
+
+
+def state_grids(p, z_prev, device):
+    import torch
+
+    from meraxes_gb300 import synthetic as syn
+
+    st = syn.initial_state(p, z_prev)
+    return {k: torch.from_numpy(v).to(device) for k, v in st.items()}
+
+
+# -------------------------------------------------------------------- arms
+def run_gb300(args, rank, world, local):
+    import torch
+
+    from meraxes_gb300.api import ReionGridStep
+
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    init_dist(world, "nccl")
+    w = workload_for(args.grid)
+    p = w.params
+    D = p.grid_dim
+    n_snap = len(w.redshifts)
+    total = args.warmup + args.steps
+    order = [i % n_snap for i in range(total)]
+    used = sorted(set(order))
+    fields = make_device_fields(w, used, device)
+    from meraxes_gb300.params import ReionParams  # noqa: F401
+
+    step = ReionGridStep(p, w.redshifts)
+    n_hist = step.n_sfr_histories
+    hist, smax = history_buffer(fields, used, n_hist, D, device)
+    state = state_grids(p, w.redshifts[0], device)
+
+    def grids_for(s):
+        g = dict(state)
+        g.update(fields[s])
+        g["sfr_histories"] = hist[smax - s: smax - s + n_hist]
+        return g
+
+    # warm-up (also the first snapshots of the evolution)
+    for i in range(args.warmup):
+        step.step(order[i], grids_for(order[i]))
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    step.profile(True)
+    launches = 0
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0.record()
+    glob = None
+    for i in range(args.warmup, total):
+        glob = step.step(order[i], grids_for(order[i]))
+        launches += step.last_launches
+    t1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = t0.elapsed_time(t1)
+    clk = clocks.stop()
+    kstats = step.profile_read()
+    step.profile(False)
+    ms_max = max_over_ranks(ms, world, device)
+    value = ms_max / (args.steps * world)
+
+    # per-kernel achieved bandwidth (algorithmic bytes / event time)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    kernels = {}
+    for name, (n, kms, b) in kstats.items():
+        kernels[name] = {"launches": n, "ms_per_launch": kms / max(n, 1), "share": kms / max(ms, 1e-9),
+                         "gbs": (b / 1e9) / (kms / 1e3) if kms > 0 else None}
+    dom = max(kstats.items(), key=lambda kv: kv[1][1]) if kstats else None
+    roofline = None
+    if dom:
+        name, (n, kms, b) = dom
+        achieved = (b / n / 1e9) / (kms / n / 1e3)
+        roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": hbm_peak,
+                    "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
+                    "peak_source": peak_src, "algorithmic_bytes_per_launch": b / n}
+    # whole-step algorithmic bandwidth
+    total_bytes = sum(v[2] for v in kstats.values())
+    step_gbs = (total_bytes / args.steps / 1e9) / (value * world / 1e3)
+
+    # ------------------------------------------------------------------ e2e
+    e2e = None
+    if not args.no_e2e and args.e2e_steps > 0:
+        e2e = run_e2e(args, step, w, fields, used, n_hist, device, world)
+
+    del fields, hist, state
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 grids/FFTs, f64 tables and reductions",
+        "data": "synthetic (seeded Gaussian density, stellar and SFR grids)",
+        "config": {"workload": f"evolve_512: {D}^3, L={p.box_size} Mpc/h, 20 snapshots z=15..6, "
+                               "ComputeTs 40 shells + find_HII_bubbles 41 radii x 5 fields + 21cm box",
+                   "grid": D, "snapshots_timed": [order[i] for i in range(args.warmup, total)],
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (each grid 0.54 GB at 512^3)"},
+        "gpu_launches": launches, "clocks": clk, "roofline": roofline, "step_algorithmic_gbs": round(step_gbs, 1),
+        "kernels": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+                    for k, v in kernels.items()},
+        "last_globals": {k: glob[k] for k in ("volume_weighted_global_xH", "volume_ave_TS", "volume_ave_Tb")},
+    }
+    if e2e:
+        out["e2e"] = e2e
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args)
+    return out, rank
+
+
+def run_e2e(args, step, w, fields, used, n_hist, device, world):
+    """Same metric through mx_step with pinned host buffers: every step copies
+    that step's inputs and state host->device and all outputs back."""
+    import torch
+
+    from meraxes_gb300.params import PADDED_GRIDS
+
+    p = w.params
+    D = p.grid_dim
+    s = used[-1]
+    host = {}
+    for k, v in fields[s].items():
+        host[k] = v.cpu().pin_memory().numpy()
+    st = state_grids(p, w.redshifts[max(s - 1, 0)], "cpu")
+    for k, v in st.items():
+        host[k] = v.pin_memory().numpy()
+    if n_hist > 0:
+        h = torch.zeros((n_hist, D * D * 2 * (D // 2 + 1)), dtype=torch.float32).pin_memory()
+        h[0] = fields[s]["sfr"].reshape(-1).cpu()
+        host["sfr_histories"] = h.numpy()
+    in_names = ["deltax", "stars", "weighted_sfr", "x_e_box", "N_rec", "z_at_ionization", "J_21_at_ionization",
+                "Gamma12", "sfr", "x_e_box_prev", "Tk_box"]
+    out_names = ["N_rec", "xH", "z_at_ionization", "r_bubble", "J_21", "J_21_at_ionization", "Gamma12", "sfr",
+                 "x_e_box", "x_e_box_prev", "Tk_box", "TS_box", "delta_T"]
+    nb = lambda n: host[n].nbytes  # noqa: E731
+    h2d = sum(nb(n) for n in in_names if n in host) + (host["sfr_histories"].nbytes if n_hist > 0 else 0)
+    d2h = sum(nb(n) for n in out_names if n in host)
+    step.step(s, host)  # first host call allocates the device mirror
+    torch.cuda.synchronize()
+    barrier(world)
+    t = 0.0
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        step.step(s, host)
+        t += time.perf_counter() - t0
+    ms = max_over_ranks(t * 1e3, world, device)
+    return {"value": round(ms / (args.e2e_steps * world), 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps, "entry_point": "mx_step (host pointers)"}
+
+
+def cpu_sample(grid_s: int, threads: int):
+    """One full snapshot of the oracle at grid_s^3 with the evolve_512 cell size
+    (and its filter radii, shells and physics), timed on the host cores."""
+    from cases import initial
+    from meraxes_gb300 import synthetic as syn
+    from oracle import OracleBackend
+
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    w = workload_for(grid_s)
+    orc = OracleBackend(w.params, w.redshifts, syn.TABLES_DIR)
+    gen = syn.FieldGenerator(w)
+    s = 10
+    st = syn.initial_state(w.params, w.redshifts[s - 1])
+    st.update(gen.inputs(s, orc.n_sfr_histories))
+    t0 = time.perf_counter()
+    orc.step(s, st)
+    return time.perf_counter() - t0
+
+
+def cpu_extrapolate(samples, grid: int):
+    """Fits t(D) = a + b * D^3 log2(D^3) to timed samples (fixed per-snapshot
+    table work + grid work) and evaluates it at `grid`."""
+    xs = np.array([d ** 3 * np.log2(d ** 3) for d, _ in samples], dtype=np.float64)
+    ts = np.array([t for _, t in samples], dtype=np.float64)
+    if len(samples) >= 2:
+        b = (ts[-1] - ts[0]) / (xs[-1] - xs[0])
+        b = max(b, ts[-1] / xs[-1] * 0.5)
+        a = max(ts[-1] - b * xs[-1], 0.0)
+    else:
+        a, b = 0.0, ts[0] / xs[0]
+    x = grid ** 3 * np.log2(grid ** 3)
+    return a + b * x, a, b
+
+
+def cpu_samples(grid_s: int, threads: int):
+    code = (f"import sys; sys.path.insert(0, {ROOT!r}); sys.path.insert(0, {os.path.join(ROOT, 'tests')!r});"
+            "import bench; print(bench.cpu_sample(%d, %d))")
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    out = []
+    for d in (grid_s // 2, grid_s):
+        r = subprocess.run([sys.executable, "-c", code % (d, threads)], capture_output=True, text=True, env=env,
+                           timeout=1800)
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr[-500:])
+        out.append((d, float(r.stdout.strip().split()[-1])))
+    return out
+
+
+def cpu_baseline(args):
+    threads = os.cpu_count() or 1
+    try:
+        samples = cpu_samples(args.cpu_sample_grid, threads)
+    except Exception as e:  # noqa: BLE001
+        return {"value": None, "unit": UNIT, "error": str(e)[-300:]}
+    t, a, b = cpu_extrapolate(samples, args.grid)
+    desc = ", ".join(f"{d}^3: {ts:.2f} s" for d, ts in samples)
+    return {"value": round(t * 1e3, 1), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle (C restatement, OpenMP on all host threads) full step of snapshot 10 of evolve_512 "
+                      f"with its cell size at {desc}; extrapolated to {args.grid}^3 by t = a + b N log2 N "
+                      f"(a = {a:.2f} s per-snapshot tables, b fitted)"}
+
+
+def run_reference(args, rank, world):
+    """The CPU implementation of the path (the oracle port: the reference's
+    own build needs FFTW/GSL/MPI/HDF5 and the reference tree, absent on the
+    GPU host) on all host threads, on bounded samples of the workload."""
+    if rank != 0:
+        return None, rank
+    threads = os.cpu_count() or 1
+    vals = []
+    samples = None
+    for i in range(args.warmup + args.steps):
+        try:
+            samples = cpu_samples(args.cpu_sample_grid, threads)
+        except Exception as e:  # noqa: BLE001
+            return {"impl": "reference", "unavailable": "oracle port failed: " + str(e)[-300:]}, rank
+        if i >= args.warmup:
+            vals.append(cpu_extrapolate(samples, args.grid)[0])
+    value = statistics.mean(vals) * 1e3
+    desc = ", ".join(f"{d}^3: {ts:.2f} s" for d, ts in samples)
+    sample = (f"per step: oracle port full step of snapshot 10 of evolve_512 (its cell size) at {desc}; "
+              f"extrapolated to {args.grid}^3 by t = a + b N log2 N")
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 1), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 grids, f64 FFT internals and physics",
+            "data": "synthetic", "config": {"workload": f"evolve_512 at {args.grid}^3 (sampled)"},
+            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}, rank
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        out, rank = run_reference(args, rank, world)
+    else:
+        out, rank = run_gb300(args, rank, world, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+
+        if dist.is_initialized():
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -190,6 +190,22 @@ int mx_ComputeBrightnessTemperatureBox_device(mx_ctx* ctx,
                                               void* stream);
 int mx_step_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream);
 
+/* Per-kernel timing with CUDA events recorded on the launching stream around
+ * every kernel and cuFFT execution of the context.  No reference counterpart
+ * (the reference times whole calls with gettimeofday, utils.c:9-24).
+ * mx_profile_enable(ctx, 1) clears and starts collection; mx_profile_read
+ * synchronises the context stream, then fills up to `cap` entries (one per
+ * kernel name) and returns the number of distinct names. */
+typedef struct mx_kernel_stat
+{
+  char name[40];
+  int32_t launches;
+  double ms;    /* summed event time */
+  double bytes; /* summed algorithmic HBM bytes (reads + writes) */
+} mx_kernel_stat;
+int mx_profile_enable(mx_ctx* ctx, int32_t on);
+int32_t mx_profile_read(mx_ctx* ctx, mx_kernel_stat* out, int32_t cap);
+
 /* Build information: returns a static string. */
 const char* mx_build_info(void);
 

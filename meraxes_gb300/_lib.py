@@ -22,8 +22,15 @@ EXPORTS = [
     "mx_create", "mx_destroy", "mx_last_error", "mx_set_redshifts", "mx_n_sfr_histories", "mx_filter_radii",
     "mx_find_HII_bubbles", "mx_ComputeTs", "mx_ComputeBrightnessTemperatureBox", "mx_step",
     "mx_find_HII_bubbles_device", "mx_ComputeTs_device", "mx_ComputeBrightnessTemperatureBox_device",
-    "mx_step_device", "mx_build_info",
+    "mx_step_device", "mx_profile_enable", "mx_profile_read", "mx_build_info",
 ]
+
+
+class MxKernelStat(ctypes.Structure):
+    """ctypes image of `mx_kernel_stat` (include/mx_reion.h)."""
+
+    _fields_ = [("name", ctypes.c_char * 40), ("launches", ctypes.c_int32), ("ms", ctypes.c_double),
+                ("bytes", ctypes.c_double)]
 
 
 class MxError(RuntimeError):
@@ -69,6 +76,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                    "mx_step_device"):
             getattr(L, fn).argtypes = [P, ctypes.c_int32, ctypes.POINTER(MxGrids), ctypes.POINTER(MxGlobals), P]
             getattr(L, fn).restype = ctypes.c_int
+        L.mx_profile_enable.argtypes = [P, ctypes.c_int32]
+        L.mx_profile_enable.restype = ctypes.c_int
+        L.mx_profile_read.argtypes = [P, ctypes.POINTER(MxKernelStat), ctypes.c_int32]
+        L.mx_profile_read.restype = ctypes.c_int32
         L.mx_build_info.argtypes = []
         L.mx_build_info.restype = ctypes.c_char_p
         _LIB = L

@@ -104,6 +104,18 @@ class ReionGridStep:
         self.last_launches = out.gpu_launches
         return out.as_dict()
 
+    def profile(self, on: bool = True):
+        """Start (clear) or stop per-kernel CUDA-event timing."""
+        self._check(self.lib.mx_profile_enable(self.ctx, 1 if on else 0))
+
+    def profile_read(self):
+        """{kernel name: (launches, total ms, algorithmic bytes)}."""
+        buf = (_lib.MxKernelStat * 64)()
+        n = self.lib.mx_profile_read(self.ctx, buf, 64)
+        if n < 0:
+            self._check(n)
+        return {buf[i].name.decode(): (buf[i].launches, buf[i].ms, buf[i].bytes) for i in range(min(n, 64))}
+
     # --------------------------------------------------------- entry points
     def find_HII_bubbles(self, snapshot: int, grids) -> Dict[str, float]:
         return self._call("mx_find_HII_bubbles", snapshot, grids)

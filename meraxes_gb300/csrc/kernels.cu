@@ -206,23 +206,25 @@ __global__ void k_threshold(ThresholdArgs a, int D, int H, long long N)
     for (int r = 0; r < a.n_r; r++) {
       const RadiusParams rp = a.rp[r];
       const float* f = a.fields + (long long)r * a.G * a.P;
-      const float dx = fmaxf(f[ip], -1 + REL_TOL);
-      float st = fmaxf(f[a.P + ip], 0.0f);
+      const bool direct = rp.last != 0;
+      auto field = [&](int g) -> float { return direct ? a.direct[g][ip] : f[(long long)g * a.P + ip]; };
+      const float dx = fmaxf(field(0), -1 + REL_TOL);
+      float st = fmaxf(field(1), 0.0f);
       if (st < ABS_TOL)
         st = 0;
-      float ws = fmaxf(f[2 * a.P + ip], 0.0f);
+      float ws = fmaxf(field(2), 0.0f);
       if (ws < ABS_TOL)
         ws = 0;
       double rec = 0.0;
       if (a.recomb) {
-        float nr = fmaxf(f[(long long)a.idx_nr * a.P + ip], 0.0f);
+        float nr = fmaxf(field(a.idx_nr), 0.0f);
         if (nr < ABS_TOL)
           nr = 0;
         rec = (double)nr / (1.0 + (double)dx);
       }
       double nf = 1.0;
       if (a.spin) {
-        float xe = fmaxf(f[(long long)a.idx_xe * a.P + ip], 0.0f);
+        float xe = fmaxf(field(a.idx_xe), 0.0f);
         if (xe < ABS_TOL)
           xe = 0;
         xe = fminf(xe, 0.999f);

@@ -51,6 +51,9 @@ struct ThresholdArgs
   int idx_xe, idx_nr;    // field slot or -1
   int n_r;               // radii in this batch
   const RadiusParams* rp; // device array, n_r entries
+  // The unfiltered last step is an identity transform: its fields are read
+  // from the input grids (PADDED) instead of a transformed copy.
+  const float* direct[MAX_FIELDS];
   float* xH;
   float* z_at_ion;
   float* r_bubble;

@@ -90,14 +90,58 @@ struct mx_ctx
   cufftHandle r2c_plan = 0;
   int launches = 0;
 
+  // per-kernel event timing (mx_profile_enable / mx_profile_read)
+  struct ProfRec
+  {
+    const char* name;
+    double bytes;
+    int ev;  // index of the start event; the stop event is ev + 1
+  };
+  bool prof_on = false;
+  std::vector<ProfRec> prof;
+  std::vector<cudaEvent_t> prof_events;
+
   ~mx_ctx();
   void alloc_scratch();
   cufftHandle c2r_plan(long long batch);
   void ensure_mirror();
 };
 
+// Records CUDA events around one kernel (or cuFFT execution) on its stream
+// when profiling is on; `bytes` is the launch's algorithmic HBM traffic.
+class Prof
+{
+ public:
+  Prof(mx_ctx* c, const char* name, double bytes, cudaStream_t s) : c_(c), s_(s)
+  {
+    if (!c->prof_on)
+      return;
+    const int ev = (int)c->prof.size() * 2;
+    while ((int)c->prof_events.size() < ev + 2) {
+      cudaEvent_t e;
+      MX_CUDA(cudaEventCreate(&e));
+      c->prof_events.push_back(e);
+    }
+    c->prof.push_back({ name, bytes, ev });
+    idx_ = ev;
+    MX_CUDA(cudaEventRecord(c->prof_events[ev], s));
+  }
+  ~Prof()
+  {
+    if (idx_ >= 0)
+      cudaEventRecord(c_->prof_events[idx_ + 1], s_);
+  }
+
+ private:
+  mx_ctx* c_;
+  cudaStream_t s_;
+  int idx_ = -1;
+};
+
 mx_ctx::~mx_ctx()
 {
+  for (cudaEvent_t e : prof_events)
+    cudaEventDestroy(e);
   for (auto& kv : c2r_plans)
     cufftDestroy(kv.second);
   if (r2c_plan)
@@ -226,10 +270,16 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
     throw CudaError{ MX_EINVAL, "find_HII_bubbles: a required grid pointer is NULL" };
 
   // initial state (find_HII_bubbles.c:102-116)
-  if (uvb)
+  const double B4N = 4.0 * (double)gd.N, B8C = 8.0 * (double)gd.C;
+  if (uvb) {
+    Prof pr(c, "k_fill", B4N, s);
     launch_fill(g->J_21, gd.N, 0.0f, s);
-  launch_fill(g->xH, gd.N, 1.0f, s);
-  launch_fill(g->r_bubble, gd.N, 0.0f, s);
+  }
+  {
+    Prof pr(c, "k_fill", 2 * B4N, s);
+    launch_fill(g->xH, gd.N, 1.0f, s);
+    launch_fill(g->r_bubble, gd.N, 0.0f, s);
+  }
 
   // forward transforms of the G fields (find_HII_bubbles.c:118-163)
   const float* src[MAX_FIELDS];
@@ -249,6 +299,7 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
   for (int f = 0; f < G; f++) {
     unf_ptrs[f] = c->d_unf + (long long)f * gd.C;
     MX_CUFFT(cufftSetStream(c->r2c_plan, s));
+    Prof pr(c, "cufft_r2c", B4N + B8C, s);
     MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)src[f], (cufftComplex*)unf_ptrs[f]));
   }
   MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, unf_ptrs, sizeof(float2*) * G, cudaMemcpyHostToDevice, s));
@@ -283,20 +334,26 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
   const int per_batch = (int)std::max<long long>(1, c->work_fields / G);
   for (int r0 = 0; r0 < nR; r0 += per_batch) {
     const int nb = std::min(per_batch, nR - r0);
+    // the last, unfiltered step is read from the input grids (identity transform)
+    const int nf = (r0 + nb == nR) ? nb - 1 : nb;
     FilterBatch fb;
-    fb.n = nb;
+    fb.n = nf;
     fb.filter_type = p.filter_type;
     fb.scale_mode = 0;
-    for (int r = 0; r < nb; r++) {
+    for (int r = 0; r < nf; r++) {
       fb.R[r] = (float)radii[r0 + r];
-      fb.apply[r] = (r0 + r) != nR - 1;
+      fb.apply[r] = 1;
     }
-    launch_filter((const float2* const*)c->d_in_ptrs, G, c->d_work, gd.C, fb, gd, (float)p.box_size, s);
+    if (nf > 0) {
+      Prof pr(c, "k_filter", (double)G * B8C * (1 + nf), s);
+      launch_filter((const float2* const*)c->d_in_ptrs, G, c->d_work, gd.C, fb, gd, (float)p.box_size, s);
+    }
     // one radius (G fields) per cuFFT execution keeps the cuFFT work area at
     // the size of one radius' spectra
     const cufftHandle plan = c->c2r_plan(G);
-    for (int r = 0; r < nb; r++) {
+    for (int r = 0; r < nf; r++) {
       cufftComplex* w = (cufftComplex*)(c->d_work + (long long)r * G * gd.C);
+      Prof pr(c, "cufft_c2r", (double)G * (B8C + B4N), s);
       MX_CUFFT(cufftExecC2R(plan, w, (cufftReal*)w));
     }
     ThresholdArgs ta;
@@ -307,6 +364,8 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
     ta.idx_nr = idx_nr;
     ta.n_r = nb;
     ta.rp = c->d_rp + r0;
+    for (int f = 0; f < MAX_FIELDS; f++)
+      ta.direct[f] = f < G ? src[f] : nullptr;
     ta.xH = g->xH;
     ta.z_at_ion = g->z_at_ionization;
     ta.r_bubble = g->r_bubble;
@@ -320,6 +379,8 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
     ta.uvb = uvb;
     ta.recomb = recomb;
     ta.spin = spin;
+    const int nstate = 3 + (uvb ? 2 : 0) + (recomb ? 1 : 0);
+    Prof pr(c, "k_threshold", ((double)nb * G + 2.0 * nstate) * B4N, s);
     launch_threshold(ta, gd, s);
   }
 
@@ -339,7 +400,10 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
   ra.uvb = uvb;
   ra.recomb = recomb;
   ra.partials = c->d_partials;
-  launch_fhb_reduce(ra, gd, s);
+  {
+    Prof pr(c, "k_fhb_reduce", (2.0 + (uvb ? 1 : 0) + (recomb ? 3 : 0)) * B4N, s);
+    launch_fhb_reduce(ra, gd, s);
+  }
   launch_finalize(c->d_partials, 4, c->d_sums, s);
   MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
   MX_CUDA(cudaStreamSynchronize(s));
@@ -430,6 +494,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     ha.pixel_volume = pixel_volume;
     ha.partials = c->d_partials;
     ha.err = c->d_err;
+    Prof pr(c, "k_homog", 5.0 * 4.0 * (double)gd.N, s);
     launch_homog(ha, gd, s);
     launch_finalize(c->d_partials, 1, c->d_sums, s);
     MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -445,7 +510,10 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     ca.R3 = std::pow(R0, 3.0);
     ca.pixel_volume = pixel_volume;
     ca.partials = c->d_partials;
-    launch_cf_xe(ca, gd, s);
+    {
+      Prof pr(c, "k_cf_xe", 3.0 * 4.0 * (double)gd.N, s);
+      launch_cf_xe(ca, gd, s);
+    }
     launch_finalize(c->d_partials, 2, c->d_sums, s);
     MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
     MX_CUDA(cudaStreamSynchronize(s));
@@ -470,6 +538,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
       int r = 0;
       while (r < S) {
         for (const SfrOp& op : sp.ops[r]) {
+          Prof pr(c, "k_sfr_history", op.kind <= SfrOp::ZERO_HALF ? 8.0 * (double)nhalf : 12.0 * (double)gd.N, s);
           if (op.kind == SfrOp::SCALE_HALF)
             launch_sfr_scale_half(g->sfr, nhalf, op.dweight, s);
           else if (op.kind == SfrOp::ZERO_HALF)
@@ -478,15 +547,26 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
             launch_sfr_load(g->sfr, g->sfr_histories + (long long)op.slice * gd.P, op.weight,
                             op.kind == SfrOp::ADD, gd, s);
         }
-        MX_CUFFT(cufftSetStream(c->r2c_plan, s));
-        MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)g->sfr, (cufftComplex*)sfr_unf));
         // shells r..r_end-1 share this spectrum (no operations in between)
         int r_end = r + 1;
         while (r_end < S && sp.ops[r_end].empty())
           r_end++;
+        int q_first = r;
+        if (r == 0) {
+          // shell 0 is unfiltered: its transform pair is the identity, so the
+          // shell is the clamped grid itself
+          Prof pr(c, "k_shell_extract", 8.0 * (double)gd.N, s);
+          launch_shell_extract(g->sfr, gd.P, 1, 0, c->d_shells, gd, s);
+          q_first = 1;
+        }
+        if (q_first < r_end) {
+          MX_CUFFT(cufftSetStream(c->r2c_plan, s));
+          Prof pr(c, "cufft_r2c", 4.0 * (double)gd.N + 8.0 * (double)gd.C, s);
+          MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)g->sfr, (cufftComplex*)sfr_unf));
+        }
         float2* in_ptr[1] = { sfr_unf };
         MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, in_ptr, sizeof(float2*), cudaMemcpyHostToDevice, s));
-        for (int q0 = r; q0 < r_end;) {
+        for (int q0 = q_first; q0 < r_end;) {
           const int nb = (int)std::min<long long>(c->work_fields, r_end - q0);
           FilterBatch fb;
           fb.n = nb;
@@ -496,13 +576,20 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
             fb.R[q] = (float)sp.R[q0 + q];
             fb.apply[q] = (q0 + q) > 0;
           }
-          launch_filter((const float2* const*)c->d_in_ptrs, 1, c->d_work, gd.C, fb, gd, (float)p.box_size, s);
+          {
+            Prof pr(c, "k_filter_ts", 8.0 * (double)gd.C * (1 + nb), s);
+            launch_filter((const float2* const*)c->d_in_ptrs, 1, c->d_work, gd.C, fb, gd, (float)p.box_size, s);
+          }
           const cufftHandle plan = c->c2r_plan(1);
           for (int q = 0; q < nb; q++) {
             cufftComplex* w = (cufftComplex*)(c->d_work + (long long)q * gd.C);
+            Prof pr(c, "cufft_c2r", 8.0 * (double)gd.C + 4.0 * (double)gd.N, s);
             MX_CUFFT(cufftExecC2R(plan, w, (cufftReal*)w));
           }
-          launch_shell_extract((const float*)c->d_work, gd.P, nb, q0, c->d_shells, gd, s);
+          {
+            Prof pr(c, "k_shell_extract", 8.0 * (double)gd.N * nb, s);
+            launch_shell_extract((const float*)c->d_work, gd.P, nb, q0, c->d_shells, gd, s);
+          }
           q0 += nb;
         }
         r = r_end;
@@ -549,14 +636,23 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     ea.cst = c->d_tsc;
     ea.partials = c->d_partials;
     ea.err = c->d_err;
-    launch_evolve(ea, gd, s);
+    {
+      Prof pr(c, "k_evolve", ((double)S + 6.0) * 4.0 * (double)gd.N, s);
+      launch_evolve(ea, gd, s);
+    }
     launch_finalize(c->d_partials, 4, c->d_sums + 8, s);
     MX_CUDA(cudaMemcpyAsync(c->h_sums + 8, c->d_sums + 8, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
   }
 
   // x_e_box <- x_e_box_prev (ComputeTs.c:940) and the means (:942-974)
-  MX_CUDA(cudaMemcpyAsync(g->x_e_box, g->x_e_box_prev, sizeof(float) * gd.P, cudaMemcpyDeviceToDevice, s));
-  launch_ts_means(g->TS_box, g->Tk_box, c->d_partials, gd, s);
+  {
+    Prof pr(c, "copy_x_e_box", 8.0 * (double)gd.P, s);
+    MX_CUDA(cudaMemcpyAsync(g->x_e_box, g->x_e_box_prev, sizeof(float) * gd.P, cudaMemcpyDeviceToDevice, s));
+  }
+  {
+    Prof pr(c, "k_ts_means", 8.0 * (double)gd.N, s);
+    launch_ts_means(g->TS_box, g->Tk_box, c->d_partials, gd, s);
+  }
   launch_finalize(c->d_partials, 2, c->d_sums, s);
   MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
   // the reference's <x_e> reads the last cell's x_e_box_prev (ComputeTs.c:957)
@@ -615,6 +711,7 @@ static void run_delta_T(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* 
   a.spin = p.flag_spin_temp;
   a.pecvel = p.flag_pecvel;
   a.partials = c->d_partials;
+  Prof pr(c, "k_delta_T", (p.flag_spin_temp ? 4.0 : 3.0) * 4.0 * (double)gd.N, s);
   launch_delta_T(a, gd, s);
   launch_finalize(c->d_partials, 1, c->d_sums, s);
   MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -754,6 +851,45 @@ int mx_set_redshifts(mx_ctx* ctx, const double* zz, int32_t n_snaps)
 }
 
 int32_t mx_n_sfr_histories(const mx_ctx* ctx) { return ctx ? ctx->n_hist : -1; }
+
+int mx_profile_enable(mx_ctx* ctx, int32_t on)
+{
+  return guarded(ctx, [&]() {
+    MX_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->prof.clear();
+    ctx->prof_on = on != 0;
+  });
+}
+
+int32_t mx_profile_read(mx_ctx* ctx, mx_kernel_stat* out, int32_t cap)
+{
+  if (!ctx)
+    return MX_EINVAL;
+  std::vector<mx_kernel_stat> stats;
+  const int rc = guarded(ctx, [&]() {
+    MX_CUDA(cudaDeviceSynchronize());
+    for (const auto& r : ctx->prof) {
+      float ms = 0.f;
+      MX_CUDA(cudaEventElapsedTime(&ms, ctx->prof_events[r.ev], ctx->prof_events[r.ev + 1]));
+      auto it = std::find_if(stats.begin(), stats.end(),
+                             [&](const mx_kernel_stat& k) { return std::strcmp(k.name, r.name) == 0; });
+      if (it == stats.end()) {
+        mx_kernel_stat k{};
+        std::snprintf(k.name, sizeof k.name, "%s", r.name);
+        stats.push_back(k);
+        it = stats.end() - 1;
+      }
+      it->launches++;
+      it->ms += ms;
+      it->bytes += r.bytes;
+    }
+  });
+  if (rc != MX_OK)
+    return rc;
+  for (int i = 0; i < (int)stats.size() && i < cap; i++)
+    out[i] = stats[i];
+  return (int32_t)stats.size();
+}
 
 int32_t mx_filter_radii(const mx_ctx* ctx, double* radii, int32_t cap)
 {

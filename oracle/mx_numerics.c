@@ -138,59 +138,63 @@ void mxo_fft_1d(double* data, int n, int sign)
   free(tmp);
 }
 
+/* Complex transforms of the half spectrum w ([D][D][H], double interleaved)
+ * along x (axis 0) or y (axis 1).  Lines are independent, so they are
+ * distributed over OpenMP threads; each line's arithmetic does not depend on
+ * the thread count. */
+static void transform_axis(double* w, int D, int H, int axis, int sign)
+{
+  (void)get_plan(D); /* create the shared plan before the parallel region */
+#pragma omp parallel
+  {
+    double* line = (double*)malloc(sizeof(double) * 2 * (size_t)D);
+#pragma omp for schedule(static)
+    for (long q = 0; q < (long)D * H; q++) {
+      const int a = (int)(q / H), kz = (int)(q % H);
+      for (int t = 0; t < D; t++) {
+        const size_t i = (axis == 0 ? ((size_t)t * D + a) : ((size_t)a * D + t)) * H + kz;
+        line[2 * t] = w[2 * i];
+        line[2 * t + 1] = w[2 * i + 1];
+      }
+      mxo_fft_1d(line, D, sign);
+      for (int t = 0; t < D; t++) {
+        const size_t i = (axis == 0 ? ((size_t)t * D + a) : ((size_t)a * D + t)) * H + kz;
+        w[2 * i] = line[2 * t];
+        w[2 * i + 1] = line[2 * t + 1];
+      }
+    }
+    free(line);
+  }
+}
+
 void mxo_r2c_3d(int D, const float* in, int in_padded, float* out)
 {
   const int H = D / 2 + 1;
   const size_t nc = (size_t)D * D * H;
   const int rstride = in_padded ? 2 * H : D;
   double* w = (double*)malloc(sizeof(double) * 2 * nc);
-  double* line = (double*)malloc(sizeof(double) * 2 * (size_t)D);
+  (void)get_plan(D);
 
   /* z: real -> half complex */
-  for (int x = 0; x < D; x++)
-    for (int y = 0; y < D; y++) {
-      const float* src = in + ((size_t)x * D + y) * rstride;
+#pragma omp parallel
+  {
+    double* line = (double*)malloc(sizeof(double) * 2 * (size_t)D);
+#pragma omp for schedule(static)
+    for (long q = 0; q < (long)D * D; q++) {
+      const float* src = in + (size_t)q * rstride;
       for (int z = 0; z < D; z++) {
         line[2 * z] = (double)src[z];
         line[2 * z + 1] = 0.0;
       }
       mxo_fft_1d(line, D, -1);
-      double* dst = w + 2 * ((size_t)x * D + y) * H;
-      memcpy(dst, line, sizeof(double) * 2 * (size_t)H);
+      memcpy(w + 2 * (size_t)q * H, line, sizeof(double) * 2 * (size_t)H);
     }
-  /* y */
-  for (int x = 0; x < D; x++)
-    for (int kz = 0; kz < H; kz++) {
-      for (int y = 0; y < D; y++) {
-        size_t i = ((size_t)x * D + y) * H + kz;
-        line[2 * y] = w[2 * i];
-        line[2 * y + 1] = w[2 * i + 1];
-      }
-      mxo_fft_1d(line, D, -1);
-      for (int y = 0; y < D; y++) {
-        size_t i = ((size_t)x * D + y) * H + kz;
-        w[2 * i] = line[2 * y];
-        w[2 * i + 1] = line[2 * y + 1];
-      }
-    }
-  /* x */
-  for (int y = 0; y < D; y++)
-    for (int kz = 0; kz < H; kz++) {
-      for (int x = 0; x < D; x++) {
-        size_t i = ((size_t)x * D + y) * H + kz;
-        line[2 * x] = w[2 * i];
-        line[2 * x + 1] = w[2 * i + 1];
-      }
-      mxo_fft_1d(line, D, -1);
-      for (int x = 0; x < D; x++) {
-        size_t i = ((size_t)x * D + y) * H + kz;
-        w[2 * i] = line[2 * x];
-        w[2 * i + 1] = line[2 * x + 1];
-      }
-    }
+    free(line);
+  }
+  transform_axis(w, D, H, 1, -1); /* y */
+  transform_axis(w, D, H, 0, -1); /* x */
   for (size_t i = 0; i < 2 * nc; i++)
     out[i] = (float)w[i];
-  free(line);
   free(w);
 }
 
@@ -199,44 +203,18 @@ void mxo_c2r_3d(int D, const float* in, float* out)
   const int H = D / 2 + 1;
   const size_t nc = (size_t)D * D * H;
   double* w = (double*)malloc(sizeof(double) * 2 * nc);
-  double* line = (double*)malloc(sizeof(double) * 2 * (size_t)D);
   for (size_t i = 0; i < 2 * nc; i++)
     w[i] = (double)in[i];
 
-  /* x */
-  for (int y = 0; y < D; y++)
-    for (int kz = 0; kz < H; kz++) {
-      for (int x = 0; x < D; x++) {
-        size_t i = ((size_t)x * D + y) * H + kz;
-        line[2 * x] = w[2 * i];
-        line[2 * x + 1] = w[2 * i + 1];
-      }
-      mxo_fft_1d(line, D, +1);
-      for (int x = 0; x < D; x++) {
-        size_t i = ((size_t)x * D + y) * H + kz;
-        w[2 * i] = line[2 * x];
-        w[2 * i + 1] = line[2 * x + 1];
-      }
-    }
-  /* y */
-  for (int x = 0; x < D; x++)
-    for (int kz = 0; kz < H; kz++) {
-      for (int y = 0; y < D; y++) {
-        size_t i = ((size_t)x * D + y) * H + kz;
-        line[2 * y] = w[2 * i];
-        line[2 * y + 1] = w[2 * i + 1];
-      }
-      mxo_fft_1d(line, D, +1);
-      for (int y = 0; y < D; y++) {
-        size_t i = ((size_t)x * D + y) * H + kz;
-        w[2 * i] = line[2 * y];
-        w[2 * i + 1] = line[2 * y + 1];
-      }
-    }
+  transform_axis(w, D, H, 0, +1); /* x */
+  transform_axis(w, D, H, 1, +1); /* y */
   /* z: half complex -> real, Hermitian extension */
-  for (int x = 0; x < D; x++)
-    for (int y = 0; y < D; y++) {
-      const double* src = w + 2 * ((size_t)x * D + y) * H;
+#pragma omp parallel
+  {
+    double* line = (double*)malloc(sizeof(double) * 2 * (size_t)D);
+#pragma omp for schedule(static)
+    for (long q = 0; q < (long)D * D; q++) {
+      const double* src = w + 2 * (size_t)q * H;
       for (int k = 0; k < H; k++) {
         line[2 * k] = src[2 * k];
         line[2 * k + 1] = src[2 * k + 1];
@@ -249,13 +227,14 @@ void mxo_c2r_3d(int D, const float* in, float* out)
         line[2 * k + 1] = -src[2 * (D - k) + 1];
       }
       mxo_fft_1d(line, D, +1);
-      float* dst = out + ((size_t)x * D + y) * 2 * H;
+      float* dst = out + (size_t)q * 2 * H;
       for (int z = 0; z < D; z++)
         dst[z] = (float)line[2 * z];
       for (int z = D; z < 2 * H; z++)
         dst[z] = 0.0f;
     }
-  free(line);
+    free(line);
+  }
   free(w);
 }
 

@@ -602,8 +602,6 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
   const int spin = p->flag_spin_temp;
   const double eff = p->reion_efficiency;
   const double unit_len = p->unit_length_cm, unit_mass = p->unit_mass_g, unit_time = c->unit_time_s;
-  float J_21_aux = 0;
-  double rec = 0.0;
 
   if (snapshot < 0 || snapshot >= c->n_snaps)
     return MX_ESTATE;
@@ -624,8 +622,8 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
     g->r_bubble[i] = 0.0f;
   }
   free(c->margin);
-  c->margin = (float*)malloc(sizeof(float) * nreal);
-  for (size_t i = 0; i < nreal; i++)
+  c->margin = (float*)malloc(sizeof(float) * 2 * nreal);
+  for (size_t i = 0; i < 2 * nreal; i++)
     c->margin[i] = INFINITY;
 
   /* fields: deltax, stars, weighted_sfr, [x_e], [N_rec] */
@@ -695,7 +693,8 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
     const double M_mean = c_RtoM(c, R);
     const double R_cubed = R * R * R;
 
-    /* threshold loop, find_HII_bubbles.c:342-443 */
+    /* threshold loop, find_HII_bubbles.c:342-443 (cells are independent) */
+#pragma omp parallel for schedule(static)
     for (int ix = 0; ix < D; ix++)
       for (int iy = 0; iy < D; iy++)
         for (int iz = 0; iz < D; iz++) {
@@ -705,14 +704,18 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
           const double f_coll_stars =
             (double)fil[F_ST][ip] / (M_mean * dom) * (4.0 / 3.0) * M_PI * R_cubed / pixel_volume;
           const double wsd = (double)fil[F_WS][ip] / pixel_volume;
+          double rec = 0.0;
           if (recomb)
             rec = (double)fil[F_NR][ip] / dom;
           const double nf = spin ? 1.0 - fil[F_XE][ip] : 1.0;
+          float J_21_aux = 0;
           if (uvb)
             J_21_aux = (float)(wsd * J_21_aux_constant);
           const double lhs = f_coll_stars * eff, rhs = nf * (1. + rec);
+          const float mrel = (float)fabs(lhs / rhs - 1.0);
           if (g->xH[ir] > K_REL_TOL)
-            c->margin[ir] = fminf(c->margin[ir], (float)fabs(lhs / rhs - 1.0));
+            c->margin[ir] = fminf(c->margin[ir], mrel);
+          c->margin[nreal + ir] = fminf(c->margin[nreal + ir], mrel);
           if (lhs > rhs) {
             if (g->xH[ir] > K_REL_TOL) {
               if (uvb)
@@ -1358,7 +1361,8 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
         c_filter(c, fil, D, (float)R, p->ts_heating_filter_type);
       mxo_c2r_3d(D, fil, fil);
 
-      /* ComputeTs.c:413-500 */
+      /* ComputeTs.c:413-500 (stores in parallel, sums in the reference order) */
+#pragma omp parallel for schedule(static)
       for (int ix = 0; ix < D; ix++)
         for (int iy = 0; iy < D; iy++)
           for (int iz = 0; iz < D; iz++) {
@@ -1366,6 +1370,11 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
             const size_t ir = real_idx(D, ix, iy, iz);
             fil[ip] = fmaxf(fil[ip], 0.0);
             smoothed[(size_t)R_ct + (size_t)S * ir] = ((fil[ip] / pixel_volume) * sfr_unit);
+          }
+      for (int ix = 0; ix < D; ix++)
+        for (int iy = 0; iy < D; iy++)
+          for (int iz = 0; iz < D; iz++) {
+            const size_t ip = pad_idx(D, ix, iy, iz);
             if (R_ct == 0) {
               const double dom = 1.0 + g->deltax[ip];
               double cf = g->stars[ip] / (c_RtoM(c, R) * p->hubble_h * p->hubble_h * dom) * (4.0 / 3.0) * M_PI *
@@ -1391,6 +1400,18 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
     double* tH = c->freq_tables;
     double* tI = c->freq_tables + (size_t)K_NXHII * S;
     double* tL = c->freq_tables + (size_t)2 * K_NXHII * S;
+    /* the integrals of different shells are independent */
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int R_ct = 0; R_ct < S; R_ct++) {
+      const double prev_zpp = R_ct == 0 ? zp : c->zpp_edge[R_ct - 1];
+      const double zpp = (c->zpp_edge[R_ct] + prev_zpp) * 0.5;
+      const double lower = fmax(c_nu_tau_one(c, zp, zpp, c->x_e_ave, snapshot), p->nu_xray_gal_threshold * K_NU_OVER_EV);
+      for (int x = 0; x < K_NXHII; x++) {
+        tH[(size_t)x * S + R_ct] = c_integrate_over_nu(c, zp, c->x_xhii[x], lower, 0);
+        tI[(size_t)x * S + R_ct] = c_integrate_over_nu(c, zp, c->x_xhii[x], lower, 1);
+        tL[(size_t)x * S + R_ct] = c_integrate_over_nu(c, zp, c->x_xhii[x], lower, 2);
+      }
+    }
     for (int R_ct = 0; R_ct < S; R_ct++) {
       double prev_zpp, prev_R;
       if (R_ct == 0) {
@@ -1401,12 +1422,6 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
         prev_R = R_values[R_ct - 1];
       }
       const double zpp = (c->zpp_edge[R_ct] + prev_zpp) * 0.5;
-      const double lower = fmax(c_nu_tau_one(c, zp, zpp, c->x_e_ave, snapshot), p->nu_xray_gal_threshold * K_NU_OVER_EV);
-      for (int x = 0; x < K_NXHII; x++) {
-        tH[(size_t)x * S + R_ct] = c_integrate_over_nu(c, zp, c->x_xhii[x], lower, 0);
-        tI[(size_t)x * S + R_ct] = c_integrate_over_nu(c, zp, c->x_xhii[x], lower, 1);
-        tL[(size_t)x * S + R_ct] = c_integrate_over_nu(c, zp, c->x_xhii[x], lower, 2);
-      }
       c->sum_lyn[R_ct] = 0;
       for (int n_ct = K_NSPEC_MAX; n_ct >= 2; n_ct--) {
         if (zpp > c_zmax((float)zp, n_ct))
@@ -1458,16 +1473,22 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
     Lconv *= (K_SEC_PER_YEAR) / (K_PLANCK);
     c->const_zp_prefactor = (p->lx_gal * Lconv) / (E0 * K_NU_OVER_EV) * K_C * pow(1 + zp, alpha + 3);
 
-    /* per-cell evolution, ComputeTs.c:743-900 */
+    /* per-cell evolution, ComputeTs.c:743-900: cells in parallel, the
+     * volume averages summed afterwards in the reference's cell order */
+    double* contrib = (double*)malloc(sizeof(double) * 4 * (size_t)D * D * D);
+#pragma omp parallel
+    {
     double* SFR = (double*)malloc(sizeof(double) * (size_t)S);
     double* fh = (double*)malloc(sizeof(double) * (size_t)S);
     double* fi = (double*)malloc(sizeof(double) * (size_t)S);
     double* fl = (double*)malloc(sizeof(double) * (size_t)S);
+#pragma omp for schedule(static)
     for (int ix = 0; ix < D; ix++)
       for (int iy = 0; iy < D; iy++)
         for (int iz = 0; iz < D; iz++) {
           const size_t ir = real_idx(D, ix, iy, iz);
-          i_padded = pad_idx(D, ix, iy, iz);
+          const size_t i_padded = pad_idx(D, ix, iy, iz);
+          float curr_xalpha;
           double ans[2], dansdz[5];
           ans[0] = g->x_e_box_prev[i_padded];
           ans[1] = g->Tk_box[ir];
@@ -1500,15 +1521,24 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
             g->Tk_box[ir] = (float)(K_TCMB * (1 + zp));
           g->TS_box[ir] = c_get_Ts(c, (float)zp, g->deltax[i_padded], g->Tk_box[ir], g->x_e_box_prev[i_padded],
                                    (float)dansdz[2], &curr_xalpha);
-          J_alpha_ave += dansdz[2];
-          xalpha_ave += curr_xalpha;
-          Xheat_ave += dansdz[3];
-          Xion_ave += dansdz[4];
+          contrib[4 * ir + 0] = dansdz[2];
+          contrib[4 * ir + 1] = curr_xalpha;
+          contrib[4 * ir + 2] = dansdz[3];
+          contrib[4 * ir + 3] = dansdz[4];
         }
     free(SFR);
     free(fh);
     free(fi);
     free(fl);
+    }
+    for (size_t ir = 0; ir < (size_t)D * D * D; ir++) {
+      J_alpha_ave += contrib[4 * ir + 0];
+      xalpha_ave += contrib[4 * ir + 1];
+      Xheat_ave += contrib[4 * ir + 2];
+      Xion_ave += contrib[4 * ir + 3];
+    }
+    free(contrib);
+    i_padded = pad_idx(D, D - 1, D - 1, D - 1); /* last cell visited */
     free(R_values);
     free(scb);
     free(smoothed);

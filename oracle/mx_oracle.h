@@ -30,11 +30,13 @@ int mxo_n_sfr_histories(const mxo_ctx* c);
 int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out);
 int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out);
 int mxo_delta_T(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out);
-/* Per-cell threshold margin of the last find_HII_bubbles call (REAL layout):
- * min over radii, up to and including the first crossing, of
- * |f_coll*eff / (nf*(1+rec)) - 1|.  A cell whose flag, r_bubble or first-crossing
- * J_21 can legitimately differ between two FP32 FFT implementations has a
- * small margin.  NULL before a call. */
+/* Per-cell threshold margins of the last find_HII_bubbles call, two REAL
+ * grids back to back: [0, N) the min over radii up to and including the first
+ * crossing of |f_coll*eff / (nf*(1+rec)) - 1| (decides the ionised flag and the
+ * first-crossing J_21 / Gamma12); [N, 2N) the same min over every radius
+ * (decides r_bubble, which is overwritten at each ionising radius).  A cell
+ * whose outputs can legitimately differ between two FP32 FFT implementations
+ * has a small margin.  NULL before a call. */
 const float* mxo_last_margin(const mxo_ctx* c);
 
 /* Table-level helpers (host physics) for tests. */

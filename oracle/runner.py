@@ -115,9 +115,10 @@ class OracleBackend:
         return self._call("mxo_delta_T", snapshot, state)
 
     def margin(self) -> np.ndarray:
+        """[2, D, D, D]: first-crossing margin and all-radii margin."""
         D = self.params.grid_dim
         p = self.lib.mxo_last_margin(self.ctx)
-        return np.ctypeslib.as_array(p, shape=(D, D, D)).copy()
+        return np.ctypeslib.as_array(p, shape=(2, D, D, D)).copy()
 
     def freq_tables(self) -> np.ndarray:
         n = ctypes.c_int()

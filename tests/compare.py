@@ -1,10 +1,17 @@
 """Parity checks between two runs of the grid step (test helpers).
 
-Tolerances follow the acceptance rule of the GB300 step: mean xHI within 1e-5
-relative; ionisation flags may disagree in at most 1e-4 of the cells and only
-where the oracle's threshold margin |f_coll*eff/(nf(1+rec)) - 1| is below 1e-5;
-T_S and delta_T within 1e-4 relative; the other grids within 1e-4 relative
-(or a small absolute floor) where the flags agree.
+Tolerances, from the acceptance rule of the step:
+  * global volume / mass weighted xHI within 1e-5 relative;
+  * ionisation flags may disagree in at most 1e-4 of the cells, and only in
+    cells whose threshold margin |f_coll*eff/(nf(1+rec)) - 1| (from the oracle)
+    is below 1e-5; r_bubble (overwritten at every ionising radius) likewise
+    with the all-radii margin;
+  * T_S, T_K, delta_T and the other grids within 1e-4 relative per cell, with
+    an absolute floor of 10 * 2^-24 * log2(N) * max|x| that bounds the rounding
+    error of an FP32 FFT of N points (the reference's FFTW single-precision
+    path carries an error of the same size); values that depend on the radius
+    of first crossing (J_21, Gamma12, N_rec) are compared where that radius
+    agrees.
 """
 from __future__ import annotations
 
@@ -12,87 +19,95 @@ from typing import Dict, Optional
 
 import numpy as np
 
-REL_TOL = 1e-5
+REL_TOL = 1e-5          # REL_TOL of the reference: ionised means xH < 1e-5
 FLAG_FRACTION = 1e-4
 MARGIN = 1e-5
 GRID_RTOL = 1e-4
+XH_ATOL = 1e-4
 
 
-def _rel(a, b, floor):
-    a = a.astype(np.float64)
-    b = b.astype(np.float64)
-    return np.abs(a - b) / np.maximum(np.abs(a), floor)
+def fft_floor(n: int) -> float:
+    return 10.0 * 2.0 ** -24 * np.log2(n)
+
+
+def _real(a: np.ndarray, D: int) -> np.ndarray:
+    if a.size == D ** 3:
+        return a.reshape(-1)
+    return np.ascontiguousarray(a.reshape(D, D, -1)[:, :, :D]).reshape(-1)
 
 
 def compare(ref: Dict[str, np.ndarray], test: Dict[str, np.ndarray], ref_globals: Dict[str, float],
-            test_globals: Dict[str, float], margin: Optional[np.ndarray] = None, exact: bool = False,
-            report: Optional[dict] = None):
+            test_globals: Dict[str, float], margin: Optional[np.ndarray] = None, report: Optional[dict] = None):
     """Raises AssertionError with a readable message on a parity violation."""
     rep = report if report is not None else {}
     D = ref["xH"].shape[0]
     n = D ** 3
+    floor = fft_floor(n)
     fa = ref["xH"].reshape(-1) < REL_TOL
     fb = test["xH"].reshape(-1) < REL_TOL
     dis = fa != fb
-    rep["flag_disagree"] = int(dis.sum())
-    # r_bubble / first-crossing quantities can differ in near-threshold cells
     rb_dis = ref["r_bubble"].reshape(-1) != test["r_bubble"].reshape(-1)
+    rep["flag_disagree"] = int(dis.sum())
     rep["rbubble_disagree"] = int(rb_dis.sum())
-    if exact:
-        assert dis.sum() == 0, f"flags differ in {dis.sum()} cells"
+    assert dis.sum() <= FLAG_FRACTION * n, f"flags differ in {dis.sum()} of {n} cells"
+    if margin is not None:
+        m_first, m_all = margin[0].reshape(-1), margin[1].reshape(-1)
+        if dis.any():
+            rep["flag_margin_max"] = float(m_first[dis].max())
+            assert np.all(m_first[dis] < MARGIN), f"flag disagreement at margin {m_first[dis].max():.3e}"
+        if rb_dis.any():
+            rep["rbubble_margin_max"] = float(m_all[rb_dis].max())
+            assert np.all(m_all[rb_dis] < MARGIN), f"r_bubble disagreement at margin {m_all[rb_dis].max():.3e}"
+        near_first = m_first < MARGIN
     else:
-        assert dis.sum() <= max(FLAG_FRACTION * n, 0), f"flags differ in {dis.sum()} of {n} cells"
-        if margin is not None and dis.any():
-            m = margin.reshape(-1)[dis]
-            assert np.all(m < MARGIN), f"flag disagreement at margin {m.max():.3e}"
-        if margin is not None and rb_dis.any():
-            m = margin.reshape(-1)[rb_dis]
-            rep["rbubble_margin_max"] = float(m.max())
-            assert np.all(m < MARGIN), f"r_bubble disagreement at margin {m.max():.3e}"
-    same = ~(dis | rb_dis)
+        assert rb_dis.sum() <= FLAG_FRACTION * n, f"r_bubble differs in {rb_dis.sum()} of {n} cells"
+        near_first = np.zeros(n, bool)
     for k in ("volume_weighted_global_xH", "mass_weighted_global_xH"):
-        if k in ref_globals:
+        if k in ref_globals and k in test_globals:
             a, b = ref_globals[k], test_globals[k]
             r = abs(a - b) / max(abs(a), 1e-30)
             rep[k] = r
-            assert r <= (1e-12 if exact else REL_TOL) or (a == 0 and b == 0), f"{k}: {a} vs {b} ({r:.3e})"
+            assert r <= REL_TOL or (a == 0 and b == 0), f"{k}: {a} vs {b} ({r:.3e})"
     for k in ("volume_ave_TS", "volume_ave_TK", "volume_ave_Tb"):
         if k in ref_globals and k in test_globals and ref_globals[k] != 0:
             r = abs(ref_globals[k] - test_globals[k]) / abs(ref_globals[k])
             rep[k] = r
-            assert r <= (1e-12 if exact else GRID_RTOL), f"{k}: {ref_globals[k]} vs {test_globals[k]} ({r:.3e})"
+            assert r <= GRID_RTOL, f"{k}: {ref_globals[k]} vs {test_globals[k]} ({r:.3e})"
+
+    same = ~(dis | rb_dis)
+    # grid -> (cells compared, allowed fraction of outliers without margins)
+    first_dep = same & ~near_first
     checks = {
-        "xH": (1e-4, 1.0),
-        "z_at_ionization": (0.0, 1.0),
-        "J_21": (GRID_RTOL, 1e-3),
-        "J_21_at_ionization": (GRID_RTOL, 1e-3),
-        "Gamma12": (GRID_RTOL, 1e-6),
-        "N_rec": (GRID_RTOL, 1e-6),
-        "delta_T": (GRID_RTOL, 1e-3),
-        "TS_box": (GRID_RTOL, 1e-3),
-        "Tk_box": (GRID_RTOL, 1e-3),
+        "xH": same,
+        "z_at_ionization": same,
+        "delta_T": same,
+        "TS_box": np.ones(n, bool),
+        "Tk_box": np.ones(n, bool),
+        "x_e_box_prev": np.ones(n, bool),
+        "J_21": first_dep,
+        "J_21_at_ionization": first_dep,
+        "Gamma12": first_dep,
+        "N_rec": first_dep,
     }
-    for k, (rtol, floor) in checks.items():
+    for k, sel in checks.items():
         if k not in ref or k not in test or ref[k] is None or test[k] is None:
             continue
-        a = ref[k].reshape(-1)[: n] if ref[k].size == n else _real(ref[k], D)
-        b = test[k].reshape(-1)[: n] if test[k].size == n else _real(test[k], D)
-        sel = same if k in ("xH", "z_at_ionization", "J_21", "J_21_at_ionization", "Gamma12", "delta_T", "N_rec") \
-            else np.ones(n, bool)
+        a = _real(ref[k], D).astype(np.float64)
+        b = _real(test[k], D).astype(np.float64)
         if not sel.any():
             continue
+        scale = max(float(np.abs(a).max()), 1e-300)
         if k == "xH":
-            err = np.abs(a[sel].astype(np.float64) - b[sel])
+            bad = np.abs(a - b) > XH_ATOL + floor
+        elif k == "z_at_ionization":
+            bad = a != b
         else:
-            err = _rel(a[sel], b[sel], floor * max(np.abs(a).max(), 1e-30) if k not in ("xH",) else floor)
-        worst = float(err.max()) if err.size else 0.0
-        rep[k] = worst
-        if exact:
-            assert worst == 0.0, f"{k}: max error {worst:.3e}"
-        else:
-            assert worst <= rtol + (0 if rtol else 0), f"{k}: max error {worst:.3e} > {rtol}"
+            bad = np.abs(a - b) > GRID_RTOL * np.abs(a) + floor * scale
+        bad &= sel
+        err = np.abs(a - b)[sel] / np.maximum(np.abs(a[sel]), floor * scale)
+        rep[k] = float(err.max()) if err.size else 0.0
+        rep[k + "_outliers"] = int(bad.sum())
+        allowed = 0 if margin is not None or k in ("TS_box", "Tk_box", "x_e_box_prev", "xH", "delta_T") \
+            else FLAG_FRACTION * n
+        assert bad.sum() <= allowed, f"{k}: {bad.sum()} cells outside tolerance (max rel {rep[k]:.3e})"
     return rep
-
-
-def _real(padded: np.ndarray, D: int) -> np.ndarray:
-    return np.ascontiguousarray(padded.reshape(D, D, -1)[:, :, :D]).reshape(-1)
