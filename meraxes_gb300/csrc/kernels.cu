@@ -17,19 +17,12 @@ int g_launches = 0;
 constexpr float REL_TOL = 1e-5f;
 constexpr float ABS_TOL = 1e-8f;
 constexpr double PI_D = 3.14159265358979323846;
-constexpr double TCMB = 2.728;
-constexpr double T21 = 0.0628;
-constexpr double A10 = 2.85e-15;
-constexpr double BOLTZMANN = 1.3806e-16;
 constexpr double FRACT_FLOAT_ERR = 1e-7;
-constexpr float MAX_TK = 5e4f;
-constexpr int NXHII = 14;
 constexpr int RR_Z_NPTS = 300;
 constexpr int RR_LNG_NPTS = 150;
 constexpr float RR_DEL_Z = 0.2f;
 constexpr float RR_DEL_LNG = 0.1f;
 constexpr double RR_LNG_MIN = -10.0;
-constexpr int TS_MAX_ITER = 10000;
 
 int blocks_for(long long n, int threads)
 {
@@ -70,28 +63,9 @@ __device__ __forceinline__ long long pad_of(long long ir, int D, int H)
   return ir - row * D + row * 2LL * H;
 }
 
-// natural cubic spline evaluation (bracketing by bisection), NaN outside
-__device__ double spline_eval(const double* x, const double* y, const double* c, int n, double xv)
-{
-  if (!(xv >= x[0] && xv <= x[n - 1]))
-    return CUDART_NAN;
-  int lo = 0, hi = n - 1;
-  while (hi > lo + 1) {
-    const int mid = (lo + hi) >> 1;
-    if (x[mid] > xv)
-      hi = mid;
-    else
-      lo = mid;
-  }
-  const double h = x[lo + 1] - x[lo];
-  const double dx = xv - x[lo];
-  const double b = (y[lo + 1] - y[lo]) / h - h * (c[lo + 1] + 2.0 * c[lo]) / 3.0;
-  const double d = (c[lo + 1] - c[lo]) / (3.0 * h);
-  return y[lo] + dx * (b + dx * (c[lo] + dx * d));
-}
 }  // namespace
 
-int kernel_launch_count() { return g_launches; }
+int kernel_launch_count() { return g_launches + ts_kernel_launches(); }
 void reset_kernel_launch_count() { g_launches = 0; }
 
 // ================================================================= filter
@@ -215,36 +189,51 @@ __global__ void k_threshold(ThresholdArgs a, int D, int H, long long N)
       float ws = fmaxf(field(2), 0.0f);
       if (ws < ABS_TOL)
         ws = 0;
-      double rec = 0.0;
+      float nr = 0.0f, xe = 0.0f;
       if (a.recomb) {
-        float nr = fmaxf(field(a.idx_nr), 0.0f);
+        nr = fmaxf(field(a.idx_nr), 0.0f);
         if (nr < ABS_TOL)
           nr = 0;
-        rec = (double)nr / (1.0 + (double)dx);
       }
-      double nf = 1.0;
       if (a.spin) {
-        float xe = fmaxf(field(a.idx_xe), 0.0f);
+        xe = fmaxf(field(a.idx_xe), 0.0f);
         if (xe < ABS_TOL)
           xe = 0;
         xe = fminf(xe, 0.999f);
-        nf = 1.0 - (double)xe;
       }
-      const double dom = 1.0 + (double)dx;
-      const double f_coll = (double)st / (rp.M_mean * dom) * (4.0 / 3.0) * PI_D * rp.R_cubed / a.pixel_volume;
-      const double wsd = (double)ws / a.pixel_volume;
-      const float J21_aux = a.uvb ? (float)(wsd * rp.J21_const) : 0.0f;
-      if (f_coll * a.eff > nf * (1. + rec)) {
+      // FP32 evaluation of the criterion f_coll*eff > nf*(1+rec); when the two
+      // sides are within 4e-6 of each other (a few float roundings), the
+      // decision and the partial xH are recomputed in FP64 as the reference
+      // writes them (find_HII_bubbles.c:348-428).
+      const float domf = 1.0f + dx;
+      const float lhs_f = st * rp.kfc / domf;
+      const float nf_f = 1.0f - xe;
+      const float rhs_f = nf_f * (1.0f + nr / domf);
+      bool ionised;
+      float xpart;
+      if (fabsf(lhs_f - rhs_f) > 4e-6f * fmaxf(lhs_f, rhs_f)) {
+        ionised = lhs_f > rhs_f;
+        xpart = nf_f - lhs_f;
+      } else {
+        const double dom = 1.0 + (double)dx;
+        const double rec = a.recomb ? (double)nr / dom : 0.0;
+        const double nf = a.spin ? 1.0 - (double)xe : 1.0;
+        const double f_coll = (double)st / (rp.M_mean * dom) * (4.0 / 3.0) * PI_D * rp.R_cubed / a.pixel_volume;
+        ionised = f_coll * a.eff > nf * (1. + rec);
+        xpart = (float)__dsub_rn(nf, __dmul_rn(f_coll, a.eff));
+      }
+      const float J21_aux = a.uvb ? ws * rp.kj : 0.0f;
+      if (ionised) {
         if (xH > REL_TOL) {
           if (a.uvb)
             J21 = J21_aux;
           if (a.recomb)
-            G12 = (float)(rp.Gamma_pref * wsd);
+            G12 = ws * rp.kg;
         }
         xH = 0.0f;
         rb = (float)rp.R;
       } else if (rp.last && (xH > REL_TOL)) {
-        xH = (float)__dsub_rn(nf, __dmul_rn(f_coll, a.eff));
+        xH = xpart;
         if (xH < 0.f)
           xH = 0.f;
         else if (xH > 1.0f)
@@ -280,37 +269,65 @@ void launch_threshold(const ThresholdArgs& a, const GridDims& gd, cudaStream_t s
 __global__ void k_fhb_reduce(FhbReduceArgs a, int D, int H, long long N)
 {
   double acc[4] = { 0, 0, 0, 0 };
+  // RR_DEL_LNG * RR_LNG_NPTS is a float product in recombinations.c:46
+  const double lng_top = RR_LNG_MIN + (double)(RR_DEL_LNG * (float)RR_LNG_NPTS);
+  const float dNfac = a.fabs_dtdz * a.zstep;
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
     const long long ip = pad_of(ir, D, H);
-    const double cell_xH = (double)a.xH[ir];
+    const float xHf = a.xH[ir];
+    const float dxf = a.deltax[ip];
+    const double cell_xH = (double)xHf;
     acc[0] += cell_xH;
     if (a.uvb)
       acc[1] += (double)a.J21[ir];
-    const double dom = 1.0 + (double)a.deltax[ip];
+    const double dom = 1.0 + (double)dxf;
     acc[2] += cell_xH * dom;
     acc[3] += dom;
-    if (a.recomb) {
-      const float z_eff = (float)__dsub_rn(__dmul_rn(1. + a.redshift, pow(dom, 1.0 / 3.0)), 1.0);
-      const double g12 = (double)a.Gamma12[ir];
-      int z_ct = (int)((double)z_eff / (double)RR_DEL_Z + 0.5);
-      double lnG = log(g12);
-      if (z_ct < 0)
-        z_ct = 0;
-      else if (z_ct >= RR_Z_NPTS)
-        z_ct = RR_Z_NPTS - 1;
-      double rr;
-      if (lnG < RR_LNG_MIN)
-        rr = 0.0;
-      else {
-        // RR_DEL_LNG * RR_LNG_NPTS is a float product in recombinations.c:46
-        const double lng_top = RR_LNG_MIN + (double)(RR_DEL_LNG * (float)RR_LNG_NPTS);
-        if (lnG >= lng_top)
-          lnG = lng_top - FRACT_FLOAT_ERR;
-        rr = spline_eval(a.rr_x, a.rr_y + (long long)z_ct * RR_LNG_NPTS, a.rr_c + (long long)z_ct * RR_LNG_NPTS,
-                         RR_LNG_NPTS, lnG);
+    const float g12 = a.recomb ? a.Gamma12[ir] : 0.0f;
+    // dNrec is exactly zero for neutral cells and for Gamma12 = 0 (log -> -inf)
+    if (a.recomb && xHf < 1.0f && g12 > 0.0f) {
+      // FP32 lookup of splined_recombination_rate (recombinations.c:30-52);
+      // the redshift bin and the lower lnGamma cut are decided in FP64 when
+      // FP32 lands within rounding of a bin edge
+      const float zf = (1.0f + (float)a.redshift) * cbrtf(1.0f + dxf) - 1.0f;
+      const float qf = zf / RR_DEL_Z + 0.5f;
+      int z_ct;
+      if (fabsf(qf - rintf(qf)) > 2e-4f) {
+        z_ct = (int)qf;
+      } else {
+        const float z_eff = (float)__dsub_rn(__dmul_rn(1. + a.redshift, pow(dom, 1.0 / 3.0)), 1.0);
+        z_ct = (int)((double)z_eff / (double)RR_DEL_Z + 0.5);
       }
-      const double dNrec = rr * (double)a.fabs_dtdz * (double)a.zstep * (1. - cell_xH);
-      a.N_rec[ip] = (float)((double)a.N_rec[ip] + dNrec);
+      z_ct = z_ct < 0 ? 0 : (z_ct >= RR_Z_NPTS ? RR_Z_NPTS - 1 : z_ct);
+      float lnG = logf(g12);
+      bool below = lnG < (float)RR_LNG_MIN;
+      if (fabsf(lnG - (float)RR_LNG_MIN) < 1e-5f)
+        below = log((double)g12) < RR_LNG_MIN;
+      if (!below) {
+        if ((double)lnG >= lng_top)
+          lnG = (float)(lng_top - FRACT_FLOAT_ERR);
+        const float* x = a.rr_xf;
+        const float* y = a.rr_yf + (long long)z_ct * RR_LNG_NPTS;
+        const float* c = a.rr_cf + (long long)z_ct * RR_LNG_NPTS;
+        float rr;
+        if (!(lnG >= x[0] && lnG <= x[RR_LNG_NPTS - 1])) {
+          rr = CUDART_NAN_F;  // outside the table (the reference's GSL reports a domain error)
+        } else {
+          int lo = 0, hi = RR_LNG_NPTS - 1;
+          while (hi > lo + 1) {
+            const int mid = (lo + hi) >> 1;
+            if (x[mid] > lnG)
+              hi = mid;
+            else
+              lo = mid;
+          }
+          const float h = x[lo + 1] - x[lo], t = lnG - x[lo];
+          const float b = (y[lo + 1] - y[lo]) / h - h * (c[lo + 1] + 2.0f * c[lo]) * (1.0f / 3.0f);
+          const float d = (c[lo + 1] - c[lo]) / (3.0f * h);
+          rr = y[lo] + t * (b + t * (c[lo] + t * d));
+        }
+        a.N_rec[ip] = a.N_rec[ip] + rr * a.rr_scale_inv * dNfac * (1.0f - xHf);
+      }
     }
   }
   block_reduce_store<4>(acc, a.partials);
@@ -417,231 +434,19 @@ void launch_shell_extract(const float* filtered, long long P, int n, int r0, flo
 __global__ void k_cf_xe(CfArgs a, int D, int H, long long N)
 {
   double acc[2] = { 0, 0 };
+  // per-cell collapse fraction in FP32, volume sums in FP64
+  const float kcf = (float)((4.0 / 3.0) * PI_D * a.R3 / a.pixel_volume / a.RtoM_h2);
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
     const long long ip = pad_of(ir, D, H);
-    const double dom = 1.0 + a.deltax[ip];
-    double cf = a.stars[ip] / (a.RtoM_h2 * dom) * (4.0 / 3.0) * PI_D * a.R3 / a.pixel_volume;
-    if (cf > 1.0)
-      cf = 1.0;
-    acc[0] += cf;
-    acc[1] += a.x_e_prev[ip];
+    const float cf = fminf(a.stars[ip] * kcf / (1.0f + a.deltax[ip]), 1.0f);
+    acc[0] += (double)cf;
+    acc[1] += (double)a.x_e_prev[ip];
   }
   block_reduce_store<2>(acc, a.partials);
 }
 void launch_cf_xe(const CfArgs& a, const GridDims& gd, cudaStream_t s)
 {
   k_cf_xe<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, gd.D, gd.H, gd.N);
-  g_launches++;
-}
-
-namespace {
-// alpha_A, XRayHeatingFunctions.c:1450-1458
-__device__ double d_alpha_A(double T)
-{
-  const double logT = log(T / (double)1.1604505e4);
-  return exp(-28.6130338 - 0.72411256 * logT - 2.02604473e-2 * pow(logT, 2) - 2.38086188e-3 * pow(logT, 3) -
-             3.21260521e-4 * pow(logT, 4) - 1.42150291e-5 * pow(logT, 5) + 4.98910892e-6 * pow(logT, 6) +
-             5.75561414e-7 * pow(logT, 7) - 1.85676704e-8 * pow(logT, 8) - 3.07113524e-9 * pow(logT, 9));
-}
-
-__device__ double d_kappa(const TsDevConst& c, int which, double T)
-{
-  // kappa_10 (which 0): power law above the table; elec/pH (1,2): linear in logs
-  const int n = c.nk[which];
-  const double* x = c.kx[which];
-  const double* y = c.ky[which];
-  double ans;
-  if (which == 0) {
-    if (log(T) < x[0])
-      ans = y[0];
-    else if (log(T) > x[n - 1])
-      ans = log(exp(y[n - 1]) * pow(T / exp(x[n - 1]), 0.381));
-    else
-      ans = spline_eval(x, y, c.kc[which], n, log(T));
-  } else {
-    const double lt = log(T);
-    if (lt < x[0])
-      ans = y[0];
-    else if (lt > x[n - 1])
-      ans = y[n - 1] + ((y[n - 1] - y[n - 2]) / (x[n - 1] - x[n - 2]) * (lt - x[n - 1]));
-    else
-      ans = spline_eval(x, y, c.kc[which], n, lt);
-  }
-  return exp(ans);
-}
-
-// get_Ts, XRayHeatingFunctions.c:1513-1558 (+ xcoll :1560-1600, xalpha_tilde
-// / taugp / Salpha_tilde / Tc_eff :1847-1882).  The fixed-point iteration is
-// capped; hitting the cap sets bit 0 of *err.
-__device__ float d_get_Ts(const TsDevConst& c, float z, float delta, float TK, float xe, float Jalpha, float* curr_xalpha,
-                          unsigned int* err)
-{
-  const double zd = z, TKd = TK, dd = delta, xd = xe;
-  const double Trad = TCMB * (1.0 + zd);
-  const double p3 = pow(1.0 + zd, 3.0);
-  const double nH = (1.0 - xd) * c.no * p3 * (1.0 + dd);
-  const double ne = xd * c.n_b0 * p3 * (1.0 + dd);
-  const double np = xd * c.no * p3 * (1.0 + dd);
-  const double xc = T21 / Trad * nH * d_kappa(c, 0, TKd) / A10 + T21 / Trad * ne * d_kappa(c, 1, TKd) / A10 +
-                    T21 / Trad * np * d_kappa(c, 2, TKd) / A10;
-  double TS, TSinv, xa = 0;
-  if (Jalpha > 1.0e-20) {
-    TS = Trad;
-    double TSold = 0.0;
-    const double tgp = 1.342881e-7 / c.hubble_z * c.no * pow(1 + zd, 3) * (1.0 + dd) * (1.0 - xd);
-    const double xi = pow(1.0e-7 * tgp / TKd / TKd, 1.0 / 3.0);
-    int it = 0;
-    while (fabs(TS - TSold) / TS > 1.0e-3) {
-      if (++it > TS_MAX_ITER) {
-        atomicOr(err, 1u);
-        break;
-      }
-      TSold = TS;
-      double St = 1.0 - 0.0631789 / TKd + 0.115995 / TKd / TKd - 0.401403 / TS / TKd;
-      St += 0.336463 / TS / TKd / TKd;
-      St /= 1.0 + 2.98394 * xi + 1.53583 * xi * xi + 3.85289 * xi * xi * xi;
-      xa = 1.66e11 / (1.0 + zd) * St * (double)Jalpha;
-      const double Tceff = 1.0 / (1.0 / TKd + 0.405535 / TKd * (1.0 / TS - 1.0 / TKd));
-      TSinv = (1.0 / Trad + xa / Tceff + xc / TKd) / (1.0 + xa + xc);
-      TS = 1.0 / TSinv;
-    }
-    *curr_xalpha = (float)xa;
-  } else {
-    TSinv = (1.0 / Trad + xc / TKd) / (1.0 + xc);
-    TS = 1.0 / TSinv;
-    *curr_xalpha = 0;
-  }
-  if (TS < 0.)
-    TS = fabs(TS);
-  return (float)TS;
-}
-}  // namespace
-
-// Per-cell spin-temperature update, ComputeTs.c:743-900 with evolveInt
-// (XRayHeatingFunctions.c:1241-1435).  The frequency tables are staged in
-// shared memory once per block.
-__global__ void k_evolve(EvolveArgs a, int D, int H, long long N)
-{
-  const TsDevConst& c = *a.cst;
-  const int S = c.S;
-  extern __shared__ double s_tab[];  // 3 * 14 * S
-  for (int i = threadIdx.x; i < 3 * NXHII * S; i += blockDim.x) {
-    const int t = i / (NXHII * S), rem = i % (NXHII * S), x = rem / S, r = rem % S;
-    s_tab[i] = c.tab[t][x][r];
-  }
-  __syncthreads();
-  const double Conversion = c.conv;
-  double acc[4] = { 0, 0, 0, 0 };
-  for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long ip = pad_of(ir, D, H);
-    const float delta = a.deltax[ip];
-    float xe_f = a.x_e_prev[ip];
-    float Tk_f = a.Tk[ir];
-    const double x_e = xe_f, T = Tk_f;
-    double xcall = xe_f;
-    if (xcall > c.xhii[NXHII - 1] * 0.999)
-      xcall = c.xhii[NXHII - 1] * 0.999;
-    else if (xcall < c.xhii[0])
-      xcall = 1.001 * c.xhii[0];
-    int lo = NXHII - 1;
-    while ((float)xcall < c.xhii[lo])
-      lo--;
-    const int hi = lo + 1;
-    const double dxh = (double)(c.xhii[hi] - c.xhii[lo]);
-    const double wx = xcall - c.xhii[lo];
-    const float zp = c.zp;
-    const double n_b = c.n_b0 * c.p3 * (1 + delta);
-    double heat = 0, ion = 0, lya = 0, starlya = 0;
-    if (!c.no_light) {
-      for (int r = 0; r < S; r++) {
-        const float sf = a.shells[(long long)r * N + ir];
-        const double SFR = ((sf / c.pixel_volume) * c.sfr_a) * c.sfr_b / 1.989e33;
-        const double fh = (s_tab[(0 * NXHII + hi) * S + r] - s_tab[(0 * NXHII + lo) * S + r]) / dxh * wx +
-                          s_tab[(0 * NXHII + lo) * S + r];
-        const double fi = (s_tab[(1 * NXHII + hi) * S + r] - s_tab[(1 * NXHII + lo) * S + r]) / dxh * wx +
-                          s_tab[(1 * NXHII + lo) * S + r];
-        const double fl = (s_tab[(2 * NXHII + hi) * S + r] - s_tab[(2 * NXHII + lo) * S + r]) / dxh * wx +
-                          s_tab[(2 * NXHII + lo) * S + r];
-        const double integrand = SFR * c.b[r];
-        heat += c.a[r] * integrand * fh;
-        ion += c.a[r] * integrand * fi;
-        lya += c.a[r] * integrand * fl;
-        starlya += SFR * c.p2 * c.zpp1[r] * c.sum_lyn[r] * c.dt_dzpp[r] * c.dzpp[r];
-      }
-      heat *= c.prefactor;
-      ion *= c.prefactor;
-      lya *= c.prefactor * n_b;
-      starlya *= Conversion;
-    }
-    const double sink = d_alpha_A(T) * c.clumping * x_e * x_e * c.f_h * n_b;
-    const double dxe_dzp = c.dt_dzp * (ion - sink);
-    double dadia = 3 / (1.0 + zp);
-    if (fabs(delta) > FRACT_FLOAT_ERR)
-      dadia += c.dgrowth / (1.0 / delta + c.growth);
-    dadia *= (2.0 / 3.0) * T;
-    const double dspec = -dxe_dzp * T / (1 + x_e);
-    const double Trad = TCMB * (1.0 + zp);
-    double dcomp = (-1.51e-4) * (x_e / (1.0 + x_e + c.f_he)) / (c.hubble_z / c.hubble0_h) / c.h * pow(Trad, 4.0) /
-                   (1.0 + zp);
-    dcomp *= Trad - T;
-    const double dxheat_dzp = heat * c.dt_dzp * 2.0 / 3.0 / BOLTZMANN / (1.0 + x_e);
-    const double d1 = dxheat_dzp + dcomp + dspec + dadia;
-    const double d2 = lya + starlya;
-    const double d4 = c.dt_dzp * ion;
-
-    xe_f = (float)((double)xe_f + dxe_dzp * c.dzp);
-    if (xe_f > 1)
-      xe_f = (float)(1 - FRACT_FLOAT_ERR);
-    else if (xe_f < 0)
-      xe_f = 0;
-    if (Tk_f < MAX_TK)
-      Tk_f = (float)((double)Tk_f + d1 * c.dzp);
-    if (Tk_f < 0)
-      Tk_f = (float)(TCMB * (1 + c.zpd));
-    float xalpha;
-    const float TS = d_get_Ts(c, zp, delta, Tk_f, xe_f, (float)d2, &xalpha, a.err);
-    a.x_e_prev[ip] = xe_f;
-    a.Tk[ir] = Tk_f;
-    a.TS[ir] = TS;
-    acc[0] += d2;
-    acc[1] += xalpha;
-    acc[2] += dxheat_dzp;
-    acc[3] += d4;
-  }
-  block_reduce_store<4>(acc, a.partials);
-}
-
-void launch_evolve(const EvolveArgs& a, const GridDims& gd, cudaStream_t s)
-{
-  // the constant block lives in device memory; S is read on the host side
-  const int S_max = MAX_SHELLS;
-  (void)S_max;
-  k_evolve<<<RED_BLOCKS, RED_THREADS, 3 * NXHII * MAX_SHELLS * sizeof(double), s>>>(a, gd.D, gd.H, gd.N);
-  g_launches++;
-}
-
-// Homogeneous branch, ComputeTs.c:189-262
-__global__ void k_homog(HomogArgs a, int D, int H, long long N)
-{
-  const TsDevConst& c = *a.cst;
-  double acc[1] = { 0 };
-  for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long ip = pad_of(ir, D, H);
-    a.x_e_prev[ip] = a.xe0;
-    a.Tk[ir] = a.tk0;
-    float xa;
-    a.TS[ir] = d_get_Ts(c, c.zp, a.deltax[ip], a.tk0, a.xe0, 0.0f, &xa, a.err);
-    const double dom = 1.0 + a.deltax[ip];
-    double cf = a.stars[ip] / (a.RtoM_h2 * dom) * (4.0 / 3.0) * PI_D * a.R3 / a.pixel_volume;
-    if (cf > 1.0)
-      cf = 1.0;
-    acc[0] += cf;
-  }
-  block_reduce_store<1>(acc, a.partials);
-}
-void launch_homog(const HomogArgs& a, const GridDims& gd, cudaStream_t s)
-{
-  k_homog<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, gd.D, gd.H, gd.N);
   g_launches++;
 }
 
@@ -667,15 +472,13 @@ __global__ void k_delta_T(DeltaTArgs a, int D, int H, long long N)
   double acc[1] = { 0 };
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
     const long long ip = pad_of(ir, D, H);
-    const double pdx = a.deltax[ip];
-    const double pxh = a.xH[ir];
-    float dT = (float)((double)a.const_factor * pxh * (1.0 + pdx));
+    float dT = a.const_factor * a.xH[ir] * (1.0f + a.deltax[ip]);
     if (a.spin) {
       const float ts = a.TS[ir];
       if (a.pecvel > 1)
-        dT = (float)((double)dT * ((1. + (double)a.redshift) / (1000. * (double)ts)));
+        dT = dT * ((1.0f + a.redshift) / (1000.0f * ts));
       else
-        dT = (float)((double)dT * (1 - a.T_rad / (double)ts));
+        dT = dT * (1.0f - a.T_rad_f / ts);
     }
     a.delta_T[ir] = dT;
     acc[0] += (double)dT;

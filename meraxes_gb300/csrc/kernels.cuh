@@ -42,6 +42,9 @@ struct RadiusParams
 {
   double R, M_mean, R_cubed, J21_const, Gamma_pref;
   int last;
+  // FP32 fast path: f_coll*eff = st * kfc / (1+dx); J21_aux = ws * kj;
+  // Gamma12 = ws * kg
+  float kfc, kj, kg;
 };
 struct ThresholdArgs
 {
@@ -74,9 +77,10 @@ struct FhbReduceArgs
   const float* deltax;  // PADDED, unfiltered input
   const float* Gamma12;
   float* N_rec;         // PADDED, updated when recomb
-  const double* rr_y;   // recombination table (device)
-  const double* rr_c;
-  const double* rr_x;
+  const float* rr_yf;   // recombination table (device, FP32, values scaled
+  const float* rr_cf;   // by rr_scale = 1/rr_scale_inv to O(1))
+  const float* rr_xf;
+  float rr_scale_inv;
   double redshift;
   float fabs_dtdz, zstep;
   int uvb, recomb;
@@ -129,6 +133,26 @@ struct TsDevConst
   // kappa splines (ln T -> ln kappa)
   int nk[3];
   double kx[3][27], ky[3][27], kc[3][27];
+
+  // FP32 fast path.  The unit and cosmology factors of evolveInt are folded
+  // into per-shell coefficients and the frequency tables are rescaled per
+  // (table, shell) by powers of two, so that every float stays far from the
+  // float range limits:
+  //   dxheat_dzp * (1+x_e) = sum_r sf_r * fKH[r] * lerp(ftab[0][.][r], x_e)
+  //   dt_dzp * dxion_src   = sum_r sf_r * fKI[r] * lerp(ftab[1][.][r], x_e)
+  //   dxlya_dt / (1+delta) = sum_r sf_r * fKL[r] * lerp(ftab[2][.][r], x_e)
+  //   dstarlya_dt          = sum_r sf_r * fKS[r]
+  float fKH[MAX_SHELLS], fKI[MAX_SHELLS], fKL[MAX_SHELLS], fKS[MAX_SHELLS];
+  float ftab[3][14][MAX_SHELLS];
+  float fksink;   // dt_dzp * CLUMPING * f_H * N_b0 * (1+zp)^3
+  float fadia0;   // 3 / (1+zp)
+  float fdgrowth, fgrowth;
+  float fccomp;   // dT_comp prefactor without x_e/(1+x_e+f_He) (Trad - T)
+  float ftrad, ff_he, fdzp, ftk_floor;
+  float fxc[3];   // T21/Trad * {No, N_b0, No} * (1+z)^3 / A10
+  float ftgp;     // 1.342881e-7 / H(z) * No * (1+z)^3
+  float fxa;      // 1.66e11 / (1+z)
+  float fkx[3][27], fky[3][27], fkc[3][27];
 };
 
 struct EvolveArgs
@@ -171,7 +195,7 @@ struct DeltaTArgs
   const float* TS;
   float* delta_T;
   float const_factor;
-  double T_rad;
+  float T_rad_f;
   float redshift;
   int spin, pecvel;
   double* partials;  // RED_BLOCKS x 1
@@ -180,5 +204,6 @@ void launch_delta_T(const DeltaTArgs& a, const GridDims& gd, cudaStream_t s);
 
 int kernel_launch_count();
 void reset_kernel_launch_count();
+int ts_kernel_launches();
 
 }  // namespace mx

@@ -67,7 +67,8 @@ struct mx_ctx
 
   RecombTable rr;
   HeatTables ht;
-  double *d_rr_x = nullptr, *d_rr_y = nullptr, *d_rr_c = nullptr;
+  float *d_rr_x = nullptr, *d_rr_y = nullptr, *d_rr_c = nullptr;  // FP32 copies, values scaled by rr_scale
+  double rr_scale = 1.0;
 
   // scratch
   float2* d_unf = nullptr;      // MAX_FIELDS x C
@@ -327,6 +328,9 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
       q.Gamma_pref *= (p.unit_mass_g / c->d.unit_time_s) * std::pow(p.unit_length_cm / p.hubble_h, -3.) *
                       p.nion_phot_per_bary / k::PROTONMASS;
     }
+    q.kfc = (float)(p.reion_efficiency * (4.0 / 3.0) * k::PI * q.R_cubed / (q.M_mean * pixel_volume));
+    q.kj = (float)(q.J21_const / pixel_volume);
+    q.kg = (float)(q.Gamma_pref / pixel_volume);
   }
   MX_CUDA(cudaMemcpyAsync(c->d_rp, rps.data(), sizeof(RadiusParams) * nR, cudaMemcpyHostToDevice, s));
 
@@ -391,9 +395,10 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
   ra.deltax = g->deltax;
   ra.Gamma12 = g->Gamma12;
   ra.N_rec = g->N_rec;
-  ra.rr_x = c->d_rr_x;
-  ra.rr_y = c->d_rr_y;
-  ra.rr_c = c->d_rr_c;
+  ra.rr_xf = c->d_rr_x;
+  ra.rr_yf = c->d_rr_y;
+  ra.rr_cf = c->d_rr_c;
+  ra.rr_scale_inv = (float)(1.0 / c->rr_scale);
   ra.redshift = redshift;
   ra.fabs_dtdz = fabs_dtdz;
   ra.zstep = zstep;
@@ -449,6 +454,74 @@ static void fill_common_ts(mx_ctx* c, TsDevConst* t, double zp)
   for (int i = 0; i < 14; i++)
     t->xhii[i] = c->ht.xhii[i];
   fill_kappa(c, t);
+  // FP32 constants of get_Ts (XRayHeatingFunctions.c:1513-1600, 1847-1882)
+  const float zpf = (float)zp;
+  const double opz = (double)(1.0f + zpf);
+  const double Trad = k::TCMB * opz;
+  const double p3 = std::pow(opz, 3.0);
+  t->ftrad = (float)Trad;
+  t->fxc[0] = (float)(k::T21 / Trad * c->d.no * p3 / k::A10);
+  t->fxc[1] = (float)(k::T21 / Trad * c->d.n_b0 * p3 / k::A10);
+  t->fxc[2] = t->fxc[0];
+  t->ftgp = (float)(1.342881e-7 / t->hubble_z * c->d.no * p3);
+  t->fxa = (float)(1.66e11 / opz);
+  t->ff_he = (float)c->d.f_he;
+  t->ftk_floor = (float)(k::TCMB * (1 + zp));
+  for (int w = 0; w < 3; w++)
+    for (int i = 0; i < t->nk[w]; i++) {
+      t->fkx[w][i] = (float)t->kx[w][i];
+      t->fky[w][i] = (float)t->ky[w][i];
+      t->fkc[w][i] = (float)t->kc[w][i];
+    }
+}
+
+// Power of two that brings |v| to [0.5, 1) (1 for v == 0).
+static double pow2_scale(double v)
+{
+  if (!(v > 0.0) || !std::isfinite(v))
+    return 1.0;
+  int e;
+  std::frexp(v, &e);
+  return std::ldexp(1.0, -e);
+}
+
+// FP32 per-shell coefficients of evolveInt (see TsDevConst).
+static void fill_fast_evolve(mx_ctx* c, TsDevConst* t, const ShellPlan& sp, const FreqTables& ft, double zp)
+{
+  const int S = t->S;
+  const float zpf = (float)zp;
+  const double opz = (double)(1.0f + zpf);
+  const double U = (1.0 / t->pixel_volume) * t->sfr_a * t->sfr_b / k::SOLAR_MASS;
+  const double Trad = k::TCMB * opz;
+  for (int r = 0; r < S; r++) {
+    const double base = U * sp.a_dt_dz[r] * sp.b_pow[r] * ft.const_zp_prefactor;
+    double K[3] = { base * ft.dt_dzp * 2.0 / 3.0 / k::BOLTZMANN, base * ft.dt_dzp, base * c->d.n_b0 * t->p3 };
+    for (int w = 0; w < 3; w++) {
+      double m = 0.0;
+      for (int x = 0; x < 14; x++)
+        m = std::max(m, std::fabs(ft.tab[((size_t)w * 14 + x) * S + r]));
+      const double sc = pow2_scale(m);
+      for (int x = 0; x < 14; x++)
+        t->ftab[w][x][r] = (float)(ft.tab[((size_t)w * 14 + x) * S + r] * sc);
+      K[w] /= sc;
+    }
+    t->fKH[r] = (float)K[0];
+    t->fKI[r] = (float)K[1];
+    t->fKL[r] = (float)K[2];
+    t->fKS[r] = (float)(U * t->p2 * sp.zpp1[r] * ft.sum_lyn[r] * sp.dt_dzpp[r] * sp.dzpp[r] * t->conv);
+  }
+  t->fksink = (float)(ft.dt_dzp * c->p.clumping_factor * c->d.f_h * c->d.n_b0 * t->p3);
+  t->fadia0 = (float)(3 / (1.0 + zpf));
+  t->fdgrowth = (float)ft.dgrowth_dzp;
+  t->fgrowth = (float)ft.growth_zp;
+  t->fccomp = (float)((-1.51e-4) / (t->hubble_z / (k::HUBBLE * c->p.hubble_h)) / c->p.hubble_h * std::pow(Trad, 4.0) /
+                      (1.0 + zpf));
+  t->fdzp = (float)t->dzp;
+  const float* fl[] = { t->fKH, t->fKI, t->fKL, t->fKS };
+  for (const float* q : fl)
+    for (int r = 0; r < S; r++)
+      if (!std::isfinite(q[r]) || (q[r] != 0.0f && std::fabs(q[r]) < 1e-30f))
+        throw CudaError{ MX_ENOTSUP, "ComputeTs: coefficient outside the FP32 range" };
 }
 
 static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s)
@@ -626,6 +699,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
         for (int w = 0; w < 3; w++)
           t->tab[w][x][q] = ft.tab[((size_t)w * 14 + x) * S + q];
     }
+    fill_fast_evolve(c, t, sp, ft, zp);
     MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
     EvolveArgs ea;
     ea.shells = c->d_shells;
@@ -702,7 +776,7 @@ static void run_delta_T(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* 
   DeltaTArgs a;
   a.const_factor = (float)(27.0 * (OmegaB * Hubble_h * Hubble_h / 0.023) *
                            std::sqrt((0.15 / OmegaM / Hubble_h / Hubble_h) * (1.0 + redshift) / 10.0));
-  a.T_rad = k::TCMB * (1. + redshift);
+  a.T_rad_f = (float)(k::TCMB * (1. + redshift));
   a.redshift = redshift;
   a.deltax = g->deltax;
   a.xH = g->xH;
@@ -814,12 +888,25 @@ int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out)
     if (p.flag_recombinations) {
       c->rr.build(p, c->d, c->nthreads);
       const size_t n = c->rr.y.size();
-      MX_CUDA(cudaMalloc(&c->d_rr_x, sizeof(double) * c->rr.lng.size()));
-      MX_CUDA(cudaMalloc(&c->d_rr_y, sizeof(double) * n));
-      MX_CUDA(cudaMalloc(&c->d_rr_c, sizeof(double) * n));
-      MX_CUDA(cudaMemcpy(c->d_rr_x, c->rr.lng.data(), sizeof(double) * c->rr.lng.size(), cudaMemcpyHostToDevice));
-      MX_CUDA(cudaMemcpy(c->d_rr_y, c->rr.y.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-      MX_CUDA(cudaMemcpy(c->d_rr_c, c->rr.c.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+      // FP32 copy of the table, rescaled by a power of two to O(1) values
+      double m = 0.0;
+      for (size_t i = 0; i < n; i++)
+        if (std::isfinite(c->rr.y[i]))
+          m = std::max(m, std::fabs(c->rr.y[i]));
+      int e = 0;
+      std::frexp(m > 0 ? m : 1.0, &e);
+      c->rr_scale = std::ldexp(1.0, -e);
+      std::vector<float> xf(c->rr.lng.begin(), c->rr.lng.end()), yf(n), cf(n);
+      for (size_t i = 0; i < n; i++) {
+        yf[i] = (float)(c->rr.y[i] * c->rr_scale);
+        cf[i] = (float)(c->rr.c[i] * c->rr_scale);
+      }
+      MX_CUDA(cudaMalloc(&c->d_rr_x, sizeof(float) * xf.size()));
+      MX_CUDA(cudaMalloc(&c->d_rr_y, sizeof(float) * n));
+      MX_CUDA(cudaMalloc(&c->d_rr_c, sizeof(float) * n));
+      MX_CUDA(cudaMemcpy(c->d_rr_x, xf.data(), sizeof(float) * xf.size(), cudaMemcpyHostToDevice));
+      MX_CUDA(cudaMemcpy(c->d_rr_y, yf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+      MX_CUDA(cudaMemcpy(c->d_rr_c, cf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     }
     c->alloc_scratch();
   } catch (const CudaError& e) {
