@@ -1,0 +1,57 @@
+// Fused inverse 3-D transforms for power-of-two grids (see fft3d.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace mx {
+
+// x-pass: filter + 1/N scale + inverse FFT along x for a batch of radii.
+struct XPassArgs
+{
+  const float2* in[MAX_FIELDS];  // unfiltered, unnormalised half spectra
+  int G;                          // fields
+  int n;                          // radii in the batch
+  float2* out;                    // spectrum (r*G + g) at out + (r*G + g)*C
+  long long C;
+  float R[MAX_RADII];
+  int apply[MAX_RADII];
+  int filter_type;
+  float delta_k;
+  float scale;       // 1/N (exact for power-of-two N)
+  float sharpk_max;  // set by launch_fft_x_filter
+};
+
+// z-pass fused with the find_HII_bubbles per-cell test.
+struct ZThresholdArgs
+{
+  const float2* spectra;  // batch spectra after the x and y passes
+  long long C;
+  int G, idx_xe, idx_nr;
+  int n_r;  // radii of the batch
+  int n_f;  // of which filtered (spectra r*G + g for r < n_f); a last radius
+            // with rp.last set reads the input grids directly
+  const RadiusParams* rp;
+  const float* direct[MAX_FIELDS];  // PADDED input grids for the unfiltered step
+  float* xH;
+  float* z_at_ion;
+  float* r_bubble;
+  float* J21;
+  float* J21_at_ion;
+  float* Gamma12;
+  double pixel_volume, eff, redshift;
+  float gamma_halo_bias;
+  int uvb, recomb, spin;
+  unsigned* err;  // bit 2: a pipeline wait timed out
+};
+
+bool fft3d_supported(int D);
+bool launch_fft_x_filter(int D, const XPassArgs& a, cudaStream_t s);
+bool launch_fft_y(int D, float2* data, long long C, int n_spectra, cudaStream_t s);
+bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s);
+bool launch_fft_z_store(int D, const float2* spectra, long long C, int n, int r0, float* shells, long long N,
+                        unsigned* err, cudaStream_t s);
+int fft_kernel_launches();
+
+}  // namespace mx

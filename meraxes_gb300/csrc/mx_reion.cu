@@ -16,6 +16,7 @@
 #include <thread>
 #include <vector>
 
+#include "fft3d.cuh"
 #include "host_physics.h"
 #include "kernels.cuh"
 #include "mx_reion.h"
@@ -64,6 +65,9 @@ struct mx_ctx
   cudaStream_t stream = nullptr;
   int device = 0;
   int nthreads = 4;
+  // inverse transforms: fused three-pass kernels for power-of-two grids
+  // (fft3d.cu), cuFFT otherwise or when MX_TRANSFORM=cufft
+  bool fused_fft = false;
 
   RecombTable rr;
   HeatTables ht;
@@ -340,6 +344,60 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
     const int nb = std::min(per_batch, nR - r0);
     // the last, unfiltered step is read from the input grids (identity transform)
     const int nf = (r0 + nb == nR) ? nb - 1 : nb;
+    const int nstate = 3 + (uvb ? 2 : 0) + (recomb ? 1 : 0);
+    if (c->fused_fft) {
+      // fused three-pass inverse transform (fft3d.cu)
+      if (nf > 0) {
+        XPassArgs xa;
+        for (int f = 0; f < MAX_FIELDS; f++)
+          xa.in[f] = f < G ? unf_ptrs[f] : nullptr;
+        xa.G = G;
+        xa.n = nf;
+        xa.out = c->d_work;
+        xa.C = gd.C;
+        for (int r = 0; r < nf; r++) {
+          xa.R[r] = (float)radii[r0 + r];
+          xa.apply[r] = 1;
+        }
+        xa.filter_type = p.filter_type;
+        xa.delta_k = (float)(2.0 * k::PI / (float)p.box_size);
+        xa.scale = (float)(1.0 / (double)gd.N);
+        {
+          Prof pr(c, "fft_x_filter", (double)G * B8C * (1 + nf), s);
+          launch_fft_x_filter(gd.D, xa, s);
+        }
+        Prof pr(c, "fft_y", 2.0 * G * nf * B8C, s);
+        launch_fft_y(gd.D, c->d_work, gd.C, nf * G, s);
+      }
+      ZThresholdArgs za;
+      za.spectra = c->d_work;
+      za.C = gd.C;
+      za.G = G;
+      za.idx_xe = idx_xe;
+      za.idx_nr = idx_nr;
+      za.n_r = nb;
+      za.n_f = nf;
+      za.rp = c->d_rp + r0;
+      for (int f = 0; f < MAX_FIELDS; f++)
+        za.direct[f] = f < G ? src[f] : nullptr;
+      za.xH = g->xH;
+      za.z_at_ion = g->z_at_ionization;
+      za.r_bubble = g->r_bubble;
+      za.J21 = g->J_21;
+      za.J21_at_ion = g->J_21_at_ionization;
+      za.Gamma12 = g->Gamma12;
+      za.pixel_volume = pixel_volume;
+      za.eff = p.reion_efficiency;
+      za.redshift = redshift;
+      za.gamma_halo_bias = (float)p.gamma_halo_bias;
+      za.uvb = uvb;
+      za.recomb = recomb;
+      za.spin = spin;
+      za.err = c->d_err;
+      Prof pr(c, "fft_z_threshold", (double)G * nf * B8C + ((double)(nb - nf) * G + 2.0 * nstate) * B4N, s);
+      launch_fft_z_threshold(gd.D, za, s);
+      continue;
+    }
     FilterBatch fb;
     fb.n = nf;
     fb.filter_type = p.filter_type;
@@ -383,7 +441,6 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
     ta.uvb = uvb;
     ta.recomb = recomb;
     ta.spin = spin;
-    const int nstate = 3 + (uvb ? 2 : 0) + (recomb ? 1 : 0);
     Prof pr(c, "k_threshold", ((double)nb * G + 2.0 * nstate) * B4N, s);
     launch_threshold(ta, gd, s);
   }
@@ -411,7 +468,13 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
   }
   launch_finalize(c->d_partials, 4, c->d_sums, s);
   MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  unsigned int errw = 0;
+  MX_CUDA(cudaMemcpyAsync(&errw, c->d_err, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
   MX_CUDA(cudaStreamSynchronize(s));
+  if (errw) {
+    MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
+    throw CudaError{ MX_ECUDA, "find_HII_bubbles: a transform pipeline wait timed out" };
+  }
   const double total = std::pow((double)gd.D, 3);
   if (out) {
     out->volume_weighted_global_xH = c->h_sums[0] / total;
@@ -640,7 +703,37 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
         float2* in_ptr[1] = { sfr_unf };
         MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, in_ptr, sizeof(float2*), cudaMemcpyHostToDevice, s));
         for (int q0 = q_first; q0 < r_end;) {
-          const int nb = (int)std::min<long long>(c->work_fields, r_end - q0);
+          const int nb = (int)std::min<long long>(std::min<long long>(c->work_fields, MAX_RADII), r_end - q0);
+          if (c->fused_fft) {
+            XPassArgs xa;
+            for (int f = 0; f < MAX_FIELDS; f++)
+              xa.in[f] = f == 0 ? sfr_unf : nullptr;
+            xa.G = 1;
+            xa.n = nb;
+            xa.out = c->d_work;
+            xa.C = gd.C;
+            for (int q = 0; q < nb; q++) {
+              xa.R[q] = (float)sp.R[q0 + q];
+              xa.apply[q] = 1;
+            }
+            xa.filter_type = p.ts_heating_filter_type;
+            xa.delta_k = (float)(2.0 * k::PI / (float)p.box_size);
+            xa.scale = (float)(1.0 / (double)gd.N);
+            {
+              Prof pr(c, "fft_x_filter", 8.0 * (double)gd.C * (1 + nb), s);
+              launch_fft_x_filter(gd.D, xa, s);
+            }
+            {
+              Prof pr(c, "fft_y", 16.0 * (double)gd.C * nb, s);
+              launch_fft_y(gd.D, c->d_work, gd.C, nb, s);
+            }
+            {
+              Prof pr(c, "fft_z_store", (8.0 * (double)gd.C + 4.0 * (double)gd.N) * nb, s);
+              launch_fft_z_store(gd.D, c->d_work, gd.C, nb, q0, c->d_shells, gd.N, c->d_err, s);
+            }
+            q0 += nb;
+            continue;
+          }
           FilterBatch fb;
           fb.n = nb;
           fb.filter_type = p.ts_heating_filter_type;
@@ -739,7 +832,8 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
   MX_CUDA(cudaStreamSynchronize(s));
   if (errw) {
     MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
-    throw CudaError{ MX_ECUDA, "ComputeTs: spin-temperature iteration did not converge" };
+    throw CudaError{ MX_ECUDA, (errw & 2u) ? "ComputeTs: a transform pipeline wait timed out"
+                                           : "ComputeTs: spin-temperature iteration did not converge" };
   }
   if (out) {
     if (!sp.homogeneous) {
@@ -873,6 +967,10 @@ int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out)
   c->nthreads = std::max(1, std::min(64, hw_threads()));
   if (const char* env = std::getenv("MX_HOST_THREADS"))
     c->nthreads = std::max(1, std::atoi(env));
+  c->fused_fft = fft3d_supported(p.grid_dim);
+  if (const char* env = std::getenv("MX_TRANSFORM"))
+    if (std::string(env) == "cufft")
+      c->fused_fft = false;
   try {
     if (cudaGetDevice(&c->device) != cudaSuccess)
       throw CudaError{ MX_ECUDA, "no CUDA device" };

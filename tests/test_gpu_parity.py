@@ -48,9 +48,8 @@ def test_gpu_matches_reference_fixture(name):
     print(name, rep)
 
 
-@pytest.mark.parametrize("name,D", [("plain32_tophat", 64), ("plain32_sharpk", 64), ("plain32_gauss", 48),
-                                    ("full24", 48), ("evolve16", 32)])
-def test_gpu_matches_oracle_with_margins(name, D, tables_dir):
+def _run_against_oracle(name, D, tables_dir):
+    from cases import initial
     from meraxes_gb300 import synthetic as syn
     from oracle import OracleBackend
 
@@ -60,8 +59,6 @@ def test_gpu_matches_oracle_with_margins(name, D, tables_dir):
     orc = OracleBackend(w.params, w.redshifts, tables_dir)
     gpu = GpuBackend(w.params, w.redshifts)
     gen = syn.FieldGenerator(w)
-    from cases import initial
-
     sa = initial(w, orc.n_sfr_histories)
     sb = {k: v.copy() for k, v in sa.items()}
     for s in w.snapshots:
@@ -73,7 +70,23 @@ def test_gpu_matches_oracle_with_margins(name, D, tables_dir):
         gb = gpu.step(s, sb)
         rep = {}
         compare(sa, sb, ga, gb, margin=margin, report=rep)
-    print(name, D, rep)
+    return rep
+
+
+@pytest.mark.parametrize("name,D", [("plain32_tophat", 64), ("plain32_sharpk", 64), ("plain32_gauss", 48),
+                                    ("full24", 48), ("evolve16", 32)])
+def test_gpu_matches_oracle_with_margins(name, D, tables_dir):
+    print(name, D, _run_against_oracle(name, D, tables_dir))
+
+
+# Power-of-two grids run the fused three-pass inverse transforms by default;
+# MX_TRANSFORM=cufft selects cuFFT C2R with separate filter and test passes.
+# Both must meet the same tolerances against the oracle.
+@pytest.mark.parametrize("transform", ["fused", "cufft"])
+@pytest.mark.parametrize("name,D", [("full24", 64), ("plain32_gauss", 64), ("evolve16", 32)])
+def test_both_transform_paths_match_oracle(name, D, transform, tables_dir, monkeypatch):
+    monkeypatch.setenv("MX_TRANSFORM", transform)
+    print(name, D, transform, _run_against_oracle(name, D, tables_dir))
 
 
 def test_device_entry_points_match_host_entry_points():
