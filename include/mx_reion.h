@@ -35,6 +35,7 @@
 #ifndef MX_REION_H
 #define MX_REION_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -208,6 +209,40 @@ int32_t mx_profile_read(mx_ctx* ctx, mx_kernel_stat* out, int32_t cap);
 
 /* Build information: returns a static string. */
 const char* mx_build_info(void);
+
+/* Brightness-temperature box without any device allocation.  No counterpart
+ * in the reference: it is the computation of
+ * ComputeBrightnessTemperatureBox (BrightnessTemperature.c:495-545) for
+ * callers that cannot allocate device memory.  A host that keeps all its
+ * grids resident has often given the rest of the GPU to its own pool.  A
+ * thread that must not stall cannot call cudaMalloc/cudaFree, which may
+ * synchronise the device.  No context is needed.  All pointers are device
+ * pointers in the run_globals.reion_grids layouts (deltax PADDED, the others
+ * REAL).  delta_T is written; *volume_ave_Tb (one device double) receives the
+ * volume average.  The work is queued on `stream` and the call does not wait.
+ *
+ * Scratch: a fixed MX_NOALLOC_SCRATCH_BYTES __device__ array inside the
+ * library, shared by every call on a device.  It holds one partial sum per
+ * 16384 cells and a completion ticket that must be zero when a launch starts.
+ * Each call zeroes the ticket on `stream` before its kernel.  Grids above
+ * MX_NOALLOC_MAX_CELLS cells (512^3) are rejected with MX_EINVAL.  Calls that
+ * overlap in time on one device (different streams or threads, not ordered
+ * by the caller) race on that scratch and give wrong means: serialise them.
+ * The first call on each device looks up the scratch address for that device
+ * (with it current).  Make that first call before starting any stream
+ * capture.  On error the message goes to errbuf (may be NULL). */
+#define MX_NOALLOC_MAX_CELLS 134217728
+#define MX_NOALLOC_SCRATCH_BYTES 65792
+int mx_brightness_temperature_noalloc(const mx_params* params,
+                                      double redshift,
+                                      const float* deltax,
+                                      const float* xH,
+                                      const float* TS_box,
+                                      float* delta_T,
+                                      double* volume_ave_Tb,
+                                      void* stream,
+                                      char* errbuf,
+                                      size_t errlen);
 
 #ifdef __cplusplus
 }

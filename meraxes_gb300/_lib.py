@@ -23,6 +23,7 @@ EXPORTS = [
     "mx_find_HII_bubbles", "mx_ComputeTs", "mx_ComputeBrightnessTemperatureBox", "mx_step",
     "mx_find_HII_bubbles_device", "mx_ComputeTs_device", "mx_ComputeBrightnessTemperatureBox_device",
     "mx_step_device", "mx_profile_enable", "mx_profile_read", "mx_build_info",
+    "mx_brightness_temperature_noalloc",
 ]
 
 
@@ -82,5 +83,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mx_profile_read.restype = ctypes.c_int32
         L.mx_build_info.argtypes = []
         L.mx_build_info.restype = ctypes.c_char_p
+        L.mx_brightness_temperature_noalloc.argtypes = [ctypes.POINTER(MxParams), ctypes.c_double, P, P, P, P, P, P,
+                                                        ctypes.c_char_p, ctypes.c_size_t]
+        L.mx_brightness_temperature_noalloc.restype = ctypes.c_int
         _LIB = L
         return L

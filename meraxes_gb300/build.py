@@ -1,6 +1,6 @@
 """Build of the in-tree CUDA library libmxreion.so (sm_103a).
 
-The library is compiled with nvcc directly: three translation units compiled
+The library is compiled with nvcc directly: the translation units compiled
 in parallel, then linked with cuFFT.  The output goes to meraxes_gb300/_lib/.
 """
 from __future__ import annotations
@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libmxreion.so")
-SOURCES = ["kernels.cu", "kernels_ts.cu", "fft3d.cu", "mx_reion.cu", "host_physics.cpp"]
+SOURCES = ["kernels.cu", "kernels_ts.cu", "fft3d.cu", "mx_reion.cu", "host_physics.cpp", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
