@@ -181,7 +181,9 @@ int mx_ComputeBrightnessTemperatureBox(mx_ctx* ctx, int32_t snapshot, const mx_g
  * temperature (if flag_21cm), the order of dracarys.c:352-390. */
 int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out);
 
-/* Device-pointer entry points. */
+/* Device-pointer entry points.  Every non-NULL grid pointer must be 8-byte
+ * aligned (cuFFT's requirement for its real inputs; cudaMalloc and
+ * fftwf_malloc give 256 and 16 bytes); other pointers return MX_EINVAL. */
 int mx_find_HII_bubbles_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream);
 int mx_ComputeTs_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream);
 int mx_ComputeBrightnessTemperatureBox_device(mx_ctx* ctx,

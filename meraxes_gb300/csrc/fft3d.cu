@@ -29,7 +29,6 @@ namespace mx {
 namespace {
 constexpr int FFT_THREADS = 256;
 constexpr int TX = 16;  // columns (kz) per x/y tile
-constexpr int TZ = 4;   // rows (y) per z tile
 constexpr float REL_TOL_F = 1e-5f;
 constexpr float ABS_TOL_F = 1e-8f;
 constexpr double PI_D = 3.14159265358979323846;
@@ -304,7 +303,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_y(float2* data, long long C
 }
 
 // ------------------------------------------------------------------ z-pass
-// The z-pass reads, per block, TZ consecutive rows (x, y0 .. y0+TZ-1) of every
+// The z-pass reads, per block, TZ consecutive rows (row = x * D + y) of every
 // spectrum of the batch: TZ*H contiguous complex values.  These row groups are
 // streamed into shared memory by bulk asynchronous copies (cp.async.bulk,
 // completion on an mbarrier) through a ZSTAGES-deep ring, so that the copies
@@ -375,25 +374,158 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
   return false;
 }
 
-// Shared-memory plan of a z-pass block.
+// Geometry of the z-pass.  A block of 256 threads owns TZ = 2048 / D rows
+// (2048 cells, 8 per thread).  Each row's C2R of D points is computed as one
+// complex inverse DFT of D/2 points: with w = exp(2 pi i / D),
+//   Z[k] = E[k] + i O[k],  E[k] = X[k] + conj(X[D/2-k]),
+//   O[k] = (X[k] - conj(X[D/2-k])) w^k,        k < D/2,
+// and z = IDFT_{D/2}(Z) gives x[2m] = Re z[m], x[2m+1] = Im z[m].
+// The D/2 points split as P1 x P2 (four-step); each P-point DFT is done by
+// P/4 consecutive lanes holding 4 points each: a 4-point DFT in registers,
+// twiddles, then a P/4-point DFT across the lanes (shuffles).  Every thread
+// has exactly one lane-part in each of the two steps.
+template <int D>
+struct ZS;
+template <>
+struct ZS<32>
+{
+  static constexpr int P1 = 4, P2 = 4, PAD = 1;
+};
+template <>
+struct ZS<64>
+{
+  static constexpr int P1 = 8, P2 = 4, PAD = 1;
+};
+template <>
+struct ZS<128>
+{
+  static constexpr int P1 = 8, P2 = 8, PAD = 2;
+};
+template <>
+struct ZS<256>
+{
+  static constexpr int P1 = 8, P2 = 16, PAD = 2;
+};
+template <>
+struct ZS<512>
+{
+  static constexpr int P1 = 16, P2 = 16, PAD = 4;
+};
+
 template <int D>
 struct ZPlan
 {
-  static constexpr int D1 = Split<D>::D1, D2 = Split<D>::D2, H = D / 2 + 1;
-  static constexpr int STAGE = TZ * H;          // complex values per stage
-  static constexpr int BT = D1 * (D2 + 1);      // padded transpose buffer per row
-  static constexpr int OS = D + D1;             // padded real output row
-  static constexpr size_t OFF_TW = 64;          // after the barriers
-  static constexpr size_t OFF_STAGE = OFF_TW + sizeof(float2) * D;
+  static constexpr int H = D / 2 + 1, DH = D / 2;
+  static constexpr int TZ = 2048 / D;  // rows per block
+  static constexpr int P1 = ZS<D>::P1, P2 = ZS<D>::P2;
+  static constexpr int L1 = P1 / 4, L2 = P2 / 4;
+  static constexpr int RS = P2 + ZS<D>::PAD;  // padded row of the transpose buffer
+  static constexpr int BROW = P1 * RS;
+  static constexpr int STAGE = TZ * H;  // complex values per stage
+  static constexpr int BUF = TZ * BROW;
+  static constexpr size_t OFF_STAGE = 64;  // after the barriers
   static constexpr size_t OFF_BUF = OFF_STAGE + sizeof(float2) * (size_t)ZSTAGES * STAGE;
-  static constexpr size_t OFF_FLD = OFF_BUF + sizeof(float2) * (size_t)TZ * BT;
-  static constexpr size_t bytes(int fields) { return OFF_FLD + sizeof(float) * (size_t)fields * TZ * OS; }
+  static constexpr size_t BYTES = OFF_BUF + sizeof(float2) * 2 * (size_t)BUF;
+  static_assert(P1 * P2 == DH, "split");
+  static_assert(TZ * P2 * L1 == FFT_THREADS && TZ * P1 * L2 == FFT_THREADS, "one lane-part per thread");
   static_assert((sizeof(float2) * STAGE) % 16 == 0, "bulk copy size");
   static_assert(OFF_STAGE % 16 == 0, "bulk copy destination");
+  static_assert(D % TZ == 0 || TZ % D == 0, "rows");
 };
 
-// The producer side of the ring: thread 0 issues item `it` into stage
-// it % ZSTAGES.  Item it is spectrum it (of C complex values), rows row0 ..
+// index of the output held in slot e by lane-part l of an L-lane DFT
+__device__ __forceinline__ int lane_out(int L, int e, int l) { return L == 4 ? l + 4 * e : e + 4 * l; }
+
+__device__ __forceinline__ void dft4_bwd(float2 (&v)[4])
+{
+  const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+  const float2 t2 = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+  const float2 t3 = make_float2(-d.y, d.x);  // i (v1 - v3)
+  v[0] = cadd(t0, t2);
+  v[1] = cadd(t1, t3);
+  v[2] = csub(t0, t2);
+  v[3] = csub(t1, t3);
+}
+
+__device__ __forceinline__ float2 shfl_xor2(float2 v, int m)
+{
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+// The L-point DFT across the L lane-parts (lane l holds u[c] = U_l[c]); on
+// return slot e holds output lane_out(L, e, l).
+template <int L>
+__device__ __forceinline__ void cross_lane(float2 (&u)[4], int l)
+{
+  if constexpr (L == 2) {
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const float2 p = shfl_xor2(u[c], 1);
+      u[c] = l == 0 ? cadd(u[c], p) : csub(p, u[c]);
+    }
+  } else if constexpr (L == 4) {
+    // 4 x 4 transpose across the lanes: slot m of lane q becomes U_m[q]
+#pragma unroll
+    for (int s = 1; s < 4; s++) {
+      const int j = l ^ s;
+      const float2 lo = (j & 1) ? u[1] : u[0], hi = (j & 1) ? u[3] : u[2];
+      const float2 r = shfl_xor2((j & 2) ? hi : lo, s);
+      u[0] = j == 0 ? r : u[0];
+      u[1] = j == 1 ? r : u[1];
+      u[2] = j == 2 ? r : u[2];
+      u[3] = j == 3 ? r : u[3];
+    }
+    dft4_bwd(u);
+  }
+}
+
+// One 4-point lane-part of a P-point DFT whose 4 points (stride L = P/4) are
+// in v: 4-point DFT, twiddles exp(2 pi i l c / P) = w1^c (w1 = exp(2 pi i l /
+// P)), cross-lane step.
+template <int P>
+__device__ __forceinline__ void lane_dft(float2 (&v)[4], int l, float2 w1)
+{
+  dft4_bwd(v);
+  if (P > 4) {
+    const float2 w2 = cmul(w1, w1);
+    v[1] = cmul(v[1], w1);
+    v[2] = cmul(v[2], w2);
+    v[3] = cmul(v[3], cmul(w2, w1));
+  }
+  cross_lane<P / 4>(v, l);
+}
+
+__device__ __forceinline__ float2 unit(int j, int n)
+{
+  float s, c;
+  sincospif(2.0f * (float)j / (float)n, &s, &c);
+  return make_float2(c, s);
+}
+
+// Per-thread twiddle factors of the z-pass.  A thread's step-A and step-B
+// roles are fixed for the whole kernel, so its twiddles are a few base values
+// kept in registers; the others follow by complex products.
+template <int D>
+struct ZTw
+{
+  float2 kb, kr;  // w_D^k for the 4 points: kb * kr^i
+  float2 fb, fs;  // four-step w_{D/2}^{n2 k1} for slot e: fb * fs^e
+  float2 la, lb;  // lane twiddles of steps A and B
+  __device__ __forceinline__ void init()
+  {
+    constexpr int P1 = ZS<D>::P1, P2 = ZS<D>::P2, L1 = P1 / 4, L2 = P2 / 4, DH = D / 2;
+    const int l = threadIdx.x % L1, n2 = (threadIdx.x / L1) % P2;
+    kb = unit(n2 + P2 * l, D);
+    kr = unit(P2 * L1, D);
+    const int k10 = lane_out(L1, 0, l), dk1 = lane_out(L1, 1, l) - k10;
+    fb = unit((n2 * k10) % DH, DH);
+    fs = unit((n2 * dk1) % DH, DH);
+    la = unit(l, P1);
+    lb = unit(threadIdx.x % L2, P2);
+  }
+};
+
+// Producer side of the ring: thread 0 issues item `it` into stage it % ZSTAGES.
 template <int D>
 __device__ __forceinline__ void z_issue(char* smem, const float2* spectra, long long C, long long row0, int it)
 {
@@ -404,77 +536,78 @@ __device__ __forceinline__ void z_issue(char* smem, const float2* spectra, long 
             &bars[it % ZSTAGES]);
 }
 
-// Inverse C2R along z of the TZ staged rows of item `it` into out[t*OS + z].
-// Returns false (for every thread of the block) if the copy did not arrive.
-// Thread 0 refills the stage with item it + ZSTAGES (< n_items) as soon as
-// every thread has read it.
+// C2R along z of the TZ staged rows of item `it`.  On return z[e] holds
+// (x[2m], x[2m+1]) of row (threadIdx.x / (L2 * P1)) for
+// m = k1 + P1 * lane_out(L2, e, l), k1 = (threadIdx.x / L2) % P1,
+// l = threadIdx.x % L2.  Returns false (for every thread) if the copy did not
+// arrive.  One block barrier per call: the transpose buffer alternates.
 template <int D>
 __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const float2* spectra, long long C,
-                                      long long row0, float* out)
+                                      long long row0, const ZTw<D>& w, float2 (&z)[4])
 {
   using P = ZPlan<D>;
-  constexpr int D1 = P::D1, D2 = P::D2, H = P::H;
+  constexpr int H = P::H, DH = P::DH, P1 = P::P1, P2 = P::P2, L1 = P::L1, L2 = P::L2;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
-  const float2* tw = reinterpret_cast<const float2*>(smem + P::OFF_TW);
   const float2* st = reinterpret_cast<const float2*>(smem + P::OFF_STAGE) + (size_t)(it % ZSTAGES) * P::STAGE;
-  float2* buf = reinterpret_cast<float2*>(smem + P::OFF_BUF);
+  float2* buf = reinterpret_cast<float2*>(smem + P::OFF_BUF) + (size_t)(it & 1) * P::BUF;
   const bool arrived = mbar_wait(&bars[it % ZSTAGES], (unsigned)(it / ZSTAGES) & 1u);
-  // step A: D1-point DFTs along n1 (Hermitian-extended input), twiddles
-  for (int item = threadIdx.x; item < TZ * D2; item += FFT_THREADS) {
-    const int n2 = item % D2, t = item / D2;
+  {
+    // step A: row t, column n2, lane-part l of the P1-point DFT over n1
+    const int l = threadIdx.x % L1, n2 = (threadIdx.x / L1) % P2, t = threadIdx.x / (L1 * P2);
     const float2* row = st + t * H;
-    float2 v[D1];
+    float2 v[4];
+    float2 tk = w.kb;
 #pragma unroll
-    for (int n1 = 0; n1 < D1; n1++) {
-      const int k = n2 + D2 * n1;
-      float2 x;
-      if (k < H) {
-        x = row[k];
-        if (k == 0 || k == D / 2)
-          x.y = 0.0f;
-      } else {
-        const float2 c = row[D - k];
-        x = make_float2(c.x, -c.y);
+    for (int i = 0; i < 4; i++) {
+      const int k = n2 + P2 * (l + L1 * i);
+      float2 A = row[k];
+      float2 B = row[DH - k];
+      if (k == 0) {
+        A.y = 0.0f;  // imaginary parts of kz = 0 and kz = D/2 are ignored
+        B.y = 0.0f;
       }
-      v[n1] = x;
+      B.y = -B.y;
+      const float2 E = cadd(A, B);
+      const float2 O = cmul(csub(A, B), tk);
+      v[i] = make_float2(E.x - O.y, E.y + O.x);
+      if (i < 3)
+        tk = cmul(tk, w.kr);
     }
-    dft_bwd<D1, D>(v, tw);
+    lane_dft<P1>(v, l, w.la);
+    float2 tf = w.fb;
 #pragma unroll
-    for (int k1 = 0; k1 < D1; k1++)
-      buf[t * P::BT + k1 * (D2 + 1) + n2] = k1 == 0 || n2 == 0 ? v[k1] : cmul(v[k1], tw[(n2 * k1) % D]);
+    for (int e = 0; e < 4; e++) {
+      const int k1 = lane_out(L1, e, l);
+      buf[t * P::BROW + k1 * P::RS + n2] = cmul(v[e], tf);
+      if (e < 3)
+        tf = cmul(tf, w.fs);
+    }
   }
   if (__syncthreads_or(!arrived))
     return false;
   if (threadIdx.x == 0 && it + ZSTAGES < n_items)
     z_issue<D>(smem, spectra, C, row0, it + ZSTAGES);
-  // step B: D2-point DFTs along n2, real parts in natural order
-  for (int item = threadIdx.x; item < TZ * D1; item += FFT_THREADS) {
-    const int k1 = item % D1, t = item / D1;
-    float2 u[D2];
+  {
+    // step B: row t, k1, lane-part l of the P2-point DFT over n2
+    const int l = threadIdx.x % L2, k1 = (threadIdx.x / L2) % P1, t = threadIdx.x / (L2 * P1);
 #pragma unroll
-    for (int n2 = 0; n2 < D2; n2++)
-      u[n2] = buf[t * P::BT + k1 * (D2 + 1) + n2];
-    dft_bwd<D2, D>(u, tw);
-#pragma unroll
-    for (int k2 = 0; k2 < D2; k2++)
-      out[t * P::OS + k1 + D1 * k2] = u[k2].x;
+    for (int i = 0; i < 4; i++)
+      z[i] = buf[t * P::BROW + k1 * P::RS + l + L2 * i];
+    lane_dft<P2>(z, l, w.lb);
   }
-  __syncthreads();
   return true;
 }
 
-// Ring setup: barriers, twiddles, the first ZSTAGES copies.
+// Ring setup: barriers, the first ZSTAGES copies.
 template <int D>
 __device__ __forceinline__ void z_setup(char* smem, const float2* spectra, long long C, long long row0, int n_items)
 {
-  using P = ZPlan<D>;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   if (threadIdx.x == 0) {
     for (int s = 0; s < ZSTAGES; s++)
       mbar_init(&bars[s], 1);
     mbar_init_fence();
   }
-  fill_twiddles<D>(reinterpret_cast<float2*>(smem + P::OFF_TW));
   __syncthreads();
   if (threadIdx.x == 0)
     for (int it = 0; it < ZSTAGES && it < n_items; it++)
@@ -494,89 +627,106 @@ __device__ void z_abort(char* smem, int it, int n_items, unsigned* err)
   for (int j = it; j < n_items && j < it + ZSTAGES; j++)
     mbar_wait(&bars[j % ZSTAGES], (unsigned)(j / ZSTAGES) & 1u);
 }
+
+// cell state bits of the threshold z-pass
+constexpr unsigned ST_ION = 1u;      // ionised at some radius of this launch
+constexpr unsigned ST_XHIGH = 2u;    // xH at launch start > REL_TOL
+constexpr unsigned ST_XLOW = 4u;     // xH at launch start < REL_TOL
+constexpr unsigned ST_ZUNSET = 8u;   // z_at_ionization < 0
+constexpr int ST_RB_SHIFT = 8;       // radius index of the last ionising radius
 }  // namespace
 
 // z-pass fused with the per-cell test of find_HII_bubbles (clamps
 // :271-311, criterion and bookkeeping :342-443) for every radius of the batch.
-// Grid: one block per (x, y tile of TZ rows).  The cell state lives in
-// registers for all radii; the G fields of a radius are transformed into
-// shared memory, then every cell is tested.
+// Grid: one block per TZ rows.  A thread transforms, for each field of a
+// radius, the 8 cells it then tests, so the fields of a cell meet in
+// registers.  The cell state is a few bits per cell: whether it is ionised,
+// the xH and z_at_ionization tests at launch start, and the index of the last
+// ionising radius.  J_21, Gamma12, z_at_ionization and J_21_at_ionization
+// change at most once per cell per launch (at the first crossing) and are
+// stored when that happens; xH and r_bubble are stored at the end.
 template <int D>
 __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdArgs a)
 {
   using P = ZPlan<D>;
-  constexpr int CELLS = TZ * D;
-  constexpr int CPT = (CELLS + FFT_THREADS - 1) / FFT_THREADS;
   extern __shared__ __align__(128) unsigned char zsmem[];
   char* smem = reinterpret_cast<char*>(zsmem);
-  float* fldbase = reinterpret_cast<float*>(smem + P::OFF_FLD);
-  const int ny = D / TZ;
-  const int x = blockIdx.x / ny;
-  const int y0 = (blockIdx.x % ny) * TZ;
-  const long long row0 = (long long)x * D + y0;  // first row index
+  const long long row0 = (long long)blockIdx.x * P::TZ;
   const int n_items = a.n_f * a.G;
   z_setup<D>(smem, a.spectra, a.C, row0, n_items);
-  float xH[CPT], zion[CPT], rb[CPT], J21[CPT], J21i[CPT], G12[CPT];
+  ZTw<D> w;
+  w.init();
+  // this thread's cells: row t, z = 2 m_e + {0, 1}
+  const int l = threadIdx.x % P::L2, k1 = (threadIdx.x / P::L2) % P::P1, t = threadIdx.x / (P::L2 * P::P1);
+  const long long rowc = row0 + t;
+  int zc[4];
 #pragma unroll
-  for (int j = 0; j < CPT; j++) {
-    const int c = threadIdx.x + j * FFT_THREADS;
-    const long long ir = row0 * D + c;
-    if (c < CELLS) {
-      xH[j] = a.xH[ir];
-      zion[j] = a.z_at_ion[ir];
-      rb[j] = a.r_bubble[ir];
-      J21[j] = a.uvb ? a.J21[ir] : 0.0f;
-      J21i[j] = a.uvb ? a.J21_at_ion[ir] : 0.0f;
-      G12[j] = a.recomb ? a.Gamma12[ir] : 0.0f;
-    }
+  for (int e = 0; e < 4; e++)
+    zc[e] = 2 * (k1 + P::P1 * lane_out(P::L2, e, l));
+  unsigned st[8];
+#pragma unroll
+  for (int e = 0; e < 4; e++) {
+    const long long ir = rowc * D + zc[e];
+    const float2 x0 = *reinterpret_cast<const float2*>(a.xH + ir);
+    const float2 z0 = *reinterpret_cast<const float2*>(a.z_at_ion + ir);
+    st[2 * e] = (x0.x > REL_TOL_F ? ST_XHIGH : 0u) | (x0.x < REL_TOL_F ? ST_XLOW : 0u) | (z0.x < 0 ? ST_ZUNSET : 0u);
+    st[2 * e + 1] = (x0.y > REL_TOL_F ? ST_XHIGH : 0u) | (x0.y < REL_TOL_F ? ST_XLOW : 0u) | (z0.y < 0 ? ST_ZUNSET : 0u);
   }
   int it = 0;
   for (int r = 0; r < a.n_r; r++) {
     const RadiusParams rp = a.rp[r];
     const bool direct = rp.last != 0;
+    float2 f[MAX_FIELDS][4];
     if (!direct) {
-      for (int g = 0; g < a.G; g++, it++)
-        if (!z_c2r<D>(smem, it, n_items, a.spectra, a.C, row0, fldbase + g * TZ * P::OS)) {
-          z_abort<D>(smem, it, n_items, a.err);
-          return;
+#pragma unroll
+      for (int g = 0; g < MAX_FIELDS; g++) {
+        if (g < a.G) {
+          if (!z_c2r<D>(smem, it, n_items, a.spectra, a.C, row0, w, f[g])) {
+            z_abort<D>(smem, it, n_items, a.err);
+            return;
+          }
+          it++;
         }
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < MAX_FIELDS; g++)
+        if (g < a.G)
+#pragma unroll
+          for (int e = 0; e < 4; e++)
+            f[g][e] = *reinterpret_cast<const float2*>(a.direct[g] + rowc * 2LL * P::H + zc[e]);
     }
 #pragma unroll
-    for (int j = 0; j < CPT; j++) {
-      const int c = threadIdx.x + j * FFT_THREADS;
-      if (c >= CELLS)
-        continue;
-      const int t = c / D, zc = c % D;
-      float f[MAX_FIELDS];
-      if (direct) {
-        const long long ip = (row0 + t) * 2LL * P::H + zc;
-        for (int g = 0; g < a.G; g++)
-          f[g] = a.direct[g][ip];
-      } else {
-        for (int g = 0; g < a.G; g++)
-          f[g] = fldbase[g * TZ * P::OS + t * P::OS + zc];
-      }
-      const float dx = fmaxf(f[0], -1 + REL_TOL_F);
-      float st = fmaxf(f[1], 0.0f);
-      if (st < ABS_TOL_F)
-        st = 0;
-      float ws = fmaxf(f[2], 0.0f);
+    for (int c = 0; c < 8; c++) {
+      const int e = c >> 1;
+      const bool hi = c & 1;
+      float fv[MAX_FIELDS];
+#pragma unroll
+      for (int g = 0; g < MAX_FIELDS; g++)
+        fv[g] = g < a.G ? (hi ? f[g][e].y : f[g][e].x) : 0.0f;
+      const float dx = fmaxf(fv[0], -1 + REL_TOL_F);
+      float stv = fmaxf(fv[1], 0.0f);
+      if (stv < ABS_TOL_F)
+        stv = 0;
+      float ws = fmaxf(fv[2], 0.0f);
       if (ws < ABS_TOL_F)
         ws = 0;
       float nr = 0.0f, xe = 0.0f;
       if (a.recomb) {
-        nr = fmaxf(f[a.idx_nr], 0.0f);
+        nr = a.idx_nr == 3 ? fv[3] : fv[4];
+        nr = fmaxf(nr, 0.0f);
         if (nr < ABS_TOL_F)
           nr = 0;
       }
       if (a.spin) {
-        xe = fmaxf(f[a.idx_xe], 0.0f);
+        xe = a.idx_xe == 3 ? fv[3] : fv[4];
+        xe = fmaxf(xe, 0.0f);
         if (xe < ABS_TOL_F)
           xe = 0;
         xe = fminf(xe, 0.999f);
       }
       const float domf = 1.0f + dx;
-      const float lhs_f = st * rp.kfc / domf;
+      const float lhs_f = stv * rp.kfc / domf;
       const float nf_f = 1.0f - xe;
       const float rhs_f = nf_f * (1.0f + nr / domf);
       bool ionised;
@@ -588,45 +738,44 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
         const double dom = 1.0 + (double)dx;
         const double rec = a.recomb ? (double)nr / dom : 0.0;
         const double nf = a.spin ? 1.0 - (double)xe : 1.0;
-        const double f_coll = (double)st / (rp.M_mean * dom) * (4.0 / 3.0) * PI_D * rp.R_cubed / a.pixel_volume;
+        const double f_coll = (double)stv / (rp.M_mean * dom) * (4.0 / 3.0) * PI_D * rp.R_cubed / a.pixel_volume;
         ionised = f_coll * a.eff > nf * (1. + rec);
         xpart = (float)__dsub_rn(nf, __dmul_rn(f_coll, a.eff));
       }
+      const long long ir = rowc * D + zc[e] + (hi ? 1 : 0);
+      unsigned s = st[c];
+      const bool xr_high = !(s & ST_ION) && (s & ST_XHIGH);  // running xH > REL_TOL
+      bool xr_low = (s & ST_ION) || (s & ST_XLOW);            // running xH < REL_TOL
       const float J21_aux = a.uvb ? ws * rp.kj : 0.0f;
       if (ionised) {
-        if (xH[j] > REL_TOL_F) {
+        if (xr_high) {
           if (a.uvb)
-            J21[j] = J21_aux;
+            a.J21[ir] = J21_aux;
           if (a.recomb)
-            G12[j] = ws * rp.kg;
+            a.Gamma12[ir] = ws * rp.kg;
         }
-        xH[j] = 0.0f;
-        rb[j] = (float)rp.R;
-      } else if (rp.last && (xH[j] > REL_TOL_F)) {
-        xH[j] = fminf(fmaxf(xpart, 0.0f), 1.0f);
+        s = (s & ((1u << ST_RB_SHIFT) - 1)) | ST_ION | ((unsigned)r << ST_RB_SHIFT);
+        xr_low = true;
+      } else if (rp.last && xr_high) {
+        const float xn = fminf(fmaxf(xpart, 0.0f), 1.0f);
+        a.xH[ir] = xn;
+        xr_low = xn < REL_TOL_F;
       }
-      if ((xH[j] < REL_TOL_F) && (zion[j] < 0)) {
-        zion[j] = (float)a.redshift;
+      if (xr_low && (s & ST_ZUNSET)) {
+        a.z_at_ion[ir] = (float)a.redshift;
         if (a.uvb)
-          J21i[j] = J21_aux * a.gamma_halo_bias;
+          a.J21_at_ion[ir] = J21_aux * a.gamma_halo_bias;
+        s &= ~ST_ZUNSET;
       }
+      st[c] = s;
     }
-    __syncthreads();
   }
 #pragma unroll
-  for (int j = 0; j < CPT; j++) {
-    const int c = threadIdx.x + j * FFT_THREADS;
-    const long long ir = row0 * D + c;
-    if (c < CELLS) {
-      a.xH[ir] = xH[j];
-      a.z_at_ion[ir] = zion[j];
-      a.r_bubble[ir] = rb[j];
-      if (a.uvb) {
-        a.J21[ir] = J21[j];
-        a.J21_at_ion[ir] = J21i[j];
-      }
-      if (a.recomb)
-        a.Gamma12[ir] = G12[j];
+  for (int c = 0; c < 8; c++) {
+    if (st[c] & ST_ION) {
+      const long long ir = rowc * D + zc[c >> 1] + (c & 1);
+      a.xH[ir] = 0.0f;
+      a.r_bubble[ir] = (float)a.rp[st[c] >> ST_RB_SHIFT].R;
     }
   }
 }
@@ -638,24 +787,26 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_store(const float2* sp
                                                                    float* shells, long long N, unsigned* err)
 {
   using P = ZPlan<D>;
-  constexpr int CELLS = TZ * D;
   extern __shared__ __align__(128) unsigned char zsmem[];
   char* smem = reinterpret_cast<char*>(zsmem);
-  float* fld = reinterpret_cast<float*>(smem + P::OFF_FLD);
-  const int ny = D / TZ;
-  const int x = blockIdx.x / ny;
-  const int y0 = (blockIdx.x % ny) * TZ;
-  const long long row0 = (long long)x * D + y0;
+  const long long row0 = (long long)blockIdx.x * P::TZ;
   z_setup<D>(smem, spectra, C, row0, n);
+  ZTw<D> w;
+  w.init();
+  const int l = threadIdx.x % P::L2, k1 = (threadIdx.x / P::L2) % P::P1, t = threadIdx.x / (P::L2 * P::P1);
+  const long long base = (row0 + t) * D;
   for (int r = 0; r < n; r++) {
-    if (!z_c2r<D>(smem, r, n, spectra, C, row0, fld)) {
+    float2 z[4];
+    if (!z_c2r<D>(smem, r, n, spectra, C, row0, w, z)) {
       z_abort<D>(smem, r, n, err);
       return;
     }
-    float* dst = shells + (long long)(r0 + r) * N + row0 * D;
-    for (int c = threadIdx.x; c < CELLS; c += FFT_THREADS)
-      dst[c] = fmaxf(fld[(c / D) * P::OS + c % D], 0.0f);
-    __syncthreads();
+    float* dst = shells + (long long)(r0 + r) * N + base;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int zc = 2 * (k1 + P::P1 * lane_out(P::L2, e, l));
+      *reinterpret_cast<float2*>(dst + zc) = make_float2(fmaxf(z[e].x, 0.0f), fmaxf(z[e].y, 0.0f));
+    }
   }
 }
 
@@ -692,17 +843,17 @@ static void launch_y(float2* data, long long C, int n_spectra, cudaStream_t s)
 template <int D>
 static void launch_zt(const ZThresholdArgs& a, cudaStream_t s)
 {
-  const size_t bytes = ZPlan<D>::bytes(MAX_FIELDS);
+  const size_t bytes = ZPlan<D>::BYTES;
   cudaFuncSetAttribute(k_fft_z_threshold<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  k_fft_z_threshold<D><<<D * (D / TZ), FFT_THREADS, bytes, s>>>(a);
+  k_fft_z_threshold<D><<<D * D / ZPlan<D>::TZ, FFT_THREADS, bytes, s>>>(a);
 }
 template <int D>
 static void launch_zs(const float2* spectra, long long C, int n, int r0, float* shells, long long N, unsigned* err,
                       cudaStream_t s)
 {
-  const size_t bytes = ZPlan<D>::bytes(1);
+  const size_t bytes = ZPlan<D>::BYTES;
   cudaFuncSetAttribute(k_fft_z_store<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  k_fft_z_store<D><<<D * (D / TZ), FFT_THREADS, bytes, s>>>(spectra, C, n, r0, shells, N, err);
+  k_fft_z_store<D><<<D * D / ZPlan<D>::TZ, FFT_THREADS, bytes, s>>>(spectra, C, n, r0, shells, N, err);
 }
 
 // Largest float kR with (float)((double)kR * 0.413566994) <= 1, the last mode

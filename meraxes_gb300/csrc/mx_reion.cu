@@ -916,6 +916,22 @@ static int guarded(mx_ctx* c, F&& f)
   }
 }
 
+// Device grids must be 8-byte aligned: cuFFT reads its real inputs in pairs,
+// as do the fused transforms (any CUDA allocator gives 256-byte alignment; a
+// float pointer alone guarantees 4).
+static void check_device_grids(const mx_grids* dev)
+{
+  if (!dev)
+    throw CudaError{ MX_EINVAL, "NULL grids" };
+  const float* const ptrs[] = { dev->deltax,  dev->stars,  dev->weighted_sfr, dev->sfr,        dev->sfr_histories,
+                                dev->N_rec,   dev->x_e_box, dev->x_e_box_prev, dev->Tk_box,    dev->TS_box,
+                                dev->xH,      dev->z_at_ionization, dev->r_bubble, dev->J_21,  dev->J_21_at_ionization,
+                                dev->Gamma12, dev->delta_T, dev->vel };
+  for (const float* q : ptrs)
+    if ((uintptr_t)q % 8 != 0)
+      throw CudaError{ MX_EINVAL, "device grids must be 8-byte aligned" };
+}
+
 static void check_snapshot(mx_ctx* c, int snapshot)
 {
   if (c->zz.empty())
@@ -1090,8 +1106,7 @@ int mx_find_HII_bubbles_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* de
 {
   return guarded(ctx, [&]() {
     check_snapshot(ctx, snapshot);
-    if (!dev)
-      throw CudaError{ MX_EINVAL, "NULL grids" };
+    check_device_grids(dev);
     run_find_HII_bubbles(ctx, snapshot, dev, out, pick(ctx, stream));
   });
 }
@@ -1100,8 +1115,7 @@ int mx_ComputeTs_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_g
 {
   return guarded(ctx, [&]() {
     check_snapshot(ctx, snapshot);
-    if (!dev)
-      throw CudaError{ MX_EINVAL, "NULL grids" };
+    check_device_grids(dev);
     run_ComputeTs(ctx, snapshot, dev, out, pick(ctx, stream));
   });
 }
@@ -1114,8 +1128,7 @@ int mx_ComputeBrightnessTemperatureBox_device(mx_ctx* ctx,
 {
   return guarded(ctx, [&]() {
     check_snapshot(ctx, snapshot);
-    if (!dev)
-      throw CudaError{ MX_EINVAL, "NULL grids" };
+    check_device_grids(dev);
     run_delta_T(ctx, snapshot, dev, out, pick(ctx, stream));
   });
 }
@@ -1124,8 +1137,7 @@ int mx_step_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_global
 {
   return guarded(ctx, [&]() {
     check_snapshot(ctx, snapshot);
-    if (!dev)
-      throw CudaError{ MX_EINVAL, "NULL grids" };
+    check_device_grids(dev);
     cudaStream_t s = pick(ctx, stream);
     int launches = 0;
     if (ctx->p.flag_spin_temp) {

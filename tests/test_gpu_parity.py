@@ -136,3 +136,36 @@ def test_errors_are_reported_not_raised_on_device():
     g.update(gen.inputs(s, 0))
     out = st.step(s, g)
     assert 0.0 <= out["volume_weighted_global_xH"] <= 1.0
+
+
+def test_unaligned_device_grids_are_rejected():
+    """Device grids 4 bytes past an 8-byte boundary (legal for float*, not for
+    cuFFT's real inputs) are refused with MX_EINVAL; the context stays usable."""
+    import torch
+
+    from cases import initial
+    from meraxes_gb300 import _lib
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+
+    w = CASES["plain32_tophat"].workload()
+    step = ReionGridStep(w.params, w.redshifts)
+    gen = syn.FieldGenerator(w)
+    s = w.snapshots[0]
+    st = initial(w, 0)
+    st.update(gen.inputs(s, 0))
+
+    def unaligned(a):
+        flat = torch.empty(a.size + 1, dtype=torch.float32, device="cuda")
+        v = flat[1:].view(a.shape)
+        v.copy_(torch.from_numpy(a))
+        assert v.data_ptr() % 8 == 4
+        return v
+
+    bad = {k: (unaligned(v) if k == "deltax" else torch.from_numpy(v.copy()).cuda()) for k, v in st.items()}
+    with pytest.raises(_lib.MxError) as e:
+        step.step(s, bad)
+    assert e.value.code == -1 and "aligned" in str(e.value)
+    good = {k: torch.from_numpy(v.copy()).cuda() for k, v in st.items()}
+    out = step.step(s, good)
+    assert 0.0 <= out["volume_weighted_global_xH"] <= 1.0
