@@ -37,6 +37,20 @@ METRIC = "ms/snapshot at 512^3 (ComputeTs + find_HII_bubbles + 21cm box)"
 UNIT = "ms/snapshot"
 REION_EFF = 1.0 / 0.15714 * 4000.0 / (1.0 - 0.75 * 0.24)
 FESC = 0.01
+# DRAM bytes (read + write) per algorithmic byte of each kernel, from one ncu
+# capture per kernel of the same workload at 256^3 (10 spectra per batch):
+# `ncu --set full -k regex:<kernel> -s 1 -c 1` on
+# `python bench.py --grid 256 --steps 1 --warmup 1 --no-cpu --no-e2e` with
+# MX_MAX_BATCH_SPECTRA=10.  Each kernel's DRAM traffic grows in proportion to
+# the spectra (or cells) it processes, so traffic per launch at 512^3 is this
+# ratio times the launch's algorithmic bytes.
+DRAM_PER_ALGORITHMIC = {
+    "fft_x_filter": 690.67e6 / (8 * 256 * 256 * 129 * 10),   # TS launch, 1 field, 9 radii
+    "fft_y": 1296.72e6 / (16 * 256 * 256 * 129 * 10),        # 10 spectra
+    "fft_z_threshold": 813.95e6 / (8 * 256 * 256 * 129 * 10 + 2 * 4 * 256 ** 3),  # 10 spectra + xH, z_at_ion reads
+    "fft_z_store": 1301.92e6 / ((8 * 256 * 256 * 129 + 4 * 256 ** 3) * 10),
+    "k_evolve": 3084.37e6 / (46 * 4 * 256 ** 3),
+}
 
 
 def parse():
@@ -296,8 +310,10 @@ def run_gb300(args, rank, world, local):
     if dom:
         name, (n, kms, b) = dom
         achieved = (b / n / 1e9) / (kms / n / 1e3)
+        ratio = DRAM_PER_ALGORITHMIC.get(name)
         roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": hbm_peak,
-                    "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
+                    "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                    "traffic": round(ratio * b / n) if ratio else None,
                     "peak_source": peak_src, "algorithmic_bytes_per_launch": b / n}
     # whole-step algorithmic bandwidth
     total_bytes = sum(v[2] for v in kstats.values())

@@ -394,7 +394,11 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
       za.recomb = recomb;
       za.spin = spin;
       za.err = c->d_err;
-      Prof pr(c, "fft_z_threshold", (double)G * nf * B8C + ((double)(nb - nf) * G + 2.0 * nstate) * B4N, s);
+      // spectra read once, unfiltered last step read once, and the per-call
+      // state (xH, z_at_ionization read and written; r_bubble, J_21,
+      // J_21_at_ionization, Gamma12 written) counted with the first batch
+      Prof pr(c, "fft_z_threshold",
+              (double)G * nf * B8C + (double)(nb - nf) * G * B4N + (r0 == 0 ? 8.0 * B4N : 0.0), s);
       launch_fft_z_threshold(gd.D, za, s);
       continue;
     }
