@@ -89,10 +89,79 @@ __device__ void fill_twiddles(float2* tw)
   }
 }
 
-// In-register backward DFT of M points (radix-2, decimation in time);
-// tw is the D-point table, so exp(+2 pi i a / M) = tw[a * D / M].
-template <int M, int D>
-__device__ __forceinline__ void dft_bwd(float2 (&v)[M], const float2* __restrict__ tw)
+// Compile-time cos and sin of 2 pi j / n, by Taylor series on [-pi, pi] (30
+// terms; the truncation error is far below double rounding).  Used only to
+// initialise constexpr twiddle factors.
+__host__ __device__ constexpr double cx_cos_sin(int j, int n, bool want_sin)
+{
+  j = ((j % n) + n) % n;
+  if (2 * j > n)
+    j -= n;  // angle in [-pi, pi]
+  const double x = 2.0 * 3.14159265358979323846 * (double)j / (double)n;
+  double term = want_sin ? x : 1.0, sum = term;
+  for (int k = 1; k < 30; k++) {
+    const double a = want_sin ? (2.0 * k) * (2.0 * k + 1.0) : (2.0 * k - 1.0) * (2.0 * k);
+    term *= -x * x / a;
+    sum += term;
+  }
+  return sum;
+}
+
+// b * exp(+2 pi i J / N) with the factor known at compile time; the eighth
+// roots of unity take their exact forms.
+template <int J, int N>
+__device__ __forceinline__ float2 mul_tw(float2 b)
+{
+  constexpr int j = ((J % N) + N) % N;
+  constexpr float h = 0.70710678118654752440f;  // 1/sqrt(2)
+  if constexpr (j == 0) {
+    return b;
+  } else if constexpr (4 * j == N) {
+    return make_float2(-b.y, b.x);
+  } else if constexpr (2 * j == N) {
+    return make_float2(-b.x, -b.y);
+  } else if constexpr (4 * j == 3 * N) {
+    return make_float2(b.y, -b.x);
+  } else if constexpr (8 * j == N) {
+    return make_float2(h * (b.x - b.y), h * (b.x + b.y));
+  } else if constexpr (8 * j == 3 * N) {
+    return make_float2(-h * (b.x + b.y), h * (b.x - b.y));
+  } else if constexpr (8 * j == 5 * N) {
+    return make_float2(h * (b.y - b.x), -h * (b.x + b.y));
+  } else if constexpr (8 * j == 7 * N) {
+    return make_float2(h * (b.x + b.y), h * (b.y - b.x));
+  } else {
+    constexpr float c = (float)cx_cos_sin(J, N, false);
+    constexpr float s = (float)cx_cos_sin(J, N, true);
+    return make_float2(c * b.x - s * b.y, c * b.y + s * b.x);
+  }
+}
+
+// Butterflies of a radix-2 decimation-in-time DFT, stage HALF, group I,
+// butterfly J, unrolled by template recursion so every twiddle is a constant.
+template <int M, int HALF, int I, int J>
+__device__ __forceinline__ void dft_stage(float2 (&v)[M])
+{
+  if constexpr (HALF < M) {
+    if constexpr (I < M) {
+      if constexpr (J < HALF) {
+        const float2 b = mul_tw<J, 2 * HALF>(v[I + J + HALF]);
+        const float2 a = v[I + J];
+        v[I + J] = cadd(a, b);
+        v[I + J + HALF] = csub(a, b);
+        dft_stage<M, HALF, I, J + 1>(v);
+      } else {
+        dft_stage<M, HALF, I + 2 * HALF, 0>(v);
+      }
+    } else {
+      dft_stage<M, 2 * HALF, 0, 0>(v);
+    }
+  }
+}
+
+// In-register backward DFT of M points: v[k] <- sum_n v[n] exp(+2 pi i nk/M).
+template <int M>
+__device__ __forceinline__ void dft_bwd(float2 (&v)[M])
 {
   constexpr int LOG = ilog2(M);
 #pragma unroll
@@ -104,20 +173,7 @@ __device__ __forceinline__ void dft_bwd(float2 (&v)[M], const float2* __restrict
       v[j] = t;
     }
   }
-#pragma unroll
-  for (int half = 1; half < M; half <<= 1) {
-#pragma unroll
-    for (int i = 0; i < M; i += 2 * half) {
-#pragma unroll
-      for (int j = 0; j < half; j++) {
-        float2 b = v[i + j + half];
-        if (j != 0)
-          b = cmul(b, tw[j * (D / (2 * half))]);
-        v[i + j + half] = csub(v[i + j], b);
-        v[i + j] = cadd(v[i + j], b);
-      }
-    }
-  }
+  dft_stage<M, 1, 0, 0>(v);
 }
 
 // k-space filter of reionization.c:2110-2170 in single precision only:
@@ -222,7 +278,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_x_filter(XPassArgs a)
             }
             v[n1] = x;
           }
-          dft_bwd<D1, D>(v, tw);
+          dft_bwd<D1>(v);
 #pragma unroll
           for (int k1 = 0; k1 < D1; k1++) {
             const float2 t2 = k1 == 0 || n2 == 0 ? v[k1] : cmul(v[k1], tw[(n2 * k1) % D]);
@@ -240,7 +296,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_x_filter(XPassArgs a)
 #pragma unroll
         for (int n2 = 0; n2 < D2; n2++)
           u[n2] = buf[(k1 * D2 + n2) * TX + t];
-        dft_bwd<D2, D>(u, tw);
+        dft_bwd<D2>(u);
         if (kz < H) {
 #pragma unroll
           for (int k2 = 0; k2 < D2; k2++) {
@@ -280,7 +336,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_y(float2* data, long long C
 #pragma unroll
     for (int n1 = 0; n1 < D1; n1++)
       v[n1] = kz < H ? plane[(long long)(n2 + D2 * n1) * H + kz] : make_float2(0.f, 0.f);
-    dft_bwd<D1, D>(v, tw);
+    dft_bwd<D1>(v);
 #pragma unroll
     for (int k1 = 0; k1 < D1; k1++)
       buf[(k1 * D2 + n2) * TX + t] = k1 == 0 || n2 == 0 ? v[k1] : cmul(v[k1], tw[(n2 * k1) % D]);
@@ -293,7 +349,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_y(float2* data, long long C
 #pragma unroll
     for (int n2 = 0; n2 < D2; n2++)
       u[n2] = buf[(k1 * D2 + n2) * TX + t];
-    dft_bwd<D2, D>(u, tw);
+    dft_bwd<D2>(u);
     if (kz < H) {
 #pragma unroll
       for (int k2 = 0; k2 < D2; k2++)
@@ -725,10 +781,12 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
           xe = 0;
         xe = fminf(xe, 0.999f);
       }
-      const float domf = 1.0f + dx;
-      const float lhs_f = stv * rp.kfc / domf;
+      // FP32 estimate of the test (a 2-ulp reciprocal is well inside the
+      // 4e-6 margin below which the FP64 comparison decides)
+      const float inv_dom = __fdividef(1.0f, 1.0f + dx);
+      const float lhs_f = stv * rp.kfc * inv_dom;
       const float nf_f = 1.0f - xe;
-      const float rhs_f = nf_f * (1.0f + nr / domf);
+      const float rhs_f = nf_f * (1.0f + nr * inv_dom);
       bool ionised;
       float xpart;
       if (fabsf(lhs_f - rhs_f) > 4e-6f * fmaxf(lhs_f, rhs_f)) {
