@@ -15,10 +15,11 @@
 //            of find_HII_bubbles for every radius with the cell state kept on
 //            chip, or the clamped store of ComputeTs shells.
 //
-// Each 1-D transform of length D = D1 * D2 is a two-step (Cooley-Tukey
-// "four-step") transform over a tile of T columns: D1-point DFTs in
-// registers, twiddles, a transpose through shared memory, D2-point DFTs in
-// registers.  Twiddles come from a shared-memory table filled with sincospi.
+// The x- and y-passes run a three-step Cooley-Tukey transform over a tile of
+// 8 columns (radix-8 or radix-4 DFTs in registers with compile-time twiddles,
+// inter-step twiddles from a shared table filled with sincospi, transposes
+// through a padded shared tile).  The z-pass computes each row's C2R as a
+// half-length complex transform split over 4-lane groups (see below).
 #include <cmath>
 #include <cstdint>
 
@@ -26,41 +27,31 @@
 
 namespace mx {
 
+// Compile-time cos and sin of 2 pi j / n, by Taylor series on [-pi, pi] (30
+// terms; the truncation error is far below double rounding).  Used only to
+// initialise constexpr twiddle factors.
+__host__ __device__ constexpr double cx_cos_sin(int j, int n, bool want_sin)
+{
+  j = ((j % n) + n) % n;
+  if (2 * j > n)
+    j -= n;  // angle in [-pi, pi]
+  const double x = 2.0 * 3.14159265358979323846 * (double)j / (double)n;
+  double term = want_sin ? x : 1.0, sum = term;
+  for (int k = 1; k < 30; k++) {
+    const double a = want_sin ? (2.0 * k) * (2.0 * k + 1.0) : (2.0 * k - 1.0) * (2.0 * k);
+    term *= -x * x / a;
+    sum += term;
+  }
+  return sum;
+}
+
+
 namespace {
 constexpr int FFT_THREADS = 256;
-constexpr int TX = 16;  // columns (kz) per x/y tile
 constexpr float REL_TOL_F = 1e-5f;
 constexpr float ABS_TOL_F = 1e-8f;
 constexpr double PI_D = 3.14159265358979323846;
 int fft_launches = 0;
-
-template <int D>
-struct Split;
-template <>
-struct Split<32>
-{
-  static constexpr int D1 = 4, D2 = 8;
-};
-template <>
-struct Split<64>
-{
-  static constexpr int D1 = 8, D2 = 8;
-};
-template <>
-struct Split<128>
-{
-  static constexpr int D1 = 8, D2 = 16;
-};
-template <>
-struct Split<256>
-{
-  static constexpr int D1 = 16, D2 = 16;
-};
-template <>
-struct Split<512>
-{
-  static constexpr int D1 = 16, D2 = 32;
-};
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -87,24 +78,6 @@ __device__ void fill_twiddles(float2* tw)
     sincospif(2.0f * (float)j / (float)D, &s, &c);
     tw[j] = make_float2(c, s);
   }
-}
-
-// Compile-time cos and sin of 2 pi j / n, by Taylor series on [-pi, pi] (30
-// terms; the truncation error is far below double rounding).  Used only to
-// initialise constexpr twiddle factors.
-__host__ __device__ constexpr double cx_cos_sin(int j, int n, bool want_sin)
-{
-  j = ((j % n) + n) % n;
-  if (2 * j > n)
-    j -= n;  // angle in [-pi, pi]
-  const double x = 2.0 * 3.14159265358979323846 * (double)j / (double)n;
-  double term = want_sin ? x : 1.0, sum = term;
-  for (int k = 1; k < 30; k++) {
-    const double a = want_sin ? (2.0 * k) * (2.0 * k + 1.0) : (2.0 * k - 1.0) * (2.0 * k);
-    term *= -x * x / a;
-    sum += term;
-  }
-  return sum;
 }
 
 // b * exp(+2 pi i J / N) with the factor known at compile time; the eighth
@@ -216,146 +189,199 @@ __device__ __forceinline__ float kcomp(int n, int D, float delta_k)
 
 int fft_kernel_launches() { return fft_launches; }
 
+// ---------------------------------------------------- column-tile engine
+// The x- and y-passes transform TXC adjacent columns (kz) of D points along
+// a slow axis.  D = R1 * R2 * R3; with n = n' + M n1 (M = R2 R3) and
+// n' = n3 + R3 n2, the three steps are
+//   A: per (column, n'): DFT_R1 over n1 from global memory, twiddle
+//      w_D^{n' k1}, into the shared tile at line k1 M + n';
+//   B: per (column, k1, n3): DFT_R2 over n2 in place (lines n3 + R3 n2),
+//      twiddle w_M^{n3 k2};
+//   C: per (column, k1, k2): DFT_R3 over n3, output k = k1 + R1 (k2 + R2 k3).
+// Every work item holds R points (R <= 8), so a block of 256 threads keeps
+// few registers and a 52 KB tile at D = 512, and four blocks fit an SM.
+constexpr int TXC = 8;  // columns per tile
+
+template <int D>
+struct Split3;
+template <>
+struct Split3<32>
+{
+  static constexpr int R1 = 4, R2 = 4, R3 = 2, PAD = 4;
+};
+template <>
+struct Split3<64>
+{
+  static constexpr int R1 = 4, R2 = 4, R3 = 4, PAD = 2;
+};
+template <>
+struct Split3<128>
+{
+  static constexpr int R1 = 8, R2 = 4, R3 = 4, PAD = 2;
+};
+template <>
+struct Split3<256>
+{
+  static constexpr int R1 = 8, R2 = 8, R3 = 4, PAD = 2;
+};
+template <>
+struct Split3<512>
+{
+  static constexpr int R1 = 8, R2 = 8, R3 = 8, PAD = 1;
+};
+
+template <int D>
+struct TilePlan
+{
+  static constexpr int R1 = Split3<D>::R1, R2 = Split3<D>::R2, R3 = Split3<D>::R3, M = R2 * R3;
+  static constexpr int BUF = D * TXC + (D / 2) * Split3<D>::PAD;  // float2, padded
+  static constexpr int NT = (D / 2 + 1 + TXC - 1) / TXC;          // tiles over kz
+  static_assert(R1 * R2 * R3 == D, "split");
+  // position of (line, column) in the padded tile: one pad slot per two lines
+  // keeps all three steps free of bank conflicts
+  static __device__ __forceinline__ int at(int line, int t) { return line * TXC + t + (line >> 1) * Split3<D>::PAD; }
+};
+
+// Inverse DFT of the tile's columns.  load(n, t) returns input point n of
+// column t; store(k, t, v) takes output point k.  Ends without a barrier:
+// the caller synchronises before reusing buf.
+template <int D, class Load, class Store>
+__device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load load, Store store)
+{
+  using P = TilePlan<D>;
+  constexpr int R1 = P::R1, R2 = P::R2, R3 = P::R3, M = P::M;
+  for (int item = threadIdx.x; item < TXC * M; item += FFT_THREADS) {
+    const int t = item % TXC, np = item / TXC;
+    float2 v[R1];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; n1++)
+      v[n1] = load(np + M * n1, t);
+    dft_bwd<R1>(v);
+#pragma unroll
+    for (int k1 = 0; k1 < R1; k1++)
+      buf[P::at(k1 * M + np, t)] = (k1 == 0 || np == 0) ? v[k1] : cmul(v[k1], tw[(np * k1) % D]);
+  }
+  __syncthreads();
+  for (int item = threadIdx.x; item < TXC * R1 * R3; item += FFT_THREADS) {
+    const int t = item % TXC, n3 = (item / TXC) % R3, k1 = item / (TXC * R3);
+    float2 v[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; n2++)
+      v[n2] = buf[P::at(k1 * M + n3 + R3 * n2, t)];
+    dft_bwd<R2>(v);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; k2++)
+      buf[P::at(k1 * M + n3 + R3 * k2, t)] = (k2 == 0 || n3 == 0) ? v[k2] : cmul(v[k2], tw[(R1 * n3 * k2) % D]);
+  }
+  __syncthreads();
+  for (int item = threadIdx.x; item < TXC * R1 * R2; item += FFT_THREADS) {
+    const int t = item % TXC, k2 = (item / TXC) % R2, k1 = item / (TXC * R2);
+    float2 v[R3];
+#pragma unroll
+    for (int n3 = 0; n3 < R3; n3++)
+      v[n3] = buf[P::at(k1 * M + n3 + R3 * k2, t)];
+    dft_bwd<R3>(v);
+#pragma unroll
+    for (int k3 = 0; k3 < R3; k3++)
+      store(k1 + R1 * (k2 + R2 * k3), t, v[k3]);
+  }
+}
+
 // ------------------------------------------------------------------ x-pass
-// Grid: one block per (ky, kz tile).  For every radius of the batch and every
-// field: load the unfiltered column tile (HBM on the first radius, L2 after),
-// scale by 1/N, multiply by W(|k| R), inverse FFT along x, store to
+// Grid: one block per (ky, tile of TXC kz columns, radius), the radius
+// fastest, so that the blocks of all radii of a tile run together and its
+// unfiltered columns are read from HBM once and from L2 by the others.  A
+// block computes the filter weights of its tile for its radius (shared by all
+// fields), then for every field loads the unfiltered columns, scales by 1/N,
+// multiplies by W(|k| R), inverse-DFTs along x and stores to
 // out[(r*G + g) * C + (x*D + ky)*H + kz].
 template <int D>
-__global__ void __launch_bounds__(FFT_THREADS) k_fft_x_filter(XPassArgs a)
+__global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_x_filter(XPassArgs a)
 {
-  constexpr int D1 = Split<D>::D1, D2 = Split<D>::D2, H = D / 2 + 1;
-  constexpr int NT = (H + TX - 1) / TX;
-  constexpr int ITEMS_A = TX * D2, ITEMS_B = TX * D1;
-  constexpr int PER_A = (ITEMS_A + FFT_THREADS - 1) / FFT_THREADS;
+  using P = TilePlan<D>;
+  constexpr int H = D / 2 + 1;
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* buf = smem + D;
-  float* wsm = reinterpret_cast<float*>(buf + D * TX);
+  float* wsm = reinterpret_cast<float*>(buf + P::BUF);
   fill_twiddles<D>(tw);
-  const int ky = blockIdx.x / NT;
-  const int kz0 = (blockIdx.x % NT) * TX;
+  const int r = blockIdx.x % a.n;
+  const int tile = blockIdx.x / a.n;
+  const int ky = tile / P::NT;
+  const int kz0 = (tile % P::NT) * TXC;
   const float kyv = kcomp(ky, D, a.delta_k);
+  // filter weights of the tile, wsm[kx * TXC + t]; a zeroed sharp-k mode is a
+  // weight of 0
+  for (int i = threadIdx.x; i < D * TXC; i += FFT_THREADS) {
+    const int kx = i / TXC, kz = kz0 + i % TXC;
+    float wv = 1.0f;
+    if (a.apply[r]) {
+      const float kxv = kcomp(kx, D, a.delta_k);
+      const float kzv = __fmul_rn((float)kz, a.delta_k);
+      const float kmag = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(kyv, kyv)), __fmul_rn(kzv, kzv)));
+      bool zero = false;
+      wv = filter_weight(a.filter_type, kmag, a.R[r], a.sharpk_max, &zero);
+      if (zero)
+        wv = 0.0f;
+    }
+    wsm[i] = wv;
+  }
   __syncthreads();
-  for (int r = 0; r < a.n; r++) {
-    // filter weights of the tile for radius r, wsm[kx * TX + t]; a zeroed
-    // sharp-k mode is a weight of 0
-    for (int i = threadIdx.x; i < D * TX; i += FFT_THREADS) {
-      const int kx = i / TX, kz = kz0 + i % TX;
-      float wv = 1.0f;
-      if (a.apply[r]) {
-        const float kxv = kcomp(kx, D, a.delta_k);
-        const float kzv = __fmul_rn((float)kz, a.delta_k);
-        const float kmag =
-          sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(kyv, kyv)), __fmul_rn(kzv, kzv)));
-        bool zero = false;
-        wv = filter_weight(a.filter_type, kmag, a.R[r], a.sharpk_max, &zero);
-        if (zero)
-          wv = 0.0f;
-      }
-      wsm[i] = wv;
-    }
-    __syncthreads();
-    for (int g = 0; g < a.G; g++) {
-      const float2* __restrict__ src = a.in[g];
-      // step A: D1-point DFTs along n1, twiddle, to shared memory
-#pragma unroll
-      for (int q = 0; q < PER_A; q++) {
-        const int item = threadIdx.x + q * FFT_THREADS;
-        if (item < ITEMS_A) {
-          const int t = item % TX, n2 = item / TX;
-          const int kz = kz0 + t;
-          float2 v[D1];
-#pragma unroll
-          for (int n1 = 0; n1 < D1; n1++) {
-            const int kx = n2 + D2 * n1;
-            float2 x = make_float2(0.f, 0.f);
-            if (kz < H) {
-              x = src[((long long)kx * D + ky) * H + kz];
-              const float wv = wsm[kx * TX + t];
-              x.x = __fmul_rn(__fmul_rn(x.x, a.scale), wv);
-              x.y = __fmul_rn(__fmul_rn(x.y, a.scale), wv);
-            }
-            v[n1] = x;
-          }
-          dft_bwd<D1>(v);
-#pragma unroll
-          for (int k1 = 0; k1 < D1; k1++) {
-            const float2 t2 = k1 == 0 || n2 == 0 ? v[k1] : cmul(v[k1], tw[(n2 * k1) % D]);
-            buf[(k1 * D2 + n2) * TX + t] = t2;
-          }
-        }
-      }
-      __syncthreads();
-      // step B: D2-point DFTs along n2, natural-order store
-      float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C;
-      for (int item = threadIdx.x; item < ITEMS_B; item += FFT_THREADS) {
-        const int t = item % TX, k1 = item / TX;
+  for (int g = 0; g < a.G; g++) {
+    const float2* __restrict__ src = a.in[g];
+    float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C;
+    const float scale = a.scale;
+    tile_dft<D>(
+      buf, tw,
+      [&](int kx, int t) {
         const int kz = kz0 + t;
-        float2 u[D2];
-#pragma unroll
-        for (int n2 = 0; n2 < D2; n2++)
-          u[n2] = buf[(k1 * D2 + n2) * TX + t];
-        dft_bwd<D2>(u);
+        float2 x = make_float2(0.f, 0.f);
         if (kz < H) {
-#pragma unroll
-          for (int k2 = 0; k2 < D2; k2++) {
-            const int x = k1 + D1 * k2;
-            dst[((long long)x * D + ky) * H + kz] = u[k2];
-          }
+          x = src[((long long)kx * D + ky) * H + kz];
+          const float wv = wsm[kx * TXC + t];
+          x.x = __fmul_rn(__fmul_rn(x.x, scale), wv);
+          x.y = __fmul_rn(__fmul_rn(x.y, scale), wv);
         }
-      }
-      __syncthreads();
-    }
+        return x;
+      },
+      [&](int x, int t, float2 v) {
+        const int kz = kz0 + t;
+        if (kz < H)
+          dst[((long long)x * D + ky) * H + kz] = v;
+      });
+    __syncthreads();
   }
 }
 
 // ------------------------------------------------------------------ y-pass
-// Grid: (spectrum, x, kz tile).  In-place inverse FFT along y.
+// Grid: (spectrum, x, tile of TXC kz columns).  In-place inverse DFT along y.
 template <int D>
-__global__ void __launch_bounds__(FFT_THREADS) k_fft_y(float2* data, long long C, int n_spectra)
+__global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_y(float2* data, long long C, int n_spectra)
 {
-  constexpr int D1 = Split<D>::D1, D2 = Split<D>::D2, H = D / 2 + 1;
-  constexpr int NT = (H + TX - 1) / TX;
-  constexpr int ITEMS_A = TX * D2, ITEMS_B = TX * D1;
+  using P = TilePlan<D>;
+  constexpr int H = D / 2 + 1;
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* buf = smem + D;
   fill_twiddles<D>(tw);
   const long long blk = blockIdx.x;
-  const int tile = (int)(blk % NT);
-  const int x = (int)((blk / NT) % D);
-  const long long s = blk / ((long long)NT * D);
-  const int kz0 = tile * TX;
+  const int tile = (int)(blk % P::NT);
+  const int x = (int)((blk / P::NT) % D);
+  const long long s = blk / ((long long)P::NT * D);
+  const int kz0 = tile * TXC;
   float2* plane = data + s * C + (long long)x * D * H;
   __syncthreads();
-  for (int item = threadIdx.x; item < ITEMS_A; item += FFT_THREADS) {
-    const int t = item % TX, n2 = item / TX;
-    const int kz = kz0 + t;
-    float2 v[D1];
-#pragma unroll
-    for (int n1 = 0; n1 < D1; n1++)
-      v[n1] = kz < H ? plane[(long long)(n2 + D2 * n1) * H + kz] : make_float2(0.f, 0.f);
-    dft_bwd<D1>(v);
-#pragma unroll
-    for (int k1 = 0; k1 < D1; k1++)
-      buf[(k1 * D2 + n2) * TX + t] = k1 == 0 || n2 == 0 ? v[k1] : cmul(v[k1], tw[(n2 * k1) % D]);
-  }
-  __syncthreads();
-  for (int item = threadIdx.x; item < ITEMS_B; item += FFT_THREADS) {
-    const int t = item % TX, k1 = item / TX;
-    const int kz = kz0 + t;
-    float2 u[D2];
-#pragma unroll
-    for (int n2 = 0; n2 < D2; n2++)
-      u[n2] = buf[(k1 * D2 + n2) * TX + t];
-    dft_bwd<D2>(u);
-    if (kz < H) {
-#pragma unroll
-      for (int k2 = 0; k2 < D2; k2++)
-        plane[(long long)(k1 + D1 * k2) * H + kz] = u[k2];
-    }
-  }
+  tile_dft<D>(
+    buf, tw,
+    [&](int ky, int t) {
+      const int kz = kz0 + t;
+      return kz < H ? plane[(long long)ky * H + kz] : make_float2(0.f, 0.f);
+    },
+    [&](int y, int t, float2 v) {
+      const int kz = kz0 + t;
+      if (kz < H)
+        plane[(long long)y * H + kz] = v;
+    });
 }
 
 // ------------------------------------------------------------------ z-pass
@@ -872,31 +898,29 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_store(const float2* sp
 bool fft3d_supported(int D) { return D == 32 || D == 64 || D == 128 || D == 256 || D == 512; }
 
 template <int D>
-constexpr size_t smem_xy()
+constexpr size_t smem_y()
 {
-  return sizeof(float2) * (D + (size_t)D * TX);
+  return sizeof(float2) * (D + (size_t)TilePlan<D>::BUF);
 }
 template <int D>
 constexpr size_t smem_x()
 {
-  return smem_xy<D>() + sizeof(float) * (size_t)D * TX;
+  return smem_y<D>() + sizeof(float) * (size_t)D * TXC;
 }
+
 template <int D>
 static void launch_x(const XPassArgs& a, cudaStream_t s)
 {
-  constexpr int H = D / 2 + 1;
-  constexpr int NT = (H + TX - 1) / TX;
   cudaFuncSetAttribute(k_fft_x_filter<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x<D>());
-  k_fft_x_filter<D><<<D * NT, FFT_THREADS, smem_x<D>(), s>>>(a);
+  const long long blocks = (long long)D * TilePlan<D>::NT * a.n;
+  k_fft_x_filter<D><<<(unsigned)blocks, FFT_THREADS, smem_x<D>(), s>>>(a);
 }
 template <int D>
 static void launch_y(float2* data, long long C, int n_spectra, cudaStream_t s)
 {
-  constexpr int H = D / 2 + 1;
-  constexpr int NT = (H + TX - 1) / TX;
-  const long long blocks = (long long)n_spectra * D * NT;
-  cudaFuncSetAttribute(k_fft_y<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_xy<D>());
-  k_fft_y<D><<<(unsigned)blocks, FFT_THREADS, smem_xy<D>(), s>>>(data, C, n_spectra);
+  const long long blocks = (long long)n_spectra * D * TilePlan<D>::NT;
+  cudaFuncSetAttribute(k_fft_y<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y<D>());
+  k_fft_y<D><<<(unsigned)blocks, FFT_THREADS, smem_y<D>(), s>>>(data, C, n_spectra);
 }
 template <int D>
 static void launch_zt(const ZThresholdArgs& a, cudaStream_t s)
