@@ -150,11 +150,12 @@ __device__ __forceinline__ void dft_bwd(float2 (&v)[M])
 }
 
 // k-space filter of reionization.c:2110-2170 in single precision only:
-//  * real-space top-hat 3 (sin kR / kR^3 - cos kR / kR^2): sin and cos from one
-//    sincosf, the powers from products (within an ulp of powf).  The
-//    reference's test (double)kR > 1e-4 is the same predicate as kR > 1e-4f
-//    (1e-4f is the largest float below 1e-4), and (float)(3.0 * (double)w) is
-//    3.0f * w rounded once, as the double product of a float and 3 is exact;
+//  * real-space top-hat 3 (sin kR / kR^3 - cos kR / kR^2) as
+//    3 (sin kR / kR - cos kR) / kR^2 from one sincosf and one fast reciprocal
+//    (a few ulp from the reference's float expression, far inside the
+//    tolerance of an FP32 transform).  The reference's test (double)kR > 1e-4
+//    is the same predicate as kR > 1e-4f (1e-4f is the largest float below
+//    1e-4);
 //  * k-space top-hat: a mode is zeroed when (float)((double)kR * 0.413566994)
 //    > 1, i.e. when kR exceeds the float threshold sharpk_max computed on the
 //    host from that expression;
@@ -167,9 +168,8 @@ __device__ __forceinline__ float filter_weight(int filter_type, float kmag, floa
     if (kR > 1e-4f) {
       float s, c;
       sincosf(kR, &s, &c);
-      const float kR2 = __fmul_rn(kR, kR);
-      const float kR3 = __fmul_rn(kR2, kR);
-      return __fmul_rn(3.0f, __fsub_rn(__fdiv_rn(s, kR3), __fdiv_rn(c, kR2)));
+      const float inv = __fdividef(1.0f, kR);
+      return 3.0f * (s * inv - c) * inv * inv;
     }
     return 1.0f;
   }
@@ -310,10 +310,11 @@ __global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_x_filter(XPassArgs a)
   const int ky = tile / P::NT;
   const int kz0 = (tile % P::NT) * TXC;
   const float kyv = kcomp(ky, D, a.delta_k);
-  // filter weights of the tile, wsm[kx * TXC + t]; a zeroed sharp-k mode is a
-  // weight of 0
-  for (int i = threadIdx.x; i < D * TXC; i += FFT_THREADS) {
-    const int kx = i / TXC, kz = kz0 + i % TXC;
+  // filter weights of the tile times the 1/N scale (a power of two, so
+  // x * (scale * W) == (x * scale) * W exactly), wsm[kx * TXC + t]; a zeroed
+  // sharp-k mode is a weight of 0.  |kx| and |D - kx| share a weight.
+  for (int i = threadIdx.x; i < (D / 2 + 1) * TXC; i += FFT_THREADS) {
+    const int kx = i / TXC, t = i % TXC, kz = kz0 + t;
     float wv = 1.0f;
     if (a.apply[r]) {
       const float kxv = kcomp(kx, D, a.delta_k);
@@ -324,13 +325,15 @@ __global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_x_filter(XPassArgs a)
       if (zero)
         wv = 0.0f;
     }
+    wv *= a.scale;
     wsm[i] = wv;
+    if (kx > 0 && kx < D / 2)
+      wsm[(D - kx) * TXC + t] = wv;
   }
   __syncthreads();
   for (int g = 0; g < a.G; g++) {
     const float2* __restrict__ src = a.in[g];
     float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C;
-    const float scale = a.scale;
     tile_dft<D>(
       buf, tw,
       [&](int kx, int t) {
@@ -339,8 +342,8 @@ __global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_x_filter(XPassArgs a)
         if (kz < H) {
           x = src[((long long)kx * D + ky) * H + kz];
           const float wv = wsm[kx * TXC + t];
-          x.x = __fmul_rn(__fmul_rn(x.x, scale), wv);
-          x.y = __fmul_rn(__fmul_rn(x.y, scale), wv);
+          x.x *= wv;
+          x.y *= wv;
         }
         return x;
       },
