@@ -209,6 +209,24 @@ typedef struct mx_kernel_stat
 int mx_profile_enable(mx_ctx* ctx, int32_t on);
 int32_t mx_profile_read(mx_ctx* ctx, mx_kernel_stat* out, int32_t cap);
 
+/* 21 cm power spectrum of a delta_T grid (REAL layout): Initialise_PowerSpectrum
+ * and Compute_PS (src/core/ComputePowerSpectrum.c:18-255, header
+ * ComputePowerSpectrum.h:9-10).  The reference writes
+ * run_globals.reion_grids.PS_k / PS_data / PS_error; here the caller passes
+ * three host arrays of at least mx_ps_length(ctx) floats.  Bins: ratio 1.35
+ * from 2 pi / (BoxSize / h) up to D times that; every half-spectrum mode is
+ * counted once.  Returns the number of bins, or a negative MX_E* code.
+ * mx_Compute_PS takes a host grid; _device a device grid on `stream`. */
+int32_t mx_ps_length(const mx_ctx* ctx);
+int mx_Compute_PS(mx_ctx* ctx, const float* delta_T, float* ps_k, float* ps_data, float* ps_error, int32_t cap);
+int mx_Compute_PS_device(mx_ctx* ctx,
+                         const float* delta_T,
+                         float* ps_k,
+                         float* ps_data,
+                         float* ps_error,
+                         int32_t cap,
+                         void* stream);
+
 /* Build information: returns a static string. */
 const char* mx_build_info(void);
 

@@ -23,7 +23,7 @@ EXPORTS = [
     "mx_find_HII_bubbles", "mx_ComputeTs", "mx_ComputeBrightnessTemperatureBox", "mx_step",
     "mx_find_HII_bubbles_device", "mx_ComputeTs_device", "mx_ComputeBrightnessTemperatureBox_device",
     "mx_step_device", "mx_profile_enable", "mx_profile_read", "mx_build_info",
-    "mx_brightness_temperature_noalloc",
+    "mx_brightness_temperature_noalloc", "mx_ps_length", "mx_Compute_PS", "mx_Compute_PS_device",
 ]
 
 
@@ -86,5 +86,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mx_brightness_temperature_noalloc.argtypes = [ctypes.POINTER(MxParams), ctypes.c_double, P, P, P, P, P, P,
                                                         ctypes.c_char_p, ctypes.c_size_t]
         L.mx_brightness_temperature_noalloc.restype = ctypes.c_int
+        L.mx_ps_length.argtypes = [P]
+        L.mx_ps_length.restype = ctypes.c_int32
+        L.mx_Compute_PS.argtypes = [P, P, P, P, P, ctypes.c_int32]
+        L.mx_Compute_PS.restype = ctypes.c_int
+        L.mx_Compute_PS_device.argtypes = [P, P, P, P, P, ctypes.c_int32, P]
+        L.mx_Compute_PS_device.restype = ctypes.c_int
         _LIB = L
         return L

@@ -129,3 +129,25 @@ class ReionGridStep:
     def step(self, snapshot: int, grids) -> Dict[str, float]:
         """ComputeTs -> find_HII_bubbles -> brightness temperature."""
         return self._call("mx_step", snapshot, grids)
+
+    def Compute_PS(self, delta_T):
+        """21 cm power spectrum of a REAL delta_T grid (numpy array, or a CUDA
+        tensor on the current stream): (k [1/Mpc], P [mK^2], error) per bin."""
+        n = self.lib.mx_ps_length(self.ctx)
+        if n < 0:
+            self._check(n)
+        out = [np.zeros(n, np.float32) for _ in range(3)]
+        ptrs = [o.ctypes.data for o in out]
+        if _is_torch_cuda(delta_T):
+            import torch
+
+            if delta_T.dtype != torch.float32 or not delta_T.is_contiguous():
+                raise ValueError("delta_T: need contiguous float32")
+            stream = torch.cuda.current_stream().cuda_stream
+            rc = self.lib.mx_Compute_PS_device(self.ctx, delta_T.data_ptr(), *ptrs, n, ctypes.c_void_p(stream))
+        else:
+            d = np.ascontiguousarray(delta_T, dtype=np.float32)
+            rc = self.lib.mx_Compute_PS(self.ctx, d.ctypes.data, *ptrs, n)
+        if rc < 0:
+            self._check(rc)
+        return tuple(out)

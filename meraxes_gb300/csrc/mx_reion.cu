@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "fft3d.cuh"
+#include "ps.cuh"
 #include "host_physics.h"
 #include "kernels.cuh"
 #include "mx_reion.h"
@@ -79,6 +80,9 @@ struct mx_ctx
   float2* d_work = nullptr;     // batch x C
   long long work_fields = 0;    // capacity in spectra
   float2** d_in_ptrs = nullptr; // device array of MAX_FIELDS pointers
+  double* d_ps_partials = nullptr; // RED_BLOCKS x 3 x PS_MAX_BINS
+  double* d_ps_sums = nullptr;     // 3 x PS_MAX_BINS + 1
+  double* h_ps_sums = nullptr;     // pinned copy
   double* d_partials = nullptr; // RED_BLOCKS x 8
   double* d_sums = nullptr;     // 16
   double* h_sums = nullptr;     // pinned, 16
@@ -154,6 +158,9 @@ mx_ctx::~mx_ctx()
   cudaFree(d_unf);
   cudaFree(d_work);
   cudaFree(d_in_ptrs);
+  cudaFree(d_ps_partials);
+  cudaFree(d_ps_sums);
+  cudaFreeHost(h_ps_sums);
   cudaFree(d_partials);
   cudaFree(d_sums);
   cudaFreeHost(h_sums);
@@ -196,6 +203,9 @@ void mx_ctx::alloc_scratch()
   MX_CUDA(cudaMalloc(&d_work, spectrum * cap));
   MX_CUDA(cudaMalloc(&d_in_ptrs, sizeof(float2*) * MAX_FIELDS));
   MX_CUDA(cudaMalloc(&d_partials, sizeof(double) * RED_BLOCKS * 8));
+  MX_CUDA(cudaMalloc(&d_ps_partials, sizeof(double) * RED_BLOCKS * 3 * PS_MAX_BINS));
+  MX_CUDA(cudaMalloc(&d_ps_sums, sizeof(double) * (3 * PS_MAX_BINS + 1)));
+  MX_CUDA(cudaMallocHost(&h_ps_sums, sizeof(double) * (3 * PS_MAX_BINS + 1)));
   MX_CUDA(cudaMalloc(&d_sums, sizeof(double) * 16));
   MX_CUDA(cudaMallocHost(&h_sums, sizeof(double) * 16));
   MX_CUDA(cudaMalloc(&d_rp, sizeof(RadiusParams) * MAX_RADII));
@@ -895,6 +905,75 @@ static void run_delta_T(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* 
 }
 
 // ======================================================================
+// 21 cm power spectrum (src/core/ComputePowerSpectrum.c:18-255)
+// ======================================================================
+// Bin ceilings of Initialise_PowerSpectrum / Compute_PS (:22-40, :133-141):
+// edges[0] = 0, edges[b + 1] = delta_k * 1.35^b by the reference's float
+// recurrence while below delta_k * D.  Returns the number of bins.
+static int ps_edges(const mx_params& p, float* edges, int cap, float* delta_k_out, float* volume_out)
+{
+  const double box_size = p.box_size / p.hubble_h;  // Mpc
+  const float k_factor = 1.35f;
+  const float delta_k = (float)(2. * k::PI / box_size);
+  const float k_max = delta_k * p.grid_dim;
+  float k_ceil = delta_k;
+  int n = 0;
+  edges[0] = 0.0f;
+  while (k_ceil < k_max) {
+    if (n + 1 > cap)
+      throw CudaError{ MX_ENOTSUP, "too many power-spectrum bins" };
+    edges[n + 1] = k_ceil;
+    n++;
+    k_ceil *= k_factor;
+  }
+  *delta_k_out = delta_k;
+  *volume_out = std::pow((float)box_size, 3.0f);
+  return n;
+}
+
+static int run_power_spectrum(mx_ctx* c, const float* dT, float* ps_k, float* ps_data, float* ps_error, int cap,
+                              cudaStream_t s)
+{
+  const GridDims& gd = c->gd;
+  PsArgs a;
+  a.nb = ps_edges(c->p, a.edges, PS_MAX_BINS, &a.delta_k, &a.volume);
+  if (a.nb > cap)
+    throw CudaError{ MX_EINVAL, "output arrays shorter than the number of power-spectrum bins" };
+  float* field = reinterpret_cast<float*>(c->d_work);  // padded real scratch (one spectrum's bytes)
+  double* mean_sum = c->d_ps_sums + 3 * PS_MAX_BINS;
+  {
+    Prof pr(c, "k_ps_mean", 4.0 * (double)gd.N, s);
+    launch_ps_mean(dT, gd.N, c->d_ps_partials, mean_sum, s);
+  }
+  {
+    Prof pr(c, "k_ps_field", 8.0 * (double)gd.N, s);
+    launch_ps_field(dT, mean_sum, a.volume, gd, field, s);
+  }
+  {
+    MX_CUFFT(cufftSetStream(c->r2c_plan, s));
+    Prof pr(c, "cufft_r2c", 4.0 * (double)gd.N + 8.0 * (double)gd.C, s);
+    MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)field, (cufftComplex*)c->d_unf));
+  }
+  a.spec = c->d_unf;
+  a.D = gd.D;
+  a.partials = c->d_ps_partials;
+  {
+    Prof pr(c, "k_ps_bin", 8.0 * (double)gd.C, s);
+    launch_ps_bin(a, c->d_ps_sums, s);
+  }
+  MX_CUDA(cudaMemcpyAsync(c->h_ps_sums, c->d_ps_sums, sizeof(double) * 3 * a.nb, cudaMemcpyDeviceToHost, s));
+  MX_CUDA(cudaStreamSynchronize(s));
+  // :228-240
+  for (int i = 0; i < a.nb; i++) {
+    const double p_box = c->h_ps_sums[i], k_ave = c->h_ps_sums[a.nb + i], ct = c->h_ps_sums[2 * a.nb + i];
+    ps_k[i] = (float)(k_ave / ct);
+    ps_data[i] = (float)(p_box / ct);
+    ps_error[i] = (float)((p_box / ct) / std::sqrt(ct));
+  }
+  return a.nb;
+}
+
+// ======================================================================
 // C ABI
 // ======================================================================
 template <class F>
@@ -949,6 +1028,44 @@ static cudaStream_t pick(mx_ctx* c, void* stream) { return stream ? (cudaStream_
 extern "C" {
 
 const char* mx_build_info(void) { return "meraxes_gb300 reion step, sm_103a, abi 1"; }
+
+int32_t mx_ps_length(const mx_ctx* ctx)
+{
+  if (!ctx)
+    return MX_EINVAL;
+  float edges[PS_MAX_BINS + 1], dk, vol;
+  try {
+    return ps_edges(ctx->p, edges, PS_MAX_BINS, &dk, &vol);
+  } catch (const CudaError& e) {
+    return e.code;
+  }
+}
+
+int mx_Compute_PS(mx_ctx* ctx, const float* delta_T, float* ps_k, float* ps_data, float* ps_error, int32_t cap)
+{
+  int nb = 0;
+  const int rc = guarded(ctx, [&]() {
+    if (!delta_T || !ps_k || !ps_data || !ps_error)
+      throw CudaError{ MX_EINVAL, "Compute_PS: NULL pointer" };
+    ctx->ensure_mirror();
+    cudaStream_t s = ctx->stream;
+    MX_CUDA(cudaMemcpyAsync(ctx->mirror.delta_T, delta_T, sizeof(float) * ctx->gd.N, cudaMemcpyHostToDevice, s));
+    nb = run_power_spectrum(ctx, ctx->mirror.delta_T, ps_k, ps_data, ps_error, cap, s);
+  });
+  return rc == MX_OK ? nb : rc;
+}
+
+int mx_Compute_PS_device(mx_ctx* ctx, const float* delta_T, float* ps_k, float* ps_data, float* ps_error, int32_t cap,
+                         void* stream)
+{
+  int nb = 0;
+  const int rc = guarded(ctx, [&]() {
+    if (!delta_T || !ps_k || !ps_data || !ps_error)
+      throw CudaError{ MX_EINVAL, "Compute_PS: NULL pointer" };
+    nb = run_power_spectrum(ctx, delta_T, ps_k, ps_data, ps_error, cap, pick(ctx, stream));
+  });
+  return rc == MX_OK ? nb : rc;
+}
 
 int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out)
 {

@@ -1625,3 +1625,101 @@ int mxo_delta_T(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
     out->volume_ave_Tb = Ave_Tb;
   return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * 21 cm power spectrum: Initialise_PowerSpectrum (ComputePowerSpectrum.c:18-42)
+ * and Compute_PS (:44-255), single rank, without the Pop III field.
+ * ---------------------------------------------------------------------- */
+int mxo_ps_length(int D, double box_size_mpc_h, double hubble_h)
+{
+  const double box_size = box_size_mpc_h / hubble_h; /* Mpc */
+  const float k_factor = 1.35f;
+  const float delta_k = (float)(2. * M_PI / box_size);
+  const float k_max = delta_k * D;
+  float k_ceil = delta_k;
+  int n = 0;
+  while (k_ceil < k_max) {
+    n++;
+    k_ceil *= k_factor;
+  }
+  return n;
+}
+
+int mxo_power_spectrum(int D, double box_size_mpc_h, double hubble_h, const float* delta_T, float* ps_k, float* ps_data,
+                       float* ps_error, int cap)
+{
+  const int nb = mxo_ps_length(D, box_size_mpc_h, hubble_h);
+  if (nb > cap)
+    return -1;
+  const double box_size = box_size_mpc_h / hubble_h;
+  const float volume = powf((float)box_size, 3);
+  const double total_n_cells = pow((double)D, 3);
+  const int H = D / 2 + 1;
+  /* :74-83 mean of delta_T */
+  double ave = 0.0;
+  for (size_t i = 0; i < (size_t)D * D * D; i++)
+    ave += delta_T[i];
+  ave /= total_n_cells;
+  /* :94-110 the field (delta_T / ave - 1) * V / N * ave in the padded layout */
+  float* deldel = (float*)calloc((size_t)D * D * 2 * H, sizeof(float));
+  float* spec = (float*)malloc(sizeof(float) * 2 * (size_t)D * D * H);
+  for (int ii = 0; ii < D; ii++)
+    for (int jj = 0; jj < D; jj++)
+      for (int kk = 0; kk < D; kk++) {
+        const size_t ip = pad_idx(D, ii, jj, kk);
+        deldel[ip] = (float)((delta_T[real_idx(D, ii, jj, kk)] / ave - 1) * volume / (float)total_n_cells);
+        deldel[ip] *= ave;
+      }
+  mxo_r2c_3d(D, deldel, 1, spec);
+  free(deldel);
+  /* :130-215 binning */
+  const float k_factor = 1.35f;
+  const float delta_k = (float)(2. * M_PI / box_size);
+  const float k_first_bin_ceil = delta_k;
+  const float k_max = delta_k * D;
+  double* p_box = (double*)calloc((size_t)nb, sizeof(double));
+  double* k_ave = (double*)calloc((size_t)nb, sizeof(double));
+  unsigned long long* in_bin_ct = (unsigned long long*)calloc((size_t)nb, sizeof(unsigned long long));
+  const int middle = D / 2;
+  for (int n_x = 0; n_x < D; n_x++) {
+    float k_x = n_x * delta_k;
+    if (n_x > middle)
+      k_x = (n_x - D) * delta_k;
+    for (int n_y = 0; n_y < D; n_y++) {
+      float k_y = n_y * delta_k;
+      if (n_y > middle)
+        k_y = (n_y - D) * delta_k;
+      for (int n_z = 0; n_z <= middle; n_z++) {
+        const float k_z = n_z * delta_k;
+        const float k_mag = (float)sqrt(k_x * k_x + k_y * k_y + k_z * k_z);
+        int ct = 0;
+        float k_floor = 0;
+        float k_ceil = k_first_bin_ceil;
+        while (k_ceil < k_max) {
+          if ((k_mag >= k_floor) && (k_mag < k_ceil)) {
+            const size_t ih = ((size_t)n_x * D + n_y) * H + n_z;
+            const float complex X = spec[2 * ih] + I * spec[2 * ih + 1];
+            in_bin_ct[ct]++;
+            p_box[ct] += pow(k_mag, 3) * pow(cabs(X), 2.) / (2.0 * M_PI * M_PI * volume);
+            k_ave[ct] += k_mag;
+            break;
+          }
+          ct++;
+          k_floor = k_ceil;
+          k_ceil *= k_factor;
+        }
+      }
+    }
+  }
+  /* :228-240 */
+  for (int i = 0; i < nb; i++) {
+    ps_k[i] = (float)(k_ave[i] / (double)in_bin_ct[i]);
+    ps_data[i] = (float)(p_box[i] / (double)in_bin_ct[i]);
+    ps_error[i] = (float)((p_box[i] / (double)in_bin_ct[i]) / sqrt((double)in_bin_ct[i]));
+  }
+  free(spec);
+  free(p_box);
+  free(k_ave);
+  free(in_bin_ct);
+  return nb;
+}

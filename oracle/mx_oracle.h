@@ -37,6 +37,12 @@ int mxo_delta_T(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out);
  * (decides r_bubble, which is overwritten at each ionising radius).  A cell
  * whose outputs can legitimately differ between two FP32 FFT implementations
  * has a small margin.  NULL before a call. */
+/* 21 cm power spectrum of a REAL delta_T grid (Initialise_PowerSpectrum and
+ * Compute_PS, ComputePowerSpectrum.c:18-255); box_size in Mpc/h.  Returns the
+ * number of k bins, or -1 if it exceeds cap. */
+int mxo_ps_length(int D, double box_size_mpc_h, double hubble_h);
+int mxo_power_spectrum(int D, double box_size_mpc_h, double hubble_h, const float* delta_T, float* ps_k, float* ps_data,
+                       float* ps_error, int cap);
 const float* mxo_last_margin(const mxo_ctx* c);
 
 /* Table-level helpers (host physics) for tests. */

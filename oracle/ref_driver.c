@@ -22,6 +22,7 @@
 #include "XRayHeatingFunctions.h"
 #include "find_HII_bubbles.h"
 #include "recombinations.h"
+#include "ComputePowerSpectrum.h"
 #include "reionization.h"
 #include "utils.h"
 
@@ -168,3 +169,24 @@ int mxref_delta_T(int snapshot)
 double mxref_splined_recombination_rate(double z_eff, double gamma12) { return splined_recombination_rate(z_eff, gamma12); }
 double mxref_dtdz(float z) { return dtdz(z); }
 double mxref_RtoM(double R) { return RtoM(R); }
+
+/* Initialise_PowerSpectrum + Compute_PS on a REAL delta_T grid (needs a
+ * context made with flag_21cm so that reion_grids.delta_T exists). */
+int mxref_power_spectrum(const float* delta_T, float* ps_k, float* ps_data, float* ps_error, int cap)
+{
+  reion_grids_t* g = &run_globals.reion_grids;
+  const int D = run_globals.params.ReionGridDim;
+  if (!g->delta_T)
+    return -2;
+  Initialise_PowerSpectrum();
+  const int nb = run_globals.params.PS_Length;
+  if (nb > cap)
+    return -1;
+  memcpy(g->delta_T, delta_T, sizeof(float) * (size_t)D * D * D);
+  g->PS_k = ps_k;
+  g->PS_data = ps_data;
+  g->PS_error = ps_error;
+  Compute_PS(0);
+  g->PS_k = g->PS_data = g->PS_error = NULL;
+  return nb;
+}

@@ -66,6 +66,8 @@ class OracleBackend:
         L.mxo_get_Ts.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                  ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
         L.mxo_get_Ts.restype = ctypes.c_double
+        L.mxo_power_spectrum.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         self.params = params
         self._pc = params.to_ctypes()
         self.ctx = ctypes.c_void_p()
@@ -114,6 +116,15 @@ class OracleBackend:
     def delta_T(self, snapshot: int, state) -> Dict[str, float]:
         return self._call("mxo_delta_T", snapshot, state)
 
+    def power_spectrum(self, delta_T: np.ndarray):
+        """Compute_PS of a REAL delta_T grid: (k, P, error) per k bin."""
+        p = self.params
+        out = [np.zeros(64, np.float32) for _ in range(3)]
+        d = np.ascontiguousarray(delta_T, dtype=np.float32)
+        n = self.lib.mxo_power_spectrum(p.grid_dim, p.box_size, p.hubble_h, _ptr(d), *(_ptr(a) for a in out), 64)
+        assert n > 0
+        return tuple(a[:n].copy() for a in out)
+
     def margin(self) -> np.ndarray:
         """[2, D, D, D]: first-crossing margin and all-radii margin."""
         D = self.params.grid_dim
@@ -158,6 +169,7 @@ class RefBackend:
         L.mxref_stored_fcoll.restype = ctypes.c_double
         L.mxref_splined_recombination_rate.argtypes = [ctypes.c_double, ctypes.c_double]
         L.mxref_splined_recombination_rate.restype = ctypes.c_double
+        L.mxref_power_spectrum.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int]
         self.params = params
         self._pc = params.to_ctypes()
         zz = (ctypes.c_double * len(redshifts))(*redshifts)
@@ -198,6 +210,13 @@ class RefBackend:
 
     def find_HII_bubbles(self, snapshot, state):
         return self._run("mxref_find_HII_bubbles", snapshot, state)
+
+    def power_spectrum(self, delta_T: np.ndarray):
+        out = [np.zeros(64, np.float32) for _ in range(3)]
+        d = np.ascontiguousarray(delta_T, dtype=np.float32)
+        n = self.lib.mxref_power_spectrum(_ptr(d), *(_ptr(a) for a in out), 64)
+        assert n > 0, n
+        return tuple(a[:n].copy() for a in out)
 
     def ComputeTs(self, snapshot, state):
         return self._run("mxref_ComputeTs", snapshot, state)

@@ -8,6 +8,7 @@ grids and the per-snapshot global scalars.
 
     python tests/golden/make_golden.py            # all cases
     python tests/golden/make_golden.py full24     # one case
+    python tests/golden/make_golden.py ps         # power spectrum fixture
 
 Each case runs in a fresh process because the reference keeps its state in
 globals.
@@ -57,9 +58,31 @@ def make_one(name: str):
     print(name, "written")
 
 
+def make_ps(name: str = "plain32_tophat"):
+    """Compute_PS of the reference on the reference's own delta_T output of a
+    golden case: ps_<case>.npz holds delta_T, k, P and error per bin."""
+    import numpy as np
+
+    from cases import CASES
+    from meraxes_gb300 import synthetic as syn
+    from oracle import RefBackend
+
+    d = np.load(os.path.join(HERE, f"{name}.npz"))
+    dT = d["out/delta_T"]
+    w = CASES[name].workload()
+    ref = RefBackend(w.params, w.redshifts, syn.TABLES_DIR)
+    k, P, err = ref.power_spectrum(dT)
+    np.savez_compressed(os.path.join(HERE, f"ps_{name}.npz"), delta_T=dT, k=k, P=P, error=err,
+                        box_size=w.params.box_size, hubble_h=w.params.hubble_h)
+    print(f"ps_{name} written")
+
+
 if __name__ == "__main__":
     from cases import CASES
 
+    if sys.argv[1:2] == ["ps"]:
+        make_ps()
+        sys.exit(0)
     names = sys.argv[1:] or list(CASES)
     if len(names) == 1:
         make_one(names[0])

@@ -169,3 +169,46 @@ def test_unaligned_device_grids_are_rejected():
     good = {k: torch.from_numpy(v.copy()).cuda() for k, v in st.items()}
     out = step.step(s, good)
     assert 0.0 <= out["volume_weighted_global_xH"] <= 1.0
+
+
+# Power spectrum: the transform is FP32 (cuFFT against the reference's FFTW
+# stand-in), so per-bin power agrees to 1e-4 relative; mean |k| per bin to
+# 1e-6 (the same float |k| summed in another order); bins and counts exactly
+# (error / power = 1 / sqrt(count)).
+def _ps_close(a, b):
+    ka, Pa, ea = a
+    kb, Pb, eb = b
+    assert ka.shape == kb.shape
+    np.testing.assert_allclose(kb, ka, rtol=1e-6, atol=0)
+    np.testing.assert_allclose(Pb, Pa, rtol=1e-4, atol=1e-7 * float(np.nanmax(np.abs(Pa))))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        np.testing.assert_allclose(eb / Pb, ea / Pa, rtol=1e-5)
+
+
+def test_gpu_power_spectrum_matches_reference_fixture():
+    import torch
+
+    from meraxes_gb300.api import ReionGridStep
+
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ps_plain32_tophat.npz"))
+    w = CASES["plain32_tophat"].workload()
+    step = ReionGridStep(w.params, w.redshifts)
+    host = step.Compute_PS(d["delta_T"])
+    _ps_close((d["k"], d["P"], d["error"]), host)
+    dev = step.Compute_PS(torch.from_numpy(d["delta_T"].copy()).cuda())
+    for x, y in zip(host, dev):
+        assert np.array_equal(x, y, equal_nan=True)
+
+
+@pytest.mark.parametrize("D,L", [(64, 100.0), (96, 60.0)])
+def test_gpu_power_spectrum_matches_oracle(D, L, tables_dir):
+    from meraxes_gb300.api import ReionGridStep
+    from meraxes_gb300.params import ReionParams
+    from oracle import OracleBackend
+
+    p = ReionParams(grid_dim=D, box_size=L, flag_21cm=1)
+    rng = np.random.default_rng(D)
+    dT = (rng.normal(12.0, 5.0, (D, D, D)) * np.exp(rng.normal(0, 0.3, (D, D, D)))).astype(np.float32)
+    ref = OracleBackend(p, [8.5, 8.0], tables_dir).power_spectrum(dT)
+    got = ReionGridStep(p, [8.5, 8.0]).Compute_PS(dT)
+    _ps_close(ref, got)

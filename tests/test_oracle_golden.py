@@ -66,3 +66,21 @@ def test_fixture_cases_cover_the_paths():
     assert any(CASES[n].workload().params.flag_recombinations for n in CASES)
     assert any(CASES[n].workload().params.flag_spin_temp for n in CASES)
     assert any(len(CASES[n].workload().snapshots) > 1 for n in CASES)
+
+
+def test_oracle_power_spectrum_matches_reference_fixture():
+    """Compute_PS restated == the reference's Compute_PS on the reference's
+    own delta_T output (bit-exact)."""
+    import os
+
+    from cases import CASES
+    from meraxes_gb300 import synthetic as syn
+    from oracle import OracleBackend
+
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ps_plain32_tophat.npz"))
+    w = CASES["plain32_tophat"].workload()
+    orc = OracleBackend(w.params, w.redshifts, syn.TABLES_DIR)
+    k, P, err = orc.power_spectrum(d["delta_T"])
+    assert np.array_equal(k, d["k"], equal_nan=True)
+    assert np.array_equal(P, d["P"], equal_nan=True)
+    assert np.array_equal(err, d["error"], equal_nan=True)

@@ -45,3 +45,28 @@ def test_restatement_bit_exact_against_reference(base, D, ov, fesc):
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip().startswith("OK"), r.stdout
+
+
+PS_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r}); sys.path.insert(0, {tests!r})
+from meraxes_gb300.params import ReionParams
+from meraxes_gb300 import synthetic as syn
+from oracle import OracleBackend, RefBackend
+p = ReionParams(grid_dim={D}, box_size={L}, flag_21cm=1)
+rng = np.random.default_rng(5)
+dT = (rng.normal(10.0, 4.0, ({D},) * 3)).astype(np.float32)
+a = RefBackend(p, [8.5, 8.0], syn.TABLES_DIR).power_spectrum(dT)
+b = OracleBackend(p, [8.5, 8.0], syn.TABLES_DIR).power_spectrum(dT)
+ok = all(np.array_equal(x, y, equal_nan=True) for x, y in zip(a, b))
+print('OK' if ok else 'MISMATCH', [np.max(np.abs(x - y)) for x, y in zip(a, b)])
+"""
+
+
+@pytest.mark.parametrize("D,L", [(16, 40.0), (24, 30.0)])
+def test_power_spectrum_restatement_bit_exact_against_reference(D, L):
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = PS_SCRIPT.format(root=os.path.dirname(here), tests=here, D=D, L=L)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip().startswith("OK"), r.stdout
