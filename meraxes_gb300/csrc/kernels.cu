@@ -9,6 +9,7 @@
 
 #include "kernels.cuh"
 #include "fft3d.cuh"
+#include "pecvel.cuh"
 #include "ps.cuh"
 
 namespace mx {
@@ -67,7 +68,10 @@ __device__ __forceinline__ long long pad_of(long long ir, int D, int H)
 
 }  // namespace
 
-int kernel_launch_count() { return g_launches + ts_kernel_launches() + fft_kernel_launches() + ps_kernel_launches(); }
+int kernel_launch_count()
+{
+  return g_launches + ts_kernel_launches() + fft_kernel_launches() + ps_kernel_launches() + pecvel_kernel_launches();
+}
 void reset_kernel_launch_count() { g_launches = 0; }
 
 // ================================================================= filter

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "fft3d.cuh"
+#include "pecvel.cuh"
 #include "ps.cuh"
 #include "host_physics.h"
 #include "kernels.cuh"
@@ -868,14 +869,77 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
 // ======================================================================
 // ComputeBrightnessTemperatureBox (src/core/BrightnessTemperature.c:24-549)
 // ======================================================================
+// Peculiar-velocity corrections (BrightnessTemperature.c:158-509), after
+// the base delta_T; vel is converted in place like the reference does.
+static void run_pecvel(mx_ctx* c, const mx_grids* g, float redshift, cudaStream_t s)
+{
+  const mx_params& p = c->p;
+  const GridDims& gd = c->gd;
+  const float H_z = (float)(float)hubble(p, redshift);
+  {
+    Prof pr(c, "k_vel_convert", 8.0 * (double)gd.N, s);
+    launch_vel_convert(g->vel, p.trees_id, redshift, gd, s);
+  }
+  float2* spec = c->d_unf;  // slot 0: spectrum, then dv/dx in place
+  {
+    MX_CUFFT(cufftSetStream(c->r2c_plan, s));
+    Prof pr(c, "cufft_r2c", 4.0 * (double)gd.N + 8.0 * (double)gd.C, s);
+    MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)g->vel, (cufftComplex*)spec));
+  }
+  {
+    // velocity_gradient (reionization.c:2172-2187): k from BoxSize in Mpc/h
+    const float box_f = (float)p.box_size;
+    const float dk = (float)(2.0 * k::PI / box_f);
+    Prof pr(c, "k_vel_grad_k", 16.0 * (double)gd.C, s);
+    launch_vel_grad_k(spec, gd, p.hubble_h, dk, s);
+  }
+  {
+    const cufftHandle plan = c->c2r_plan(1);
+    MX_CUFFT(cufftSetStream(plan, s));
+    Prof pr(c, "cufft_c2r", 8.0 * (double)gd.C + 4.0 * (double)gd.N, s);
+    MX_CUFFT(cufftExecC2R(plan, (cufftComplex*)spec, (cufftReal*)spec));
+  }
+  PecvelArgs pa;
+  pa.grad = reinterpret_cast<const float*>(spec);
+  pa.delta_T = g->delta_T;
+  pa.TS = g->TS_box;
+  pa.mode = p.flag_pecvel;
+  pa.H_z = H_z;
+  pa.redshift = redshift;
+  pa.max_v_deriv = std::fabs((double)(0.2f * H_z));  // fabs(MAX_DVDR * H_z), MAX_DVDR = (float)0.2
+  pa.T_rad = k::TCMB * (1. + redshift);
+  {
+    Prof pr(c, "k_pecvel_cells", (p.flag_pecvel > 1 ? 16.0 : 12.0) * (double)gd.N, s);
+    launch_pecvel_cells(pa, gd, s);
+  }
+  if (p.flag_pecvel == 3) {
+    RsdArgs ra;
+    ra.vel = g->vel;
+    ra.delta_T = g->delta_T;
+    ra.xH = g->xH;
+    ra.los = reinterpret_cast<float*>(c->d_unf + gd.C);  // slot 1 as REAL scratch
+    ra.delta_T_out = g->delta_T;
+    ra.box = p.box_size / p.hubble_h;
+    ra.subcell_width = (ra.box / ((double)gd.D)) / (double)RSD_STEPS;
+    for (int i = 0; i < RSD_STEPS; i++) {
+      ra.x_pos_offset[i] = (float)(ra.subcell_width * (float)i + ra.subcell_width / 2.);
+      ra.x_pos[i] = (float)(ra.x_pos_offset[i] / (ra.box / (float)gd.D));
+    }
+    ra.H_z = H_z;
+    Prof pr(c, "k_rsd_columns", 20.0 * (double)gd.N, s);
+    launch_rsd(ra, gd, s);
+  }
+}
+
 static void run_delta_T(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s)
 {
   const mx_params& p = c->p;
   const GridDims& gd = c->gd;
   const int launches0 = kernel_launch_count();
-  if (p.flag_spin_temp && p.flag_pecvel > 0)
-    throw CudaError{ MX_ENOTSUP, "peculiar-velocity modes of the brightness temperature are not built" };
-  if (!g->deltax || !g->xH || !g->delta_T || (p.flag_spin_temp && !g->TS_box))
+  const bool pecvel = p.flag_spin_temp && p.flag_pecvel > 0;
+  if (p.flag_pecvel < 0 || p.flag_pecvel > 3)
+    throw CudaError{ MX_EINVAL, "Flag_IncludePecVelsFor21cm must be 0-3" };
+  if (!g->deltax || !g->xH || !g->delta_T || (p.flag_spin_temp && !g->TS_box) || (pecvel && !g->vel))
     throw CudaError{ MX_EINVAL, "ComputeBrightnessTemperatureBox: a required grid pointer is NULL" };
   const float redshift = (float)(float)c->zz[snapshot];
   const float Hubble_h = (float)(float)p.hubble_h;
@@ -893,9 +957,17 @@ static void run_delta_T(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* 
   a.spin = p.flag_spin_temp;
   a.pecvel = p.flag_pecvel;
   a.partials = c->d_partials;
-  Prof pr(c, "k_delta_T", (p.flag_spin_temp ? 4.0 : 3.0) * 4.0 * (double)gd.N, s);
-  launch_delta_T(a, gd, s);
-  launch_finalize(c->d_partials, 1, c->d_sums, s);
+  {
+    Prof pr(c, "k_delta_T", (p.flag_spin_temp ? 4.0 : 3.0) * 4.0 * (double)gd.N, s);
+    launch_delta_T(a, gd, s);
+  }
+  if (pecvel) {
+    run_pecvel(c, g, redshift, s);
+    Prof pr(c, "k_ps_mean", 4.0 * (double)gd.N, s);
+    launch_ps_mean(g->delta_T, gd.N, c->d_ps_partials, c->d_sums, s);
+  } else {
+    launch_finalize(c->d_partials, 1, c->d_sums, s);
+  }
   MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double), cudaMemcpyDeviceToHost, s));
   MX_CUDA(cudaStreamSynchronize(s));
   if (out) {
@@ -1295,6 +1367,9 @@ void copy_fields(mx_ctx* c, const mx_grids* host, const std::vector<FieldIO>& fi
     float* d = c->mirror.*(f.member);
     if (!h)
       continue;
+    // vel is read (and converted in place) only by the peculiar-velocity modes
+    if (f.member == &mx_grids::vel && !(c->p.flag_spin_temp && c->p.flag_pecvel > 0))
+      continue;
     const size_t n = f.padded ? (size_t)c->gd.P : (size_t)c->gd.N;
     if (dir == IN)
       MX_CUDA(cudaMemcpyAsync(d, h, n * sizeof(float), cudaMemcpyHostToDevice, s));
@@ -1348,6 +1423,7 @@ const std::vector<FieldIO>& dt_fields()
     { &mx_grids::xH, false, IN },
     { &mx_grids::TS_box, false, IN },
     { &mx_grids::delta_T, false, OUT },
+    { &mx_grids::vel, true, IN | OUT },  // only with peculiar velocities (see copy_fields)
   };
   return f;
 }
@@ -1422,6 +1498,8 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
     if (ctx->p.flag_spin_temp)
       for (const FieldIO& f : ts_fields())
         all.push_back(f);
+    if (ctx->p.flag_21cm)
+      all.push_back({ &mx_grids::vel, true, IN | OUT });  // peculiar-velocity modes only
     copy_fields(ctx, host, all, IN, s);
     if (ctx->p.flag_spin_temp)
       copy_histories(ctx, host, s);

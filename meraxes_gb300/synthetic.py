@@ -97,6 +97,31 @@ class FieldGenerator:
         d = self.base * (growth_factor(z, self.p) / self.d_norm)
         return np.maximum(d, -0.99).astype(np.float32)
 
+    def velocity_real(self, snapshot: int) -> np.ndarray:
+        """Line-of-sight velocity grid in the trees' units: a Gaussian field
+        (seed + 7919) smoothed over 3 cells, with 50 km/s rms peculiar
+        velocity at the normalisation redshift, grown like the density (in
+        the small test boxes |dv/dx| stays below half the Hubble rate, away
+        from the caustics where the optical-depth form is ill-conditioned);
+        divided by (1+z) for the VELOCIRAPTOR convention (the step multiplies
+        it back), times 1000 sqrt(1+z) for GBPTREES."""
+        if not hasattr(self, "_vbase"):
+            D, L = self.p.grid_dim, self.p.box_size
+            v = gaussian_field(D, L, self.w.seed + 7919, sigma=1.0)
+            k = 2.0 * np.pi * np.fft.fftfreq(D, d=L / D)
+            kz = 2.0 * np.pi * np.fft.rfftfreq(D, d=L / D)
+            k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + kz[None, None, :] ** 2
+            rs = 3.0 * L / D
+            v = np.fft.irfftn(np.fft.rfftn(v) * np.exp(-0.5 * k2 * rs * rs), s=(D, D, D), axes=(0, 1, 2))
+            self._vbase = v / v.std()
+        z = self.w.redshifts[snapshot]
+        v = 50.0 * self._vbase * (growth_factor(z, self.p) / self.d_norm)
+        if self.p.trees_id == 1:
+            v = v * 1000.0 * np.sqrt(1.0 + z)
+        else:
+            v = v / (1.0 + z)
+        return v.astype(np.float32)
+
     def stars_sfr_real(self, snapshot: int):
         d = self.deltax_real(snapshot).astype(np.float64)
         stars = np.where(d > 0.5, 1e-3 * np.exp(2.0 * d), 0.0)
@@ -115,6 +140,8 @@ class FieldGenerator:
             "weighted_sfr": to_padded((fesc * sfr.astype(np.float64)).astype(np.float32)),
             "sfr": to_padded(sfr),
         }
+        if self.p.flag_pecvel > 0 and self.p.flag_spin_temp:
+            out["vel"] = to_padded(self.velocity_real(snapshot))
         if n_sfr_hist > 0:
             D = self.p.grid_dim
             n_pad = int(np.prod(padded_shape(D)))

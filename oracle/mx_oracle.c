@@ -68,6 +68,7 @@
 struct mxo_ctx
 {
   mx_params p;
+  float* last_vel_grad; /* dv/dx of the last peculiar-velocity delta_T (padded), for tests */
   double unit_time_s, G, hubble_int, rho_crit;
   double no, he_no, f_h, f_he, n_b0;
   double* zz;
@@ -506,6 +507,7 @@ void mxo_destroy(mxo_ctx* c)
 {
   if (!c)
     return;
+  free(c->last_vel_grad);
   if (c->mhr_ready) {
     mxo_spline_free(&c->A_sp);
     mxo_spline_free(&c->C_sp);
@@ -1584,14 +1586,234 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
 
 /* ComputeBrightnessTemperatureBox, BrightnessTemperature.c:24-124, 512-548
  * (peculiar-velocity modes are not restated here) */
+#define MXO_N_RSD_STEPS 50
+#define MXO_MAX_DVDR 0.2f
+#define MXO_FRACT_FLOAT_ERR 1e-7
+#define MXO_MPC 3.086e24
+
+/* One z column of the line-of-sight remap (BrightnessTemperature.c:325-499):
+ * the sub-cells of every cell are displaced by the interpolated velocity and
+ * deposited, with the reference's float / double mix, into los[0..D). */
+void mxo_rsd_column(int D, double BoxSize, double subcell_width, double x_val1, double x_val2, const float* x_pos,
+                    const float* x_pos_offset, float H_z, const float* vel, const float* delta_T, const float* xH,
+                    float* los)
+{
+  const int N = MXO_N_RSD_STEPS;
+  for (int kk = 0; kk < D; kk++)
+    los[kk] = 0.0;
+  for (int kk = 0; kk < D; kk++) {
+    if (!((fabs(delta_T[kk]) >= MXO_FRACT_FLOAT_ERR) && (xH[kk] >= MXO_FRACT_FLOAT_ERR)))
+      continue;
+    double d1_low, d2_low, d1_high, d2_high;
+    if (kk == 0) {
+      d1_low = vel[D - 1] / H_z;
+      d2_low = vel[kk] / H_z;
+    } else {
+      d1_low = vel[kk - 1] / H_z;
+      d2_low = vel[kk] / H_z;
+    }
+    if (kk == (D - 1)) {
+      d1_high = vel[kk] / H_z;
+      d2_high = vel[0] / H_z;
+    } else {
+      d1_high = vel[kk] / H_z;
+      d2_high = vel[kk + 1] / H_z;
+    }
+    const float dT = delta_T[kk];
+    for (int iii = 0; iii < N; iii++) {
+      double subcell_displacement;
+      if (x_pos[iii] <= 0.5)
+        subcell_displacement = d1_low + ((x_pos[iii] + 0.5) - x_val1) * (d2_low - d1_low) / (x_val2 - x_val1);
+      else
+        subcell_displacement = d1_high + ((x_pos[iii] - 0.5) - x_val1) * (d2_high - d1_high) / (x_val2 - x_val1);
+      const double RSD_pos_new = (x_pos_offset[iii] + subcell_displacement) / (BoxSize / (float)D);
+      const double lo = RSD_pos_new - (subcell_width / 2.) / (BoxSize / (float)D);
+      const double hi = RSD_pos_new + (subcell_width / 2.) / (BoxSize / (float)D);
+      if (lo >= 0.0 && hi < 1.0) {
+        los[kk] += dT / (float)N;
+      } else if (lo < 0.0 && hi < 0.0) {
+        const double cell_distance = ceil(fabs(lo)) - 1.;
+        const int cd = (int)cell_distance;
+        if (fabs(hi) > cell_distance) {
+          if (kk < (cd + 1))
+            los[kk - (cd + 1) + D] += dT / (float)N;
+          else
+            los[kk - (cd + 1)] += dT / (float)N;
+        } else {
+          const double fraction_outside = (fabs(lo) - cell_distance) / (subcell_width / (BoxSize / (float)D));
+          const double fraction_within = 1. - fraction_outside;
+          if (kk < cd)
+            los[kk - cd + D] += fraction_within * dT / (float)N;
+          else
+            los[kk - cd] += fraction_within * dT / (float)N;
+          if (kk < (cd + 1))
+            los[kk - (cd + 1) + D] += fraction_outside * dT / (float)N;
+          else
+            los[kk - (cd + 1)] += fraction_outside * dT / (float)N;
+        }
+      } else if (lo < 0.0 && (hi > 0.0 && hi < 1.0)) {
+        const double fraction_within = hi / (subcell_width / (BoxSize / (float)D));
+        const double fraction_outside = 1. - fraction_within;
+        if (kk == 0) {
+          los[D - 1] += fraction_outside * dT / (float)N;
+          los[kk] += fraction_within * dT / (float)N;
+        } else {
+          los[kk - 1] += fraction_outside * dT / (float)N;
+          los[kk] += fraction_within * dT / (float)N;
+        }
+      } else if ((lo >= 0.0 && lo < 1.0) && (hi >= 1.0)) {
+        const double fraction_outside = (hi - 1.) / (subcell_width / (BoxSize / (float)D));
+        const double fraction_within = 1. - fraction_outside;
+        if (kk == (D - 1)) {
+          los[kk] += fraction_within * dT / (float)N;
+          los[0] += fraction_outside * dT / (float)N;
+        } else {
+          los[kk] += fraction_within * dT / (float)N;
+          los[kk + 1] += fraction_outside * dT / (float)N;
+        }
+      } else {
+        const double cell_distance = floor(fabs(hi));
+        const int cd = (int)cell_distance;
+        if (lo >= cell_distance) {
+          if (kk > (D - 1 - cd))
+            los[kk + cd - D] += dT / (float)N;
+          else
+            los[kk + cd] += dT / (float)N;
+        } else {
+          const double fraction_outside = (hi - cell_distance) / (subcell_width / (BoxSize / (float)D));
+          const double fraction_within = 1. - fraction_outside;
+          if (kk > (D - 1 - (cd - 1)))
+            los[kk + cd - 1 - D] += fraction_within * dT / (float)N;
+          else
+            los[kk + cd - 1] += fraction_within * dT / (float)N;
+          if (kk > (D - 1 - cd))
+            los[kk + cd - D] += fraction_outside * dT / (float)N;
+          else
+            los[kk + cd] += fraction_outside * dT / (float)N;
+        }
+      }
+    }
+  }
+}
+
+/* Peculiar-velocity corrections of the brightness temperature,
+ * BrightnessTemperature.c:158-509 (spin temperature on,
+ * Flag_IncludePecVelsFor21cm 1-3); vel is converted in place like the
+ * reference does. */
+static void pecvel_correction(mxo_ctx* c, const mx_grids* g, float redshift, double T_rad)
+{
+  const mx_params* p = &c->p;
+  const int D = p->grid_dim, H = D / 2 + 1;
+  const double total_n_cells = pow((double)D, 3);
+  const double BoxSize = p->box_size / p->hubble_h;
+  const float H_z = (float)(float)c_hubble(c, redshift);
+  float* vel = g->vel;
+  float* delta_T = g->delta_T;
+  /* :180-209 velocity units */
+  for (int ii = 0; ii < D; ii++)
+    for (int jj = 0; jj < D; jj++)
+      for (int kk = 0; kk < D; kk++) {
+        const size_t ip = pad_idx(D, ii, jj, kk);
+        switch (p->trees_id) {
+          case 1: /* GBPTREES_TREES */
+            vel[ip] = (float)(sqrt(1. / (1. + redshift)) * vel[ip] / 1000.);
+            break;
+          case 0: /* VELOCIRAPTOR_TREES */
+          case 2: /* VELOCIRAPTOR_TREES_AUG */
+            vel[ip] = (float)((1. + redshift) * vel[ip]);
+            break;
+        }
+        vel[ip] *= 1000. * 100. / MXO_MPC;
+        vel[ip] = (float)(vel[ip] / (1. / (1. + redshift)));
+      }
+  /* :212-228 gradient along z in k-space */
+  const size_t nc = (size_t)D * D * H;
+  float* spec = (float*)malloc(sizeof(float) * 2 * nc);
+  float* grad = (float*)malloc(sizeof(float) * 2 * nc);
+  mxo_r2c_3d(D, vel, 1, spec);
+  for (size_t i = 0; i < nc; i++) {
+    float complex v = spec[2 * i] + I * spec[2 * i + 1];
+    v /= total_n_cells;
+    v *= p->hubble_h;
+    spec[2 * i] = crealf(v);
+    spec[2 * i + 1] = cimagf(v);
+  }
+  {
+    /* velocity_gradient, reionization.c:2172-2187 (k from BoxSize in Mpc/h) */
+    const float box_size = (float)p->box_size;
+    const float delta_k = (float)(2.0 * M_PI / box_size);
+    for (int n_x = 0; n_x < D; n_x++)
+      for (int n_y = 0; n_y < D; n_y++)
+        for (int n_z = 0; n_z <= D / 2; n_z++) {
+          const float k_z = n_z * delta_k;
+          const size_t ih = ((size_t)n_x * D + n_y) * H + n_z;
+          float complex v = spec[2 * ih] + I * spec[2 * ih + 1];
+          v *= (float complex)(k_z * I);
+          spec[2 * ih] = crealf(v);
+          spec[2 * ih + 1] = cimagf(v);
+        }
+  }
+  mxo_c2r_3d(D, spec, grad); /* padded real */
+  free(spec);
+  free(c->last_vel_grad);
+  c->last_vel_grad = grad;
+  const double max_v_deriv = fabs(MXO_MAX_DVDR * H_z);
+  if (p->flag_pecvel == 1) {
+    /* :232-257 */
+    for (int ii = 0; ii < D; ii++)
+      for (int jj = 0; jj < D; jj++)
+        for (int kk = 0; kk < D; kk++) {
+          const size_t ir = real_idx(D, ii, jj, kk), ip = pad_idx(D, ii, jj, kk);
+          double dvdx = (double)grad[ip];
+          if (fabs(dvdx) > max_v_deriv)
+            dvdx = dvdx < 0 ? -max_v_deriv : max_v_deriv;
+          delta_T[ir] /= (dvdx / H_z + 1.0);
+        }
+  }
+  if (p->flag_pecvel > 1) {
+    /* :261-315 (spin temperature on) */
+    for (int ii = 0; ii < D; ii++)
+      for (int jj = 0; jj < D; jj++)
+        for (int kk = 0; kk < D; kk++) {
+          const size_t ir = real_idx(D, ii, jj, kk), ip = pad_idx(D, ii, jj, kk);
+          const double gradient_component = fabs((double)grad[ip] / H_z + 1.0);
+          if (gradient_component < MXO_FRACT_FLOAT_ERR)
+            delta_T[ir] = (float)(1000. * (g->TS_box[ir] - T_rad) / (1. + redshift));
+          else
+            delta_T[ir] = (float)((1. - exp(-delta_T[ir] / gradient_component)) * 1000. * (g->TS_box[ir] - T_rad) /
+                                  (1. + redshift));
+        }
+  }
+  if (p->flag_pecvel == 3) {
+    /* :317-505 line-of-sight redshift-space distortions along z */
+    const double subcell_width = (BoxSize / ((double)D)) / (double)MXO_N_RSD_STEPS;
+    float x_pos[MXO_N_RSD_STEPS], x_pos_offset[MXO_N_RSD_STEPS];
+    for (int iii = 0; iii < MXO_N_RSD_STEPS; iii++) {
+      x_pos_offset[iii] = (float)(subcell_width * (float)iii + subcell_width / 2.);
+      x_pos[iii] = (float)(x_pos_offset[iii] / (BoxSize / (float)D));
+    }
+    float* los = (float*)malloc(sizeof(float) * (size_t)D);
+    for (int ii = 0; ii < D; ii++)
+      for (int jj = 0; jj < D; jj++) {
+        mxo_rsd_column(D, BoxSize, subcell_width, 0., 1., x_pos, x_pos_offset, H_z, vel + pad_idx(D, ii, jj, 0),
+                       delta_T + real_idx(D, ii, jj, 0), g->xH + real_idx(D, ii, jj, 0), los);
+        for (int kk = 0; kk < D; kk++)
+          delta_T[real_idx(D, ii, jj, kk)] = los[kk];
+      }
+    free(los);
+  }
+}
+
 int mxo_delta_T(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
 {
   const mx_params* p = &c->p;
   const int D = p->grid_dim;
   if (snapshot < 0 || snapshot >= c->n_snaps)
     return MX_ESTATE;
-  if (p->flag_pecvel != 0 && p->flag_spin_temp)
-    return MX_ENOTSUP;
+  if (p->flag_pecvel < 0 || p->flag_pecvel > 3)
+    return MX_EINVAL;
+  if (p->flag_pecvel != 0 && p->flag_spin_temp && (!g->vel || !g->TS_box))
+    return MX_EINVAL;
   const double total_n_cells = pow((double)D, 3);
   const float redshift = (float)(float)c->zz[snapshot];
   const float Hubble_h = (float)(float)p->hubble_h;
@@ -1617,6 +1839,8 @@ int mxo_delta_T(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
           }
         }
       }
+  if (p->flag_spin_temp && p->flag_pecvel > 0)
+    pecvel_correction(c, g, redshift, T_rad);
   double Ave_Tb = 0.0;
   for (size_t i = 0; i < (size_t)D * D * D; i++)
     Ave_Tb += (double)g->delta_T[i];
@@ -1723,3 +1947,5 @@ int mxo_power_spectrum(int D, double box_size_mpc_h, double hubble_h, const floa
   free(in_bin_ct);
   return nb;
 }
+
+const float* mxo_last_velocity_gradient(const mxo_ctx* c) { return c->last_vel_grad; }

@@ -44,6 +44,8 @@ int mxo_ps_length(int D, double box_size_mpc_h, double hubble_h);
 int mxo_power_spectrum(int D, double box_size_mpc_h, double hubble_h, const float* delta_T, float* ps_k, float* ps_data,
                        float* ps_error, int cap);
 const float* mxo_last_margin(const mxo_ctx* c);
+/* dv/dx (padded layout) of the last delta_T with peculiar velocities, or NULL. */
+const float* mxo_last_velocity_gradient(const mxo_ctx* c);
 
 /* Table-level helpers (host physics) for tests. */
 double mxo_recombination_rate_splined(mxo_ctx* c, double z_eff, double gamma12);

@@ -66,6 +66,8 @@ class OracleBackend:
         L.mxo_get_Ts.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                  ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
         L.mxo_get_Ts.restype = ctypes.c_double
+        L.mxo_last_velocity_gradient.argtypes = [ctypes.c_void_p]
+        L.mxo_last_velocity_gradient.restype = ctypes.POINTER(ctypes.c_float)
         L.mxo_power_spectrum.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         self.params = params
@@ -115,6 +117,15 @@ class OracleBackend:
 
     def delta_T(self, snapshot: int, state) -> Dict[str, float]:
         return self._call("mxo_delta_T", snapshot, state)
+
+    def velocity_gradient(self) -> Optional[np.ndarray]:
+        """dv/dx (REAL layout) of the last delta_T with peculiar velocities."""
+        ptr = self.lib.mxo_last_velocity_gradient(self.ctx)
+        if not ptr:
+            return None
+        D = self.params.grid_dim
+        a = np.ctypeslib.as_array(ptr, shape=(D * D * 2 * (D // 2 + 1),)).reshape(D, D, -1)
+        return np.ascontiguousarray(a[:, :, :D])
 
     def power_spectrum(self, delta_T: np.ndarray):
         """Compute_PS of a REAL delta_T grid: (k, P, error) per k bin."""

@@ -52,6 +52,15 @@ CASES = {
     # several snapshots with the SFR-history reweighting and persistent state
     "evolve16": Case("evolve16", "evolve_512", 16, {"reion_efficiency": REION_EFF, "clumping_factor": 2.0},
                      fesc=0.01, snapshots=[0, 1, 2, 3, 4, 5]),
+    # peculiar-velocity modes of the brightness temperature: 1 capped
+    # gradient, 2 optical depth (GBPTREES velocity units), 3 with the
+    # line-of-sight redshift-space remap
+    "full24_pv1": Case("full24_pv1", "full_256", 24, {"reion_efficiency": REION_EFF, "clumping_factor": 2.0,
+                                                      "flag_pecvel": 1}, fesc=0.01),
+    "full24_pv2": Case("full24_pv2", "full_256", 24, {"reion_efficiency": REION_EFF, "clumping_factor": 2.0,
+                                                      "flag_pecvel": 2, "trees_id": 1}, fesc=0.01),
+    "full24_pv3": Case("full24_pv3", "full_256", 24, {"reion_efficiency": REION_EFF, "clumping_factor": 2.0,
+                                                      "flag_pecvel": 3}, fesc=0.01),
 }
 
 
@@ -76,4 +85,4 @@ def run_case(backend, w: Workload, gen: Optional[syn.FieldGenerator] = None, sta
 
 
 OUTPUT_GRIDS = ["xH", "z_at_ionization", "r_bubble", "J_21", "J_21_at_ionization", "Gamma12", "N_rec", "delta_T",
-                "TS_box", "Tk_box", "x_e_box_prev", "x_e_box"]
+                "TS_box", "Tk_box", "x_e_box_prev", "x_e_box", "vel"]

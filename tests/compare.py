@@ -95,6 +95,7 @@ def compare(ref: Dict[str, np.ndarray], test: Dict[str, np.ndarray], ref_globals
         "TS_box": np.ones(n, bool),
         "Tk_box": np.ones(n, bool),
         "x_e_box_prev": np.ones(n, bool),
+        "vel": np.ones(n, bool),
         "J_21": first_dep,
         "J_21_at_ionization": first_dep,
         "Gamma12": first_dep,
@@ -126,7 +127,7 @@ def compare(ref: Dict[str, np.ndarray], test: Dict[str, np.ndarray], ref_globals
         err = np.abs(a - b)[sel] / np.maximum(np.abs(a[sel]), floor * scale)
         rep[k] = float(err.max()) if err.size else 0.0
         rep[k + "_outliers"] = int(bad.sum())
-        allowed = 0 if margin is not None or k in ("TS_box", "Tk_box", "x_e_box_prev", "xH", "delta_T") \
+        allowed = 0 if margin is not None or k in ("TS_box", "Tk_box", "x_e_box_prev", "xH", "delta_T", "vel") \
             else FLAG_FRACTION * n
         if bad.sum() > allowed:
             i = int(np.flatnonzero(bad)[0])

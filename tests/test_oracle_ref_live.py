@@ -38,6 +38,11 @@ print('MISMATCH' if bad else 'OK', bad)
     ("plain_64", 16, {"reion_efficiency": 2000.0, "delta_r_factor": 1.3}, 1.0),
     ("plain_64", 20, {"reion_efficiency": 5000.0, "filter_type": 1, "uvb_flag": 0}, 1.0),
     ("full_256", 16, {"reion_efficiency": 31043.0, "clumping_factor": 2.0, "filter_type": 2}, 0.02),
+    # peculiar-velocity modes of the brightness temperature (half-neutral
+    # boxes: mean xH ~0.5, delta_T ~10 mK, every mode changes it)
+    ("full_256", 16, {"reion_efficiency": 31043.3, "clumping_factor": 2.0, "flag_pecvel": 1}, 0.01),
+    ("full_256", 16, {"reion_efficiency": 31043.3, "clumping_factor": 2.0, "flag_pecvel": 2, "trees_id": 1}, 0.01),
+    ("full_256", 20, {"reion_efficiency": 31043.3, "clumping_factor": 2.0, "flag_pecvel": 3}, 0.01),
 ])
 def test_restatement_bit_exact_against_reference(base, D, ov, fesc):
     here = os.path.dirname(os.path.abspath(__file__))
