@@ -209,6 +209,37 @@ typedef struct mx_kernel_stat
 int mx_profile_enable(mx_ctx* ctx, int32_t on);
 int32_t mx_profile_read(mx_ctx* ctx, mx_kernel_stat* out, int32_t cap);
 
+/* Light cone: Initialise_ConstructLightcone and ConstructLightcone
+ * (src/core/ConstructLightcone.c:12-166, header ConstructLightcone.h).  The
+ * reference keeps LightconeLength, EndSnapshotLightcone and CurrentLCPos in
+ * run_globals.params and the boxes in run_globals.reion_grids; here the
+ * context keeps the first three and the caller passes the arrays.
+ * mx_lightcone_init(ctx, EndRedshiftLightcone, LastOutputSnap, &end) returns
+ * LightconeLength (or a negative MX_E* code) and sets *end to
+ * EndSnapshotLightcone; call it after mx_set_redshifts.
+ * mx_ConstructLightcone is called for every snapshot in order, like the
+ * reference: it fills the slices between ZZ[snapshot] and ZZ[snapshot-1] of
+ * lightcone (float[D][D][LightconeLength], slice fastest: grid_index_LC,
+ * misc_tools.c:222-229) by time interpolation between delta_T_prev and
+ * delta_T (REAL grids), writes their redshifts into lightcone_redshifts
+ * (float[LightconeLength], a HOST array in both variants), then copies
+ * delta_T into delta_T_prev.  The _device variant takes device grids and a
+ * device light cone. */
+int64_t mx_lightcone_init(mx_ctx* ctx, double end_redshift, int32_t last_output_snap, int32_t* end_snapshot);
+int mx_ConstructLightcone(mx_ctx* ctx,
+                          int32_t snapshot,
+                          const float* delta_T,
+                          float* delta_T_prev,
+                          float* lightcone,
+                          float* lightcone_redshifts);
+int mx_ConstructLightcone_device(mx_ctx* ctx,
+                                 int32_t snapshot,
+                                 const float* delta_T,
+                                 float* delta_T_prev,
+                                 float* lightcone,
+                                 float* lightcone_redshifts,
+                                 void* stream);
+
 /* 21 cm power spectrum of a delta_T grid (REAL layout): Initialise_PowerSpectrum
  * and Compute_PS (src/core/ComputePowerSpectrum.c:18-255, header
  * ComputePowerSpectrum.h:9-10).  The reference writes

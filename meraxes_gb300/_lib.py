@@ -24,6 +24,7 @@ EXPORTS = [
     "mx_find_HII_bubbles_device", "mx_ComputeTs_device", "mx_ComputeBrightnessTemperatureBox_device",
     "mx_step_device", "mx_profile_enable", "mx_profile_read", "mx_build_info",
     "mx_brightness_temperature_noalloc", "mx_ps_length", "mx_Compute_PS", "mx_Compute_PS_device",
+    "mx_lightcone_init", "mx_ConstructLightcone", "mx_ConstructLightcone_device",
 ]
 
 
@@ -92,5 +93,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mx_Compute_PS.restype = ctypes.c_int
         L.mx_Compute_PS_device.argtypes = [P, P, P, P, P, ctypes.c_int32, P]
         L.mx_Compute_PS_device.restype = ctypes.c_int
+        L.mx_lightcone_init.argtypes = [P, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+        L.mx_lightcone_init.restype = ctypes.c_int64
+        L.mx_ConstructLightcone.argtypes = [P, ctypes.c_int32, P, P, P, P]
+        L.mx_ConstructLightcone.restype = ctypes.c_int
+        L.mx_ConstructLightcone_device.argtypes = [P, ctypes.c_int32, P, P, P, P, P]
+        L.mx_ConstructLightcone_device.restype = ctypes.c_int
         _LIB = L
         return L

@@ -151,3 +151,33 @@ class ReionGridStep:
         if rc < 0:
             self._check(rc)
         return tuple(out)
+
+    def lightcone_init(self, end_redshift: float, last_output_snap: int):
+        """Initialise_ConstructLightcone: (LightconeLength, EndSnapshotLightcone)."""
+        end = ctypes.c_int32()
+        n = self.lib.mx_lightcone_init(self.ctx, end_redshift, last_output_snap, ctypes.byref(end))
+        if n < 0:
+            self._check(int(n))
+        return int(n), end.value
+
+    def ConstructLightcone(self, snapshot: int, delta_T, delta_T_prev, lightcone, lightcone_redshifts):
+        """Fills this snapshot's slices of `lightcone` ([D][D][length]) and
+        `lightcone_redshifts` (numpy, host) and copies delta_T into
+        delta_T_prev.  Grids and light cone are numpy arrays or CUDA tensors
+        (device family, current stream)."""
+        z = lightcone_redshifts
+        if not (isinstance(z, np.ndarray) and z.dtype == np.float32 and z.flags.c_contiguous):
+            raise ValueError("lightcone_redshifts: need a C-contiguous float32 numpy array")
+        if _is_torch_cuda(delta_T):
+            import torch
+
+            stream = torch.cuda.current_stream().cuda_stream
+            rc = self.lib.mx_ConstructLightcone_device(self.ctx, snapshot, delta_T.data_ptr(), delta_T_prev.data_ptr(),
+                                                       lightcone.data_ptr(), z.ctypes.data, ctypes.c_void_p(stream))
+        else:
+            for a in (delta_T, delta_T_prev, lightcone):
+                if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+                    raise ValueError("need C-contiguous float32 numpy arrays")
+            rc = self.lib.mx_ConstructLightcone(self.ctx, snapshot, delta_T.ctypes.data, delta_T_prev.ctypes.data,
+                                                lightcone.ctypes.data, z.ctypes.data)
+        self._check(rc)

@@ -449,6 +449,16 @@ double hubble(const mx_params& p, float z)
 
 double drdz(const mx_params& p, float z) { return (1.0 + z) * k::C * dtdz(p, z); }
 
+// gettime, XRayHeatingFunctions.c:483-494: age of a flat universe at z (s)
+double gettime(const mx_params& p, double z)
+{
+  const double OMl = p.omega_lambda, OMm = p.omega_m;
+  const double x = std::sqrt(OMl / OMm) * std::pow(1 + z, -3.0 / 2.0);
+  const double term1 = std::log(x + std::sqrt(std::pow(x, 2) + 1));
+  const double const1 = 2 * std::sqrt(1 + OMm / OMl) / (3 * k::HUBBLE * p.hubble_h);
+  return term1 * const1;
+}
+
 // find_HII_bubbles.c:26-45
 double RtoM(const mx_params& p, const Derived& d, double R)
 {

@@ -97,6 +97,7 @@ struct Derived
 double dtdz(const mx_params& p, float z);
 double hubble(const mx_params& p, float z);
 double drdz(const mx_params& p, float z);
+double gettime(const mx_params& p, double z);
 double RtoM(const mx_params& p, const Derived& d, double R);
 double dicke(const mx_params& p, double z);
 double ddicke_dz(const mx_params& p, double z);

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "fft3d.cuh"
+#include "lightcone.cuh"
 #include "pecvel.cuh"
 #include "ps.cuh"
 #include "host_physics.h"
@@ -81,6 +82,12 @@ struct mx_ctx
   float2* d_work = nullptr;     // batch x C
   long long work_fields = 0;    // capacity in spectra
   float2** d_in_ptrs = nullptr; // device array of MAX_FIELDS pointers
+  // light cone (Initialise_ConstructLightcone / ConstructLightcone state)
+  long long lc_length = -1, lc_pos = 0;
+  int lc_end_snapshot = 0;
+  double* d_lc_times = nullptr;  // slice times of one snapshot
+  float* d_lc_scratch = nullptr; // host-pointer calls: D*D x max slices per snapshot
+  long long lc_max_slices = 0;
   double* d_ps_partials = nullptr; // RED_BLOCKS x 3 x PS_MAX_BINS
   double* d_ps_sums = nullptr;     // 3 x PS_MAX_BINS + 1
   double* h_ps_sums = nullptr;     // pinned copy
@@ -159,6 +166,8 @@ mx_ctx::~mx_ctx()
   cudaFree(d_unf);
   cudaFree(d_work);
   cudaFree(d_in_ptrs);
+  cudaFree(d_lc_times);
+  cudaFree(d_lc_scratch);
   cudaFree(d_ps_partials);
   cudaFree(d_ps_sums);
   cudaFreeHost(h_ps_sums);
@@ -1046,6 +1055,124 @@ static int run_power_spectrum(mx_ctx* c, const float* dT, float* ps_k, float* ps
 }
 
 // ======================================================================
+// Light cone (src/core/ConstructLightcone.c:12-166)
+// ======================================================================
+// Redshifts of the slices ConstructLightcone fills at `snapshot` (the
+// reference's walk from the light cone's low-redshift end in steps of one
+// comoving cell, dR / drdz, keeping those in [ZZ[snapshot], ZZ[snapshot-1])).
+static std::vector<double> lc_slices(const mx_ctx* c, int snapshot)
+{
+  const mx_params& p = c->p;
+  const double box_size = p.box_size / p.hubble_h;
+  const double dR = (box_size / (double)p.grid_dim) * k::MPC;
+  const double z2 = c->zz[snapshot - 1];
+  double z_LC = c->zz[c->lc_end_snapshot];
+  std::vector<double> zs;
+  while (z_LC < z2) {
+    if (z_LC >= c->zz[snapshot] && z_LC < c->zz[snapshot - 1])
+      zs.push_back(z_LC);
+    z_LC -= dR / drdz(p, (float)z_LC);
+  }
+  return zs;
+}
+
+// Initialise_ConstructLightcone (:12-67)
+static long long lightcone_init(mx_ctx* c, double end_redshift, int last_output_snap)
+{
+  const mx_params& p = c->p;
+  if (c->zz.empty())
+    throw CudaError{ MX_ESTATE, "mx_set_redshifts has not been called" };
+  if (last_output_snap < 0 || last_output_snap >= (int)c->zz.size())
+    throw CudaError{ MX_EINVAL, "last output snapshot out of range" };
+  const double box_size = p.box_size / p.hubble_h;
+  const double dR = (box_size / (double)p.grid_dim) * k::MPC;
+  const double start_redshift = c->zz[0];
+  int i = 0;
+  while (i < (int)c->zz.size() - 1 && c->zz[i] > end_redshift)
+    i++;
+  int closest = std::min(i, last_output_snap);
+  double z1 = c->zz[closest], z_LC = z1;
+  long long total = 0;
+  i = 0;
+  while (z1 < start_redshift) {
+    const double z2 = c->zz[closest - 1 - i];
+    while (z_LC < z2) {
+      total++;
+      z_LC -= dR / drdz(p, (float)z_LC);
+    }
+    z1 = z2;
+    i += 1;
+  }
+  c->lc_length = total;
+  c->lc_end_snapshot = closest;
+  c->lc_pos = total;
+  long long mx = 0;
+  for (int s = 1; s <= closest; s++)
+    mx = std::max<long long>(mx, (long long)lc_slices(c, s).size());
+  cudaFree(c->d_lc_times);
+  cudaFree(c->d_lc_scratch);
+  c->d_lc_times = nullptr;
+  c->d_lc_scratch = nullptr;
+  c->lc_max_slices = mx;
+  if (mx > 0) {
+    MX_CUDA(cudaMalloc(&c->d_lc_times, sizeof(double) * mx));
+    MX_CUDA(cudaMalloc(&c->d_lc_scratch, sizeof(float) * (size_t)c->gd.D * c->gd.D * (size_t)mx));
+  }
+  return total;
+}
+
+// ConstructLightcone (:69-166).  Device pointers; `out` is either the
+// caller's device light cone (pitch = length, written at the slice offset)
+// or the scratch (pitch = slices of this snapshot) when host_lc is given.
+static void construct_lightcone(mx_ctx* c, int snapshot, const float* dT, const float* dT_prev, float* dev_lc,
+                                float* host_lc, float* lc_z, cudaStream_t s)
+{
+  const GridDims& gd = c->gd;
+  if (c->lc_length < 0)
+    throw CudaError{ MX_ESTATE, "mx_lightcone_init has not been called" };
+  if (snapshot == 0) {
+    c->lc_pos = c->lc_length;
+    return;
+  }
+  const std::vector<double> zs = lc_slices(c, snapshot);
+  const long long n = (long long)zs.size();
+  c->lc_pos -= n;
+  if (n == 0)
+    return;
+  if (c->lc_pos < 0 || n > c->lc_max_slices)
+    throw CudaError{ MX_ESTATE, "light-cone snapshots called out of order" };
+  const long long slice0 = c->lc_pos;
+  std::vector<double> t(n);
+  for (long long i = 0; i < n; i++) {
+    t[i] = gettime(c->p, zs[i]);
+    lc_z[slice0 + i] = (float)zs[i];
+  }
+  MX_CUDA(cudaMemcpyAsync(c->d_lc_times, t.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  LightconeArgs a;
+  a.delta_T = dT;
+  a.delta_T_prev = dT_prev;
+  a.t_slice = c->d_lc_times;
+  a.n = (int)n;
+  a.iz0 = (int)(slice0 % gd.D);
+  a.t1 = gettime(c->p, c->zz[snapshot]);
+  a.t2 = gettime(c->p, c->zz[snapshot - 1]);
+  if (host_lc) {
+    a.out = c->d_lc_scratch;
+    a.pitch = n;
+  } else {
+    a.out = dev_lc + slice0;
+    a.pitch = c->lc_length;
+  }
+  {
+    Prof pr(c, "k_lightcone", 12.0 * (double)gd.D * gd.D * n, s);
+    launch_lightcone(a, gd, s);
+  }
+  if (host_lc)
+    MX_CUDA(cudaMemcpy2DAsync(host_lc + slice0, sizeof(float) * c->lc_length, c->d_lc_scratch, sizeof(float) * n,
+                              sizeof(float) * n, (size_t)gd.D * gd.D, cudaMemcpyDeviceToHost, s));
+}
+
+// ======================================================================
 // C ABI
 // ======================================================================
 template <class F>
@@ -1100,6 +1227,54 @@ static cudaStream_t pick(mx_ctx* c, void* stream) { return stream ? (cudaStream_
 extern "C" {
 
 const char* mx_build_info(void) { return "meraxes_gb300 reion step, sm_103a, abi 1"; }
+
+int64_t mx_lightcone_init(mx_ctx* ctx, double end_redshift, int32_t last_output_snap, int32_t* end_snapshot)
+{
+  long long n = 0;
+  const int rc = guarded(ctx, [&]() {
+    n = lightcone_init(ctx, end_redshift, last_output_snap);
+    if (end_snapshot)
+      *end_snapshot = ctx->lc_end_snapshot;
+  });
+  return rc == MX_OK ? (int64_t)n : (int64_t)rc;
+}
+
+int mx_ConstructLightcone(mx_ctx* ctx, int32_t snapshot, const float* delta_T, float* delta_T_prev, float* lightcone,
+                          float* lightcone_redshifts)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!delta_T || !delta_T_prev || !lightcone || !lightcone_redshifts)
+      throw CudaError{ MX_EINVAL, "ConstructLightcone: NULL pointer" };
+    cudaStream_t s = ctx->stream;
+    const size_t bytes = sizeof(float) * ctx->gd.N;
+    if (snapshot > 0) {
+      // the two co-eval boxes go to unfiltered-spectrum scratch (slots 0, 1)
+      float* d0 = reinterpret_cast<float*>(ctx->d_unf);
+      float* d1 = reinterpret_cast<float*>(ctx->d_unf + ctx->gd.C);
+      MX_CUDA(cudaMemcpyAsync(d0, delta_T, bytes, cudaMemcpyHostToDevice, s));
+      MX_CUDA(cudaMemcpyAsync(d1, delta_T_prev, bytes, cudaMemcpyHostToDevice, s));
+      construct_lightcone(ctx, snapshot, d0, d1, nullptr, lightcone, lightcone_redshifts, s);
+      MX_CUDA(cudaStreamSynchronize(s));
+    } else {
+      construct_lightcone(ctx, snapshot, nullptr, nullptr, nullptr, lightcone, lightcone_redshifts, s);
+    }
+    std::memcpy(delta_T_prev, delta_T, bytes);
+  });
+}
+
+int mx_ConstructLightcone_device(mx_ctx* ctx, int32_t snapshot, const float* delta_T, float* delta_T_prev,
+                                 float* lightcone, float* lightcone_redshifts, void* stream)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    if (!delta_T || !delta_T_prev || !lightcone || !lightcone_redshifts)
+      throw CudaError{ MX_EINVAL, "ConstructLightcone: NULL pointer" };
+    cudaStream_t s = pick(ctx, stream);
+    construct_lightcone(ctx, snapshot, delta_T, delta_T_prev, lightcone, nullptr, lightcone_redshifts, s);
+    MX_CUDA(cudaMemcpyAsync(delta_T_prev, delta_T, sizeof(float) * ctx->gd.N, cudaMemcpyDeviceToDevice, s));
+  });
+}
 
 int32_t mx_ps_length(const mx_ctx* ctx)
 {

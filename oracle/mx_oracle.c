@@ -69,6 +69,8 @@ struct mxo_ctx
 {
   mx_params p;
   float* last_vel_grad; /* dv/dx of the last peculiar-velocity delta_T (padded), for tests */
+  long long lc_length, lc_pos; /* LightconeLength, CurrentLCPos */
+  int lc_end_snapshot;         /* EndSnapshotLightcone */
   double unit_time_s, G, hubble_int, rho_crit;
   double no, he_no, f_h, f_he, n_b0;
   double* zz;
@@ -1949,3 +1951,92 @@ int mxo_power_spectrum(int D, double box_size_mpc_h, double hubble_h, const floa
 }
 
 const float* mxo_last_velocity_gradient(const mxo_ctx* c) { return c->last_vel_grad; }
+
+/* ------------------------------------------------------------------------
+ * Light cone: Initialise_ConstructLightcone (ConstructLightcone.c:12-67) and
+ * ConstructLightcone (:69-166), single rank.
+ * ---------------------------------------------------------------------- */
+/* gettime, XRayHeatingFunctions.c:483-494 (zero curvature, Weinberg 1989) */
+static double c_gettime(const mxo_ctx* c, double z)
+{
+  const double OMl = c->p.omega_lambda, OMm = c->p.omega_m;
+  const double x = sqrt(OMl / OMm) * pow(1 + z, -3.0 / 2.0);
+  const double term1 = log(x + sqrt(pow(x, 2) + 1));
+  const double const1 = 2 * sqrt(1 + OMm / OMl) / (3 * K_HUBBLE * c->p.hubble_h);
+  return term1 * const1;
+}
+
+long long mxo_lightcone_init(mxo_ctx* c, double end_redshift, int last_output_snap, int* end_snapshot)
+{
+  const double box_size = c->p.box_size / c->p.hubble_h;
+  const double dR = (box_size / (double)c->p.grid_dim) * MXO_MPC;
+  const double start_redshift = c->zz[0];
+  int i = 0;
+  while (c->zz[i] > end_redshift)
+    i++;
+  int closest = i;
+  if (closest > last_output_snap)
+    closest = last_output_snap;
+  double z1 = c->zz[closest], z_LC = z1;
+  long long total = 0;
+  i = 0;
+  while (z1 < start_redshift) {
+    const double z2 = c->zz[closest - 1 - i];
+    while (z_LC < z2) {
+      total++;
+      z_LC -= dR / c_drdz(c, (float)z_LC);
+    }
+    z1 = z2;
+    i += 1;
+  }
+  c->lc_length = total;
+  c->lc_end_snapshot = closest;
+  if (end_snapshot)
+    *end_snapshot = closest;
+  return total;
+}
+
+int mxo_construct_lightcone(mxo_ctx* c, int snapshot, const float* delta_T, float* delta_T_prev, float* lightcone,
+                            float* lightcone_redshifts)
+{
+  const int D = c->p.grid_dim;
+  const double box_size = c->p.box_size / c->p.hubble_h;
+  const double dR = (box_size / (double)D) * MXO_MPC;
+  if (snapshot > 0) {
+    const double z2_LC = c->zz[snapshot - 1], t_z2 = c_gettime(c, z2_LC);
+    const double z1_LC = c->zz[snapshot], t_z1 = c_gettime(c, z1_LC);
+    double z_LC = c->zz[c->lc_end_snapshot];
+    long long n_snap = 0;
+    while (z_LC < z2_LC) {
+      if (z_LC >= c->zz[snapshot] && z_LC < c->zz[snapshot - 1])
+        n_snap++;
+      z_LC -= dR / c_drdz(c, (float)z_LC);
+    }
+    z_LC = c->zz[c->lc_end_snapshot];
+    c->lc_pos -= n_snap;
+    long long slice_ct = c->lc_pos;
+    int iz = (int)(slice_ct % D);
+    while (z_LC < z2_LC) {
+      if (z_LC >= c->zz[snapshot] && z_LC < c->zz[snapshot - 1]) {
+        const double t_slice = c_gettime(c, z_LC);
+        lightcone_redshifts[slice_ct] = (float)z_LC;
+        if (iz >= D)
+          iz = 0;
+        for (int ii = 0; ii < D; ii++)
+          for (int jj = 0; jj < D; jj++) {
+            const size_t i_lc = (size_t)slice_ct + (size_t)c->lc_length * ((size_t)jj + (size_t)D * ii);
+            const size_t ir = real_idx(D, ii, jj, iz);
+            const double fz1 = delta_T[ir], fz2 = delta_T_prev[ir];
+            lightcone[i_lc] = (float)((fz2 - fz1) / (t_z2 - t_z1) * (t_slice - t_z1) + fz1);
+          }
+        iz++;
+        slice_ct++;
+      }
+      z_LC -= dR / c_drdz(c, (float)z_LC);
+    }
+  } else {
+    c->lc_pos = c->lc_length;
+  }
+  memcpy(delta_T_prev, delta_T, sizeof(float) * (size_t)D * D * D);
+  return 0;
+}

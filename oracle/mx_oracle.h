@@ -37,6 +37,10 @@ int mxo_delta_T(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out);
  * (decides r_bubble, which is overwritten at each ionising radius).  A cell
  * whose outputs can legitimately differ between two FP32 FFT implementations
  * has a small margin.  NULL before a call. */
+/* Light cone (ConstructLightcone.c:12-166): returns LightconeLength. */
+long long mxo_lightcone_init(mxo_ctx* c, double end_redshift, int last_output_snap, int* end_snapshot);
+int mxo_construct_lightcone(mxo_ctx* c, int snapshot, const float* delta_T, float* delta_T_prev, float* lightcone,
+                            float* lightcone_redshifts);
 /* 21 cm power spectrum of a REAL delta_T grid (Initialise_PowerSpectrum and
  * Compute_PS, ComputePowerSpectrum.c:18-255); box_size in Mpc/h.  Returns the
  * number of k bins, or -1 if it exceeds cap. */

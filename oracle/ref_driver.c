@@ -23,6 +23,7 @@
 #include "find_HII_bubbles.h"
 #include "recombinations.h"
 #include "ComputePowerSpectrum.h"
+#include "ConstructLightcone.h"
 #include "reionization.h"
 #include "utils.h"
 
@@ -189,4 +190,38 @@ int mxref_power_spectrum(const float* delta_T, float* ps_k, float* ps_data, floa
   Compute_PS(0);
   g->PS_k = g->PS_data = g->PS_error = NULL;
   return nb;
+}
+
+/* Initialise_ConstructLightcone with EndRedshiftLightcone and LastOutputSnap;
+ * allocates delta_T_prev, LightconeBox and Lightcone_redshifts. */
+long long mxref_lightcone_init(double end_redshift, int last_output_snap, int* end_snapshot)
+{
+  reion_grids_t* g = &run_globals.reion_grids;
+  const int D = run_globals.params.ReionGridDim;
+  run_globals.params.EndRedshiftLightcone = end_redshift;
+  run_globals.LastOutputSnap = last_output_snap;
+  Initialise_ConstructLightcone();
+  const long long n = run_globals.params.LightconeLength;
+  free(g->LightconeBox);
+  free(g->Lightcone_redshifts);
+  if (!g->delta_T_prev)
+    g->delta_T_prev = (float*)calloc((size_t)D * D * D, sizeof(float));
+  g->LightconeBox = (float*)calloc((size_t)D * D * (size_t)n, sizeof(float));
+  g->Lightcone_redshifts = (float*)calloc((size_t)n, sizeof(float));
+  *end_snapshot = run_globals.params.EndSnapshotLightcone;
+  return n;
+}
+
+int mxref_construct_lightcone(int snapshot, const float* delta_T, float* delta_T_prev, float* lightcone, float* lc_z)
+{
+  reion_grids_t* g = &run_globals.reion_grids;
+  const int D = run_globals.params.ReionGridDim;
+  const long long n = run_globals.params.LightconeLength;
+  memcpy(g->delta_T, delta_T, sizeof(float) * (size_t)D * D * D);
+  memcpy(g->delta_T_prev, delta_T_prev, sizeof(float) * (size_t)D * D * D);
+  ConstructLightcone(snapshot);
+  memcpy(delta_T_prev, g->delta_T_prev, sizeof(float) * (size_t)D * D * D);
+  memcpy(lightcone, g->LightconeBox, sizeof(float) * (size_t)D * D * (size_t)n);
+  memcpy(lc_z, g->Lightcone_redshifts, sizeof(float) * (size_t)n);
+  return 0;
 }

@@ -66,6 +66,9 @@ class OracleBackend:
         L.mxo_get_Ts.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                  ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
         L.mxo_get_Ts.restype = ctypes.c_double
+        L.mxo_lightcone_init.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.mxo_lightcone_init.restype = ctypes.c_longlong
+        L.mxo_construct_lightcone.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 4
         L.mxo_last_velocity_gradient.argtypes = [ctypes.c_void_p]
         L.mxo_last_velocity_gradient.restype = ctypes.POINTER(ctypes.c_float)
         L.mxo_power_spectrum.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
@@ -117,6 +120,18 @@ class OracleBackend:
 
     def delta_T(self, snapshot: int, state) -> Dict[str, float]:
         return self._call("mxo_delta_T", snapshot, state)
+
+    def lightcone_init(self, end_redshift: float, last_output_snap: int):
+        """Initialise_ConstructLightcone: (LightconeLength, EndSnapshotLightcone)."""
+        e = ctypes.c_int()
+        n = self.lib.mxo_lightcone_init(self.ctx, end_redshift, last_output_snap, ctypes.byref(e))
+        return int(n), e.value
+
+    def construct_lightcone(self, snapshot: int, delta_T, delta_T_prev, lightcone, lightcone_z):
+        """ConstructLightcone, in place on delta_T_prev, lightcone and lightcone_z."""
+        rc = self.lib.mxo_construct_lightcone(self.ctx, snapshot, _ptr(delta_T), _ptr(delta_T_prev), _ptr(lightcone),
+                                              _ptr(lightcone_z))
+        assert rc == 0
 
     def velocity_gradient(self) -> Optional[np.ndarray]:
         """dv/dx (REAL layout) of the last delta_T with peculiar velocities."""
@@ -181,6 +196,9 @@ class RefBackend:
         L.mxref_splined_recombination_rate.argtypes = [ctypes.c_double, ctypes.c_double]
         L.mxref_splined_recombination_rate.restype = ctypes.c_double
         L.mxref_power_spectrum.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int]
+        L.mxref_lightcone_init.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.mxref_lightcone_init.restype = ctypes.c_longlong
+        L.mxref_construct_lightcone.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 4
         self.params = params
         self._pc = params.to_ctypes()
         zz = (ctypes.c_double * len(redshifts))(*redshifts)
@@ -221,6 +239,15 @@ class RefBackend:
 
     def find_HII_bubbles(self, snapshot, state):
         return self._run("mxref_find_HII_bubbles", snapshot, state)
+
+    def lightcone_init(self, end_redshift: float, last_output_snap: int):
+        e = ctypes.c_int()
+        n = self.lib.mxref_lightcone_init(end_redshift, last_output_snap, ctypes.byref(e))
+        return int(n), e.value
+
+    def construct_lightcone(self, snapshot: int, delta_T, delta_T_prev, lightcone, lightcone_z):
+        self.lib.mxref_construct_lightcone(snapshot, _ptr(delta_T), _ptr(delta_T_prev), _ptr(lightcone),
+                                           _ptr(lightcone_z))
 
     def power_spectrum(self, delta_T: np.ndarray):
         out = [np.zeros(64, np.float32) for _ in range(3)]

@@ -9,6 +9,7 @@ grids and the per-snapshot global scalars.
     python tests/golden/make_golden.py            # all cases
     python tests/golden/make_golden.py full24     # one case
     python tests/golden/make_golden.py ps         # power spectrum fixture
+    python tests/golden/make_golden.py lightcone  # light-cone fixture
 
 Each case runs in a fresh process because the reference keeps its state in
 globals.
@@ -77,11 +78,46 @@ def make_ps(name: str = "plain32_tophat"):
     print(f"ps_{name} written")
 
 
+LC_ZZ = [12.0 - 4.0 * i / 9 for i in range(10)]
+
+
+def lightcone_inputs(D: int = 16):
+    """Seeded delta_T boxes of the light-cone fixture, one per snapshot."""
+    import numpy as np
+
+    rng = np.random.default_rng(3)
+    return [rng.normal(10, 3, (D, D, D)).astype(np.float32) for _ in LC_ZZ]
+
+
+def make_lightcone(D: int = 16, L: float = 64.0, end_z: float = 8.6):
+    """ConstructLightcone of the reference over the 10-snapshot list LC_ZZ."""
+    import numpy as np
+
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.params import ReionParams
+    from oracle import RefBackend
+
+    p = ReionParams(grid_dim=D, box_size=L, flag_21cm=1)
+    ref = RefBackend(p, LC_ZZ, syn.TABLES_DIR)
+    n, end = ref.lightcone_init(end_z, len(LC_ZZ) - 1)
+    prev = np.zeros((D, D, D), np.float32)
+    lc = np.zeros((D, D, n), np.float32)
+    lz = np.zeros(n, np.float32)
+    for s, dT in enumerate(lightcone_inputs(D)):
+        ref.construct_lightcone(s, dT, prev, lc, lz)
+    np.savez_compressed(os.path.join(HERE, "lightcone16.npz"), lightcone=lc, redshifts=lz, delta_T_prev=prev,
+                        length=n, end_snapshot=end, box_size=L, end_redshift=end_z)
+    print("lightcone16 written")
+
+
 if __name__ == "__main__":
     from cases import CASES
 
     if sys.argv[1:2] == ["ps"]:
         make_ps()
+        sys.exit(0)
+    if sys.argv[1:2] == ["lightcone"]:
+        make_lightcone()
         sys.exit(0)
     names = sys.argv[1:] or list(CASES)
     if len(names) == 1:

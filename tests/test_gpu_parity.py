@@ -212,3 +212,46 @@ def test_gpu_power_spectrum_matches_oracle(D, L, tables_dir):
     ref = OracleBackend(p, [8.5, 8.0], tables_dir).power_spectrum(dT)
     got = ReionGridStep(p, [8.5, 8.0]).Compute_PS(dT)
     _ps_close(ref, got)
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_gpu_lightcone_matches_reference_fixture_and_oracle(device, tables_dir):
+    """Light cone through the C ABI, host and device families: equal to the
+    oracle run on this machine (same double arithmetic and host times), and to
+    the reference fixture within one float rounding (its host times were made
+    with another machine's libm)."""
+    import sys
+
+    import torch
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_golden import LC_ZZ, lightcone_inputs
+
+    from meraxes_gb300.api import ReionGridStep
+    from meraxes_gb300.params import ReionParams
+    from oracle import OracleBackend
+
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "lightcone16.npz"))
+    p = ReionParams(grid_dim=16, box_size=float(d["box_size"]), flag_21cm=1)
+    runs = []
+    for backend in ("oracle", "gpu"):
+        b = OracleBackend(p, LC_ZZ, tables_dir) if backend == "oracle" else ReionGridStep(p, LC_ZZ)
+        n, end = b.lightcone_init(float(d["end_redshift"]), len(LC_ZZ) - 1)
+        assert (n, end) == (int(d["length"]), int(d["end_snapshot"]))
+        prev = np.zeros((16, 16, 16), np.float32)
+        lc = np.zeros((16, 16, n), np.float32)
+        lz = np.zeros(n, np.float32)
+        if backend == "gpu" and device:
+            prev_t, lc_t = torch.from_numpy(prev).cuda(), torch.from_numpy(lc).cuda()
+            for s, dT in enumerate(lightcone_inputs(16)):
+                b.ConstructLightcone(s, torch.from_numpy(dT).cuda(), prev_t, lc_t, lz)
+            torch.cuda.synchronize()
+            prev, lc = prev_t.cpu().numpy(), lc_t.cpu().numpy()
+        else:
+            for s, dT in enumerate(lightcone_inputs(16)):
+                (b.construct_lightcone if backend == "oracle" else b.ConstructLightcone)(s, dT, prev, lc, lz)
+        runs.append((lc, lz, prev))
+    (lo, zo, po), (lg, zg, pg) = runs
+    assert np.array_equal(lg, lo) and np.array_equal(zg, zo) and np.array_equal(pg, po)
+    np.testing.assert_allclose(lg, d["lightcone"], rtol=2 ** -23, atol=0)
+    np.testing.assert_allclose(zg, d["redshifts"], rtol=2 ** -23, atol=0)

@@ -84,3 +84,27 @@ def test_oracle_power_spectrum_matches_reference_fixture():
     assert np.array_equal(k, d["k"], equal_nan=True)
     assert np.array_equal(P, d["P"], equal_nan=True)
     assert np.array_equal(err, d["error"], equal_nan=True)
+
+
+def test_oracle_lightcone_matches_reference_fixture():
+    """ConstructLightcone restated == the reference's, over 10 snapshots."""
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_golden import LC_ZZ, lightcone_inputs
+
+    from meraxes_gb300.params import ReionParams
+
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "lightcone16.npz"))
+    p = ReionParams(grid_dim=16, box_size=float(d["box_size"]), flag_21cm=1)
+    orc = OracleBackend(p, LC_ZZ, syn.TABLES_DIR)
+    n, end = orc.lightcone_init(float(d["end_redshift"]), len(LC_ZZ) - 1)
+    assert (n, end) == (int(d["length"]), int(d["end_snapshot"]))
+    prev = np.zeros((16, 16, 16), np.float32)
+    lc = np.zeros((16, 16, n), np.float32)
+    lz = np.zeros(n, np.float32)
+    for s, dT in enumerate(lightcone_inputs(16)):
+        orc.construct_lightcone(s, dT, prev, lc, lz)
+    assert np.array_equal(lc, d["lightcone"]) and np.array_equal(lz, d["redshifts"])
+    assert np.array_equal(prev, d["delta_T_prev"])

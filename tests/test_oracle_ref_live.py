@@ -75,3 +75,38 @@ def test_power_spectrum_restatement_bit_exact_against_reference(D, L):
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip().startswith("OK"), r.stdout
+
+
+LC_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r}); sys.path.insert(0, {tests!r})
+from meraxes_gb300.params import ReionParams
+from meraxes_gb300 import synthetic as syn
+from oracle import OracleBackend, RefBackend
+D = {D}
+p = ReionParams(grid_dim=D, box_size={L}, flag_21cm=1)
+zz = [12.0 - 4.0 * i / 9 for i in range(10)]
+out = []
+for B in (RefBackend, OracleBackend):
+    b = B(p, zz, syn.TABLES_DIR)
+    n, end = b.lightcone_init(8.6, len(zz) - 1)
+    prev = np.zeros((D, D, D), np.float32)
+    lc = np.zeros((D, D, n), np.float32); lz = np.zeros(n, np.float32)
+    rng = np.random.default_rng(3)
+    for s in range(len(zz)):
+        dT = rng.normal(10, 3, (D, D, D)).astype(np.float32)
+        b.construct_lightcone(s, dT, prev, lc, lz)
+    out.append((n, end, lc, lz, prev))
+a, c = out
+ok = a[0] == c[0] and a[1] == c[1] and all(np.array_equal(x, y) for x, y in zip(a[2:], c[2:]))
+print('OK' if ok else 'MISMATCH', a[0], a[1], c[0], c[1])
+"""
+
+
+@pytest.mark.parametrize("D,L", [(16, 64.0), (20, 200.0)])
+def test_lightcone_restatement_bit_exact_against_reference(D, L):
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = LC_SCRIPT.format(root=os.path.dirname(here), tests=here, D=D, L=L)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip().startswith("OK"), r.stdout
