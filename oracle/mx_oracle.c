@@ -2040,3 +2040,110 @@ int mxo_construct_lightcone(mxo_ctx* c, int snapshot, const float* delta_T, floa
   memcpy(delta_T_prev, delta_T, sizeof(float) * (size_t)D * D * D);
   return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * Galaxy -> grid deposit: construct_baryon_grids (reionization.c:1353-1615),
+ * single rank, no mini-haloes; and the grid -> galaxy feedback mass
+ * calculate_Mvir_crit (physics/reionization.c:10-59).
+ * ---------------------------------------------------------------------- */
+/* pos_to_ngp, misc_tools.c:163-173; -1 for a negative index */
+static int ngp(double x, double side, int nx)
+{
+  int ind = (int)nearbyint(x / side * (double)nx);
+  if (ind > nx - 1)
+    ind = 0;
+  return ind > -1 ? ind : -1;
+}
+
+/* hubble_time, virial_properties.c:79-93 (internal time units) */
+static double c_hubble_time(const mxo_ctx* c, int snapshot)
+{
+  const double zplus1 = c->zz[snapshot] + 1;
+  return 1.0 / (c->hubble_int * sqrt(c->p.omega_m * zplus1 * zplus1 * zplus1 + c->p.omega_k * zplus1 * zplus1 +
+                                     c->p.omega_lambda));
+}
+
+int mxo_construct_baryon_grids(mxo_ctx* c, int snapshot, int n, const float* pos, const int* type, const double* fesc_gsm,
+                               const double* gross_sm, const double* bhm, const double* ebhm, int flag_bh,
+                               double bh_limit, double alpha_uv_bh, const mx_grids* g)
+{
+  const mx_params* p = &c->p;
+  const int D = p->grid_dim, H = D / 2 + 1;
+  const size_t np = (size_t)D * D * 2 * H, nr = (size_t)D * D * D;
+  const double box_size = p->box_size;
+  const double sfr_timescale = p->reion_sfr_timescale * c_hubble_time(c, snapshot);
+  /* :1375-1397 */
+  memset(g->stars, 0, sizeof(float) * np);
+  memset(g->weighted_sfr, 0, sizeof(float) * np);
+  if (p->flag_spin_temp) {
+    memset(g->sfr, 0, sizeof(float) * np);
+    for (int snap = c->n_hist - 2; snap >= 0; snap--)
+      memcpy(g->sfr_histories + (size_t)(snap + 1) * np, g->sfr_histories + (size_t)snap * np, sizeof(float) * np);
+  }
+  float* buffer = (float*)malloc(sizeof(float) * nr);
+  int rc = 0;
+  for (int prop = 0; prop < 3; prop++) { /* stellar, weighted_sfr, sfr */
+    if (!p->flag_spin_temp && prop == 2)
+      continue;
+    memset(buffer, 0, sizeof(float) * nr);
+    for (int i = 0; i < n; i++) {
+      if (type[i] > 2)
+        continue;
+      const int ix = ngp(pos[3 * i], box_size, D), iy = ngp(pos[3 * i + 1], box_size, D),
+                iz = ngp(pos[3 * i + 2], box_size, D);
+      if (ix < 0 || iy < 0 || iz < 0) {
+        rc = MX_EINVAL;
+        continue;
+      }
+      const size_t ind = real_idx(D, ix, iy, iz);
+      if (prop == 0) {
+        buffer[ind] += fesc_gsm[i];
+        if (flag_bh && bhm[i] >= bh_limit)
+          buffer[ind] += ebhm[i];
+      } else if (prop == 1) {
+        buffer[ind] += (fesc_gsm[i]);
+        if (flag_bh && bhm[i] >= bh_limit)
+          buffer[ind] += ebhm[i] * alpha_uv_bh / p->alpha_uv;
+      } else {
+        buffer[ind] += gross_sm[i];
+      }
+    }
+    for (int ix = 0; ix < D; ix++)
+      for (int iy = 0; iy < D; iy++)
+        for (int iz = 0; iz < D; iz++) {
+          const size_t ir = real_idx(D, ix, iy, iz), ip = pad_idx(D, ix, iy, iz);
+          if (prop == 0) {
+            float val = buffer[ir];
+            if (val < 0)
+              val = 0;
+            g->stars[ip] = val;
+          } else {
+            double val = (double)buffer[ir];
+            val = (val > 0) ? val / sfr_timescale : 0;
+            if (prop == 1) {
+              g->weighted_sfr[ip] = (float)val;
+            } else {
+              g->sfr[ip] = (float)val;
+              g->sfr_histories[ip] = (float)val;
+            }
+          }
+        }
+  }
+  free(buffer);
+  return rc;
+}
+
+int mxo_calculate_Mvir_crit(mxo_ctx* c, double redshift, double m0, double a, double b, double cc, double d,
+                            const float* J_21_at_ion, const float* z_at_ion, float* Mvir_crit)
+{
+  const int D = c->p.grid_dim;
+  const double Hubble_h = c->p.hubble_h;
+  for (size_t i = 0; i < (size_t)D * D * D; i++) {
+    double cell = 0.0;
+    if (z_at_ion[i] > redshift)
+      cell = m0 * pow((double)(J_21_at_ion[i]) * Hubble_h * Hubble_h, a) * pow((1.0 + redshift) / 10.0, b) *
+             pow((1.0 - pow((1.0 + redshift) / (1.0 + (double)(z_at_ion[i])), cc)), d);
+    Mvir_crit[i] = (float)cell;
+  }
+  return 0;
+}

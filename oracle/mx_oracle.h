@@ -37,6 +37,13 @@ int mxo_delta_T(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out);
  * (decides r_bubble, which is overwritten at each ionising radius).  A cell
  * whose outputs can legitimately differ between two FP32 FFT implementations
  * has a small margin.  NULL before a call. */
+/* construct_baryon_grids (reionization.c:1353-1615) on galaxy arrays, and
+ * calculate_Mvir_crit (physics/reionization.c:10-59). */
+int mxo_construct_baryon_grids(mxo_ctx* c, int snapshot, int n, const float* pos, const int* type, const double* fesc_gsm,
+                               const double* gross_sm, const double* bhm, const double* ebhm, int flag_bh,
+                               double bh_limit, double alpha_uv_bh, const mx_grids* g);
+int mxo_calculate_Mvir_crit(mxo_ctx* c, double redshift, double m0, double a, double b, double cc, double d,
+                            const float* J_21_at_ion, const float* z_at_ion, float* Mvir_crit);
 /* Light cone (ConstructLightcone.c:12-166): returns LightconeLength. */
 long long mxo_lightcone_init(mxo_ctx* c, double end_redshift, int last_output_snap, int* end_snapshot);
 int mxo_construct_lightcone(mxo_ctx* c, int snapshot, const float* delta_T, float* delta_T_prev, float* lightcone,

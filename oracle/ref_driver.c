@@ -24,6 +24,7 @@
 #include "recombinations.h"
 #include "ComputePowerSpectrum.h"
 #include "ConstructLightcone.h"
+#include "physics/reionization.h"
 #include "reionization.h"
 #include "utils.h"
 
@@ -223,5 +224,70 @@ int mxref_construct_lightcone(int snapshot, const float* delta_T, float* delta_T
   memcpy(delta_T_prev, g->delta_T_prev, sizeof(float) * (size_t)D * D * D);
   memcpy(lightcone, g->LightconeBox, sizeof(float) * (size_t)D * D * (size_t)n);
   memcpy(lc_z, g->Lightcone_redshifts, sizeof(float) * (size_t)n);
+  return 0;
+}
+
+/* construct_baryon_grids (reionization.c:1353-1615) on a galaxy list given
+ * as arrays (Pos, Type, FescWeightedGSM, GrossStellarMass, BlackHoleMass,
+ * EffectiveBHM; the last two may be NULL when flag_bh is 0). */
+int mxref_construct_baryon_grids(int snapshot, int n, const float* pos, const int* type, const double* fesc_gsm,
+                                 const double* gross_sm, const double* bhm, const double* ebhm, int flag_bh,
+                                 double bh_limit, double alpha_uv_bh)
+{
+  reion_grids_t* g = &run_globals.reion_grids;
+  const int D = run_globals.params.ReionGridDim;
+  physics_params_t* ph = &run_globals.params.physics;
+  ph->Flag_BHFeedback = flag_bh;
+  ph->BlackHoleMassLimitReion = bh_limit;
+  ph->ReionAlphaUVBH = alpha_uv_bh;
+  galaxy_t* gals = (galaxy_t*)calloc((size_t)(n > 0 ? n : 1), sizeof(galaxy_t));
+  gal_to_slab_t* map = (gal_to_slab_t*)calloc((size_t)(n > 0 ? n : 1), sizeof(gal_to_slab_t));
+  int live = 0;
+  for (int i = 0; i < n; i++) {
+    for (int k = 0; k < 3; k++)
+      gals[i].Pos[k] = pos[3 * i + k];
+    gals[i].Type = type[i];
+    gals[i].FescWeightedGSM = fesc_gsm[i];
+    gals[i].GrossStellarMass = gross_sm[i];
+    gals[i].BlackHoleMass = bhm ? bhm[i] : 0.0;
+    gals[i].EffectiveBHM = ebhm ? ebhm[i] : 0.0;
+    map[i].index = i;
+    map[i].galaxy = &gals[i];
+    map[i].slab_ind = 0;
+    if (type[i] <= 2)
+      live++;
+  }
+  g->galaxy_to_slab_map = map;
+  g->buffer_size = (int)((size_t)D * D * D);
+  float* buf = (float*)calloc((size_t)D * D * D, sizeof(float));
+  g->buffer = buf;
+  construct_baryon_grids(snapshot, live);
+  g->buffer = NULL;
+  g->galaxy_to_slab_map = NULL;
+  free(buf);
+  free(map);
+  free(gals);
+  return 0;
+}
+
+/* calculate_Mvir_crit (physics/reionization.c:10-59) on given grids */
+int mxref_calculate_Mvir_crit(double redshift, double m0, double a, double b, double c, double d,
+                              const float* J_21_at_ion, const float* z_at_ion, float* out)
+{
+  reion_grids_t* g = &run_globals.reion_grids;
+  const int D = run_globals.params.ReionGridDim;
+  physics_params_t* ph = &run_globals.params.physics;
+  ph->ReionSMParam_m0 = m0;
+  ph->ReionSMParam_a = a;
+  ph->ReionSMParam_b = b;
+  ph->ReionSMParam_c = c;
+  ph->ReionSMParam_d = d;
+  const size_t n = (size_t)D * D * D;
+  if (!g->Mvir_crit)
+    g->Mvir_crit = (float*)calloc(n, sizeof(float));
+  memcpy(g->J_21_at_ionization, J_21_at_ion, sizeof(float) * n);
+  memcpy(g->z_at_ionization, z_at_ion, sizeof(float) * n);
+  calculate_Mvir_crit(redshift);
+  memcpy(out, g->Mvir_crit, sizeof(float) * n);
   return 0;
 }

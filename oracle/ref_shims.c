@@ -220,5 +220,4 @@ static void mxs_unreachable(const char* what)
 void cleanup(void) { mxs_unreachable("cleanup"); }
 void cn_quote(void) {}
 void mpi_debug_here(void) { mxs_unreachable("mpi_debug_here"); }
-double hubble_time(int snapshot) { (void)snapshot; mxs_unreachable("hubble_time"); return 0; }
 void read_grid(int property, int snapshot, float* slab) { (void)property; (void)snapshot; (void)slab; mxs_unreachable("read_grid"); }

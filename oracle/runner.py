@@ -66,6 +66,9 @@ class OracleBackend:
         L.mxo_get_Ts.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                  ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
         L.mxo_get_Ts.restype = ctypes.c_double
+        L.mxo_construct_baryon_grids.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6 + \
+            [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+        L.mxo_calculate_Mvir_crit.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 6 + [ctypes.c_void_p] * 3
         L.mxo_lightcone_init.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
         L.mxo_lightcone_init.restype = ctypes.c_longlong
         L.mxo_construct_lightcone.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 4
@@ -120,6 +123,23 @@ class OracleBackend:
 
     def delta_T(self, snapshot: int, state) -> Dict[str, float]:
         return self._call("mxo_delta_T", snapshot, state)
+
+    def construct_baryon_grids(self, snapshot: int, gals: Dict[str, np.ndarray], state, bh=(0, 0.0, 0.0)):
+        """construct_baryon_grids on galaxy arrays (pos [n,3] float32, type int32,
+        fesc_gsm / gross_sm / bhm / ebhm float64); writes stars, weighted_sfr,
+        sfr and sfr_histories of `state` in place."""
+        n = len(gals["type"])
+        g = self._grids(state)
+        rc = self.lib.mxo_construct_baryon_grids(
+            self.ctx, snapshot, n, _ptr(gals["pos"]), _ptr(gals["type"]), _ptr(gals["fesc_gsm"]),
+            _ptr(gals["gross_sm"]), _ptr(gals.get("bhm")), _ptr(gals.get("ebhm")), bh[0], bh[1], bh[2],
+            ctypes.byref(g))
+        assert rc == 0, rc
+
+    def calculate_Mvir_crit(self, redshift: float, sm, J_21_at_ion, z_at_ion) -> np.ndarray:
+        out = np.zeros_like(J_21_at_ion, dtype=np.float32)
+        self.lib.mxo_calculate_Mvir_crit(self.ctx, redshift, *sm, _ptr(J_21_at_ion), _ptr(z_at_ion), _ptr(out))
+        return out
 
     def lightcone_init(self, end_redshift: float, last_output_snap: int):
         """Initialise_ConstructLightcone: (LightconeLength, EndSnapshotLightcone)."""
@@ -196,6 +216,9 @@ class RefBackend:
         L.mxref_splined_recombination_rate.argtypes = [ctypes.c_double, ctypes.c_double]
         L.mxref_splined_recombination_rate.restype = ctypes.c_double
         L.mxref_power_spectrum.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int]
+        L.mxref_construct_baryon_grids.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6 + \
+            [ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.mxref_calculate_Mvir_crit.argtypes = [ctypes.c_double] * 6 + [ctypes.c_void_p] * 3
         L.mxref_lightcone_init.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
         L.mxref_lightcone_init.restype = ctypes.c_longlong
         L.mxref_construct_lightcone.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 4
@@ -239,6 +262,18 @@ class RefBackend:
 
     def find_HII_bubbles(self, snapshot, state):
         return self._run("mxref_find_HII_bubbles", snapshot, state)
+
+    def construct_baryon_grids(self, snapshot: int, gals, state, bh=(0, 0.0, 0.0)):
+        self._sync_in(state)
+        self.lib.mxref_construct_baryon_grids(snapshot, len(gals["type"]), _ptr(gals["pos"]), _ptr(gals["type"]),
+                                              _ptr(gals["fesc_gsm"]), _ptr(gals["gross_sm"]), _ptr(gals.get("bhm")),
+                                              _ptr(gals.get("ebhm")), bh[0], bh[1], bh[2])
+        self._sync_out(state)
+
+    def calculate_Mvir_crit(self, redshift: float, sm, J_21_at_ion, z_at_ion) -> np.ndarray:
+        out = np.zeros_like(J_21_at_ion, dtype=np.float32)
+        self.lib.mxref_calculate_Mvir_crit(redshift, *sm, _ptr(J_21_at_ion), _ptr(z_at_ion), _ptr(out))
+        return out
 
     def lightcone_init(self, end_redshift: float, last_output_snap: int):
         e = ctypes.c_int()

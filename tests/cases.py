@@ -86,3 +86,17 @@ def run_case(backend, w: Workload, gen: Optional[syn.FieldGenerator] = None, sta
 
 OUTPUT_GRIDS = ["xH", "z_at_ionization", "r_bubble", "J_21", "J_21_at_ionization", "Gamma12", "N_rec", "delta_T",
                 "TS_box", "Tk_box", "x_e_box_prev", "x_e_box", "vel"]
+
+
+def galaxies(D: int, L: float, n: int, seed: int) -> Dict[str, np.ndarray]:
+    """Seeded galaxy list for the deposit: uniform positions (a few exactly on
+    the far box face, which the nearest-grid-point rule wraps to cell 0), ~10%
+    dead galaxies (Type 3, skipped), lognormal masses in internal units
+    (1e10 Msun/h), and black holes."""
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(0.0, L, (n, 3)).astype(np.float32)
+    pos[: max(1, n // 50), 0] = np.float32(L)
+    typ = rng.choice([0, 1, 2, 3], size=n, p=[0.5, 0.3, 0.1, 0.1]).astype(np.int32)
+    gsm = 10.0 ** rng.normal(-4.0, 1.0, n)
+    return {"pos": np.ascontiguousarray(pos), "type": typ, "fesc_gsm": 0.1 * gsm, "gross_sm": gsm,
+            "bhm": 10.0 ** rng.normal(-5.0, 1.0, n), "ebhm": 10.0 ** rng.normal(-6.0, 1.0, n)}

@@ -110,3 +110,43 @@ def test_lightcone_restatement_bit_exact_against_reference(D, L):
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip().startswith("OK"), r.stdout
+
+
+DEPOSIT_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r}); sys.path.insert(0, {tests!r})
+from cases import Case, initial, galaxies
+from meraxes_gb300 import synthetic as syn
+from oracle import OracleBackend, RefBackend
+c = Case('dep', 'full_256', {D}, {{'reion_efficiency': 31043.3, 'clumping_factor': 2.0}}, fesc=0.01)
+w = c.workload()
+outs = []
+for B in (RefBackend, OracleBackend):
+    b = B(w.params, w.redshifts, syn.TABLES_DIR)
+    st = initial(w, b.n_sfr_histories)
+    D = w.params.grid_dim
+    npad = D * D * 2 * (D // 2 + 1)
+    st.update({{k: np.zeros(npad, np.float32).reshape(D, D, -1) for k in ('stars', 'weighted_sfr', 'sfr')}})
+    st['sfr_histories'] = np.random.default_rng(1).random((b.n_sfr_histories, npad)).astype(np.float32)
+    res = []
+    for s, bh in ((0, (0, 0.0, 0.0)), (1, (1, 1e-5, 1.57))):
+        b.construct_baryon_grids(s, galaxies(D, w.params.box_size, {n}, 11 + s), st, bh)
+        res += [st[k].copy() for k in ('stars', 'weighted_sfr', 'sfr', 'sfr_histories')]
+    rng = np.random.default_rng(2)
+    J = (10.0 ** rng.normal(-1, 0.5, (D,) * 3)).astype(np.float32)
+    zi = np.where(rng.random((D,) * 3) < 0.6, rng.uniform(9.0, 14.0, (D,) * 3), -1.0).astype(np.float32)
+    res.append(b.calculate_Mvir_crit(10.0, (0.049, 0.17, -2.1, 2.0, 2.5), J, zi))
+    outs.append(res)
+ok = all(np.array_equal(x, y) for x, y in zip(*outs))
+print('OK' if ok else 'MISMATCH', [float(np.abs(x - y).max()) for x, y in zip(*outs)],
+      'nonzero stars', int((outs[0][0] > 0).sum()), 'Mvir_crit>0', int((outs[0][-1] > 0).sum()))
+"""
+
+
+@pytest.mark.parametrize("D,n", [(16, 3000), (24, 20000)])
+def test_deposit_and_Mvir_crit_restatements_bit_exact_against_reference(D, n):
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = DEPOSIT_SCRIPT.format(root=os.path.dirname(here), tests=here, D=D, n=n)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip().startswith("OK"), r.stdout
