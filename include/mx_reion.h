@@ -106,7 +106,7 @@ typedef struct mx_params
   double spec_index_xray_gal;   /* SpecIndexXrayGal */
   double nu_xray_soft_cut;      /* NuXraySoftCut [eV] */
   double nu_xray_max;           /* NuXrayMax [eV] */
-  double reion_sfr_timescale;   /* ReionSfrTimescale (kept for completeness) */
+  double reion_sfr_timescale;   /* ReionSfrTimescale (construct_baryon_grids) */
   double clumping_factor;       /* x_e sink clumping; the reference hard-codes
                                    CLUMPING_FACTOR = 2 (XRayHeatingFunctions.h:30-32) */
 } mx_params;
@@ -257,6 +257,78 @@ int mx_Compute_PS_device(mx_ctx* ctx,
                          float* ps_error,
                          int32_t cap,
                          void* stream);
+
+/* Galaxy properties read by construct_baryon_grids, one entry per galaxy of
+ * the snapshot in the reference's galaxy-list order (map_galaxies_to_slabs,
+ * reionization.c:1109-1161, sorts the gal_to_slab_t map stably; one rank).
+ * Field names follow galaxy_t (src/meraxes.h).  gross_stellar_mass is read
+ * only with the spin temperature, black_hole_mass and effective_bhm only with
+ * BH feedback; the others may be NULL then. */
+typedef struct mx_galaxies
+{
+  int64_t n;
+  const float* pos;                  /* Pos, float[n][3], Mpc/h */
+  const int32_t* type;               /* Type; galaxies of Type > 2 are skipped */
+  const double* fesc_weighted_gsm;   /* FescWeightedGSM */
+  const double* gross_stellar_mass;  /* GrossStellarMass */
+  const double* black_hole_mass;     /* BlackHoleMass */
+  const double* effective_bhm;       /* EffectiveBHM */
+} mx_galaxies;
+
+/* Galaxy -> grid deposit: construct_baryon_grids(snapshot, local_ngals)
+ * (src/core/reionization.c:1353-1615, declared reionization.h:66; one rank,
+ * no mini-haloes).  Writes grids->stars and grids->weighted_sfr (PADDED) and,
+ * with the spin temperature, grids->sfr and the newest slice of
+ * grids->sfr_histories after shifting the older slices back by one, like the
+ * reference.  Each galaxy goes to its nearest grid point (pos_to_ngp,
+ * misc_tools.c:163-173); the cell sums are the reference's float sums in
+ * galaxy order.  flag_bh_feedback, bh_limit and alpha_uv_bh are
+ * physics.Flag_BHFeedback, BlackHoleMassLimitReion and ReionAlphaUVBH; the
+ * SFR timescale is ReionSfrTimescale * hubble_time(snapshot).  A galaxy below
+ * the box (a negative grid index, where the reference asserts) gives
+ * MX_EINVAL; grids with 2^32 - 1 cells or more give MX_ENOTSUP.
+ * mx_construct_baryon_grids takes HOST galaxy arrays and grids;
+ * the _device variant takes DEVICE arrays (the double arrays 8-byte aligned)
+ * and grids, orders the work on `stream` and waits for it before returning
+ * (to report the error above).  The galaxy scratch (sort keys and CUB
+ * storage) grows with the largest galaxy count seen. */
+int mx_construct_baryon_grids(mx_ctx* ctx,
+                              int32_t snapshot,
+                              const mx_galaxies* galaxies,
+                              int32_t flag_bh_feedback,
+                              double bh_limit,
+                              double alpha_uv_bh,
+                              mx_grids* grids);
+int mx_construct_baryon_grids_device(mx_ctx* ctx,
+                                     int32_t snapshot,
+                                     const mx_galaxies* galaxies,
+                                     int32_t flag_bh_feedback,
+                                     double bh_limit,
+                                     double alpha_uv_bh,
+                                     mx_grids* grids,
+                                     void* stream);
+
+/* Critical virial mass of UVB feedback per cell: calculate_Mvir_crit(redshift)
+ * (src/physics/reionization.c:10-59, declared physics/reionization.h:11;
+ * Sobacchi & Mesinger 2013b).  sm_params = {ReionSMParam_m0, _a, _b, _c, _d};
+ * J_21_at_ionization, z_at_ionization and Mvir_crit are REAL grids; cells not
+ * yet ionised at `redshift` get 0.  Computed in double per cell, like the
+ * reference; pow is CUDA's, so a cell may differ from the reference's by one
+ * float ulp.  Host grids for mx_calculate_Mvir_crit, device grids on `stream`
+ * for the _device variant (which does not wait). */
+int mx_calculate_Mvir_crit(mx_ctx* ctx,
+                           double redshift,
+                           const double sm_params[5],
+                           const float* J_21_at_ionization,
+                           const float* z_at_ionization,
+                           float* Mvir_crit);
+int mx_calculate_Mvir_crit_device(mx_ctx* ctx,
+                                  double redshift,
+                                  const double sm_params[5],
+                                  const float* J_21_at_ionization,
+                                  const float* z_at_ionization,
+                                  float* Mvir_crit,
+                                  void* stream);
 
 /* Build information: returns a static string. */
 const char* mx_build_info(void);

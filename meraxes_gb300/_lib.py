@@ -9,7 +9,7 @@ import ctypes
 import os
 import threading
 
-from .params import MxGlobals, MxGrids, MxParams
+from .params import MxGalaxies, MxGlobals, MxGrids, MxParams
 
 _LOCK = threading.Lock()
 _LIB = None
@@ -25,6 +25,8 @@ EXPORTS = [
     "mx_step_device", "mx_profile_enable", "mx_profile_read", "mx_build_info",
     "mx_brightness_temperature_noalloc", "mx_ps_length", "mx_Compute_PS", "mx_Compute_PS_device",
     "mx_lightcone_init", "mx_ConstructLightcone", "mx_ConstructLightcone_device",
+    "mx_construct_baryon_grids", "mx_construct_baryon_grids_device", "mx_calculate_Mvir_crit",
+    "mx_calculate_Mvir_crit_device",
 ]
 
 
@@ -99,5 +101,16 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mx_ConstructLightcone.restype = ctypes.c_int
         L.mx_ConstructLightcone_device.argtypes = [P, ctypes.c_int32, P, P, P, P, P]
         L.mx_ConstructLightcone_device.restype = ctypes.c_int
+        gal = [P, ctypes.c_int32, ctypes.POINTER(MxGalaxies), ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+               ctypes.POINTER(MxGrids)]
+        L.mx_construct_baryon_grids.argtypes = gal
+        L.mx_construct_baryon_grids.restype = ctypes.c_int
+        L.mx_construct_baryon_grids_device.argtypes = gal + [P]
+        L.mx_construct_baryon_grids_device.restype = ctypes.c_int
+        mvir = [P, ctypes.c_double, ctypes.POINTER(ctypes.c_double), P, P, P]
+        L.mx_calculate_Mvir_crit.argtypes = mvir
+        L.mx_calculate_Mvir_crit.restype = ctypes.c_int
+        L.mx_calculate_Mvir_crit_device.argtypes = mvir + [P]
+        L.mx_calculate_Mvir_crit_device.restype = ctypes.c_int
         _LIB = L
         return L

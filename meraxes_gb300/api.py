@@ -20,7 +20,7 @@ from typing import Dict, Optional, Sequence
 import numpy as np
 
 from . import _lib
-from .params import GRID_NAMES, MxGlobals, MxGrids, ReionParams
+from .params import GRID_NAMES, MxGalaxies, MxGlobals, MxGrids, ReionParams
 from .synthetic import TABLES_DIR
 
 
@@ -180,4 +180,76 @@ class ReionGridStep:
                     raise ValueError("need C-contiguous float32 numpy arrays")
             rc = self.lib.mx_ConstructLightcone(self.ctx, snapshot, delta_T.ctypes.data, delta_T_prev.ctypes.data,
                                                 lightcone.ctypes.data, z.ctypes.data)
+        self._check(rc)
+
+    _GALAXY_DTYPES = {"pos": "float32", "type": "int32", "fesc_weighted_gsm": "float64",
+                      "gross_stellar_mass": "float64", "black_hole_mass": "float64", "effective_bhm": "float64"}
+
+    def _galaxies(self, galaxies, device: bool):
+        g = MxGalaxies()
+        n = None
+        for name, dt in self._GALAXY_DTYPES.items():
+            a = galaxies.get(name)
+            if a is None:
+                continue
+            if device:
+                import torch
+
+                if not _is_torch_cuda(a) or a.dtype != getattr(torch, dt) or not a.is_contiguous():
+                    raise ValueError(f"{name}: need a contiguous {dt} CUDA tensor")
+                ptr = a.data_ptr()
+            else:
+                if not isinstance(a, np.ndarray) or a.dtype != np.dtype(dt) or not a.flags.c_contiguous:
+                    raise ValueError(f"{name}: need a C-contiguous {dt} numpy array")
+                ptr = a.ctypes.data
+            rows = a.shape[0] if len(a.shape) else 0
+            if name == "pos" and tuple(a.shape[1:]) != (3,):
+                raise ValueError("pos: need shape [n, 3]")
+            if n is not None and rows != n:
+                raise ValueError(f"{name}: {rows} galaxies, expected {n}")
+            n = rows
+            setattr(g, name, ptr)
+        g.n = n or 0
+        return g
+
+    def construct_baryon_grids(self, snapshot: int, galaxies, grids, flag_bh_feedback: int = 0,
+                               bh_limit: float = 0.0, alpha_uv_bh: float = 0.0):
+        """construct_baryon_grids: deposits the galaxies (dict of arrays named
+        like `mx_galaxies`: pos [n, 3] float32, type int32, the masses float64)
+        into grids["stars"], ["weighted_sfr"] and, with the spin temperature,
+        ["sfr"] and ["sfr_histories"].  numpy arrays select the host entry
+        point; CUDA tensors the device one on torch's current stream."""
+        g, device = self._grids(grids)
+        gal = self._galaxies(galaxies, device)
+        if device:
+            import torch
+
+            stream = torch.cuda.current_stream().cuda_stream
+            rc = self.lib.mx_construct_baryon_grids_device(self.ctx, snapshot, ctypes.byref(gal), flag_bh_feedback,
+                                                          bh_limit, alpha_uv_bh, ctypes.byref(g),
+                                                          ctypes.c_void_p(stream))
+        else:
+            rc = self.lib.mx_construct_baryon_grids(self.ctx, snapshot, ctypes.byref(gal), flag_bh_feedback, bh_limit,
+                                                   alpha_uv_bh, ctypes.byref(g))
+        self._check(rc)
+
+    def calculate_Mvir_crit(self, redshift: float, sm_params, J_21_at_ionization, z_at_ionization, Mvir_crit):
+        """calculate_Mvir_crit: writes Mvir_crit (REAL) from the ionisation
+        history; sm_params = (ReionSMParam_m0, _a, _b, _c, _d)."""
+        sm = (ctypes.c_double * 5)(*[float(v) for v in sm_params])
+        arrays = (J_21_at_ionization, z_at_ionization, Mvir_crit)
+        if _is_torch_cuda(Mvir_crit):
+            import torch
+
+            for a in arrays:
+                if not _is_torch_cuda(a) or a.dtype != torch.float32 or not a.is_contiguous():
+                    raise ValueError("need contiguous float32 CUDA tensors")
+            stream = torch.cuda.current_stream().cuda_stream
+            rc = self.lib.mx_calculate_Mvir_crit_device(self.ctx, redshift, sm, *[a.data_ptr() for a in arrays],
+                                                        ctypes.c_void_p(stream))
+        else:
+            for a in arrays:
+                if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+                    raise ValueError("need C-contiguous float32 numpy arrays")
+            rc = self.lib.mx_calculate_Mvir_crit(self.ctx, redshift, sm, *[a.ctypes.data for a in arrays])
         self._check(rc)

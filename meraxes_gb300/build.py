@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libmxreion.so")
-SOURCES = ["kernels.cu", "kernels_ts.cu", "fft3d.cu", "mx_reion.cu", "host_physics.cpp", "noalloc.cu", "ps.cu", "pecvel.cu", "lightcone.cu"]
+SOURCES = ["kernels.cu", "kernels_ts.cu", "fft3d.cu", "mx_reion.cu", "host_physics.cpp", "noalloc.cu", "ps.cu", "pecvel.cu", "lightcone.cu", "deposit.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -8,6 +8,7 @@
 #include <cmath>
 
 #include "kernels.cuh"
+#include "deposit.cuh"
 #include "fft3d.cuh"
 #include "lightcone.cuh"
 #include "pecvel.cuh"
@@ -72,7 +73,7 @@ __device__ __forceinline__ long long pad_of(long long ir, int D, int H)
 int kernel_launch_count()
 {
   return g_launches + ts_kernel_launches() + fft_kernel_launches() + ps_kernel_launches() + pecvel_kernel_launches() +
-         lightcone_kernel_launches();
+         lightcone_kernel_launches() + deposit_kernel_launches();
 }
 void reset_kernel_launch_count() { g_launches = 0; }
 

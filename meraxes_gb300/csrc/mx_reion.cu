@@ -16,6 +16,7 @@
 #include <thread>
 #include <vector>
 
+#include "deposit.cuh"
 #include "fft3d.cuh"
 #include "lightcone.cuh"
 #include "pecvel.cuh"
@@ -88,6 +89,8 @@ struct mx_ctx
   double* d_lc_times = nullptr;  // slice times of one snapshot
   float* d_lc_scratch = nullptr; // host-pointer calls: D*D x max slices per snapshot
   long long lc_max_slices = 0;
+  void* d_gal = nullptr;          // galaxy sort keys, indices, CUB scratch, host-copy arrays
+  size_t gal_bytes = 0;
   double* d_ps_partials = nullptr; // RED_BLOCKS x 3 x PS_MAX_BINS
   double* d_ps_sums = nullptr;     // 3 x PS_MAX_BINS + 1
   double* h_ps_sums = nullptr;     // pinned copy
@@ -168,6 +171,7 @@ mx_ctx::~mx_ctx()
   cudaFree(d_in_ptrs);
   cudaFree(d_lc_times);
   cudaFree(d_lc_scratch);
+  cudaFree(d_gal);
   cudaFree(d_ps_partials);
   cudaFree(d_ps_sums);
   cudaFreeHost(h_ps_sums);
@@ -1173,6 +1177,137 @@ static void construct_lightcone(mx_ctx* c, int snapshot, const float* dT, const 
 }
 
 // ======================================================================
+// construct_baryon_grids (reionization.c:1353-1615) and calculate_Mvir_crit
+// (physics/reionization.c:10-59)
+// ======================================================================
+// hubble_time (virial_properties.c:79-93), internal time units
+static double hubble_time(const mx_ctx* c, int snapshot)
+{
+  const double zp1 = c->zz[snapshot] + 1;
+  return 1.0 / (c->d.hubble_int * std::sqrt(c->p.omega_m * zp1 * zp1 * zp1 + c->p.omega_k * zp1 * zp1 +
+                                            c->p.omega_lambda));
+}
+
+struct GalaxyScratch
+{
+  unsigned *keys_in, *keys;
+  int *idx_in, *idx;
+  void* sort_tmp;
+  size_t sort_bytes;
+  // device copies of host galaxy arrays
+  float* pos;
+  int* type;
+  double *fesc, *gross, *bhm, *ebhm;
+};
+
+// Galaxy scratch in one allocation that grows with the galaxy count.
+static GalaxyScratch galaxy_scratch(mx_ctx* c, int n, bool host_copy, cudaStream_t s)
+{
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t nn = (size_t)std::max(n, 1);
+  GalaxyScratch g{};
+  g.sort_bytes = deposit_sort_bytes(n);
+  size_t bytes = 4 * up(4 * nn) + up(g.sort_bytes);
+  if (host_copy)
+    bytes += up(12 * nn) + up(4 * nn) + 4 * up(8 * nn);
+  if (bytes > c->gal_bytes) {
+    MX_CUDA(cudaStreamSynchronize(s));
+    MX_CUDA(cudaFree(c->d_gal));
+    c->d_gal = nullptr;
+    c->gal_bytes = 0;
+    MX_CUDA(cudaMalloc(&c->d_gal, bytes));
+    c->gal_bytes = bytes;
+  }
+  char* q = static_cast<char*>(c->d_gal);
+  auto take = [&](size_t b) {
+    char* r = q;
+    q += up(b);
+    return r;
+  };
+  g.keys_in = reinterpret_cast<unsigned*>(take(4 * nn));
+  g.keys = reinterpret_cast<unsigned*>(take(4 * nn));
+  g.idx_in = reinterpret_cast<int*>(take(4 * nn));
+  g.idx = reinterpret_cast<int*>(take(4 * nn));
+  g.sort_tmp = take(g.sort_bytes);
+  if (host_copy) {
+    g.pos = reinterpret_cast<float*>(take(12 * nn));
+    g.type = reinterpret_cast<int*>(take(4 * nn));
+    g.fesc = reinterpret_cast<double*>(take(8 * nn));
+    g.gross = reinterpret_cast<double*>(take(8 * nn));
+    g.bhm = reinterpret_cast<double*>(take(8 * nn));
+    g.ebhm = reinterpret_cast<double*>(take(8 * nn));
+  }
+  return g;
+}
+
+static void check_galaxies(const mx_params& p, const mx_galaxies* gals, int flag_bh)
+{
+  if (!gals || gals->n < 0 || gals->n > INT32_MAX / 3)
+    throw CudaError{ MX_EINVAL, "construct_baryon_grids: invalid galaxy list" };
+  if (gals->n > 0 && (!gals->pos || !gals->type || !gals->fesc_weighted_gsm ||
+                      (p.flag_spin_temp && !gals->gross_stellar_mass) ||
+                      (flag_bh && (!gals->black_hole_mass || !gals->effective_bhm))))
+    throw CudaError{ MX_EINVAL, "construct_baryon_grids: a galaxy array the configuration reads is NULL" };
+}
+
+// Deposit of device galaxy arrays into device grids.  `sfr_hist` holds the
+// n_hist slices; the reference shifts them one snapshot back first
+// (reionization.c:1384-1389), slice by slice from the oldest.
+static void run_deposit(mx_ctx* c, int snapshot, const mx_galaxies& gal, const GalaxyScratch& gs, int flag_bh,
+                        double bh_limit, double alpha_uv_bh, float* stars, float* wsfr, float* sfr, float* sfr_hist,
+                        bool shift_history, cudaStream_t s)
+{
+  const mx_params& p = c->p;
+  const GridDims& gd = c->gd;
+  const bool spin = p.flag_spin_temp != 0;
+  if (gd.N >= 0xffffffffLL)
+    throw CudaError{ MX_ENOTSUP, "construct_baryon_grids: 32-bit cell keys hold grids below 2^32 - 1 cells" };
+  if (spin && shift_history && sfr_hist)
+    for (int k = c->n_hist - 2; k >= 0; k--)
+      MX_CUDA(cudaMemcpyAsync(sfr_hist + (size_t)(k + 1) * gd.P, sfr_hist + (size_t)k * gd.P, sizeof(float) * gd.P,
+                              cudaMemcpyDeviceToDevice, s));
+  DepositArgs a{};
+  a.n = (int)gal.n;
+  a.pos = gal.pos;
+  a.type = gal.type;
+  a.fesc_gsm = gal.fesc_weighted_gsm;
+  a.gross_sm = gal.gross_stellar_mass;
+  a.bhm = gal.black_hole_mass;
+  a.ebhm = gal.effective_bhm;
+  a.flag_bh = flag_bh;
+  a.bh_limit = bh_limit;
+  a.alpha_uv_bh = alpha_uv_bh;
+  a.alpha_uv = p.alpha_uv;
+  a.box_size = p.box_size;
+  a.spin = spin;
+  a.sfr_timescale = p.reion_sfr_timescale * hubble_time(c, snapshot);
+  a.keys_in = gs.keys_in;
+  a.keys = gs.keys;
+  a.idx_in = gs.idx_in;
+  a.idx = gs.idx;
+  // REAL sums in unfiltered-spectrum scratch slots 0-2
+  a.buf_stars = reinterpret_cast<float*>(c->d_unf);
+  a.buf_wsfr = reinterpret_cast<float*>(c->d_unf + gd.C);
+  a.buf_sfr = reinterpret_cast<float*>(c->d_unf + 2 * gd.C);
+  a.err = c->d_err;
+  a.stars = stars;
+  a.weighted_sfr = wsfr;
+  a.sfr = sfr;
+  a.sfr_hist0 = sfr_hist;
+  {
+    Prof pr(c, "deposit", (double)gal.n * 44.0 + 4.0 * gd.P * (spin ? 5 : 2), s);
+    MX_CUDA(launch_deposit(a, gs.sort_tmp, gs.sort_bytes, gd, s));
+  }
+  unsigned int errw = 0;
+  MX_CUDA(cudaMemcpyAsync(&errw, c->d_err, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+  MX_CUDA(cudaStreamSynchronize(s));
+  if (errw) {
+    MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
+    throw CudaError{ MX_EINVAL, "construct_baryon_grids: a galaxy lies below the box (negative grid index)" };
+  }
+}
+
+// ======================================================================
 // C ABI
 // ======================================================================
 template <class F>
@@ -1312,6 +1447,124 @@ int mx_Compute_PS_device(mx_ctx* ctx, const float* delta_T, float* ps_k, float* 
     nb = run_power_spectrum(ctx, delta_T, ps_k, ps_data, ps_error, cap, pick(ctx, stream));
   });
   return rc == MX_OK ? nb : rc;
+}
+
+int mx_construct_baryon_grids(mx_ctx* ctx, int32_t snapshot, const mx_galaxies* galaxies, int32_t flag_bh_feedback,
+                              double bh_limit, double alpha_uv_bh, mx_grids* grids)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    const mx_params& p = ctx->p;
+    const GridDims& gd = ctx->gd;
+    check_galaxies(p, galaxies, flag_bh_feedback);
+    const bool spin = p.flag_spin_temp != 0;
+    const bool hist = spin && ctx->n_hist > 0;
+    if (!grids || !grids->stars || !grids->weighted_sfr || (spin && !grids->sfr) || (hist && !grids->sfr_histories))
+      throw CudaError{ MX_EINVAL, "construct_baryon_grids: an output grid is NULL" };
+    ctx->ensure_mirror();
+    cudaStream_t s = ctx->stream;
+    const int n = (int)galaxies->n;
+    const GalaxyScratch gs = galaxy_scratch(ctx, n, true, s);
+    mx_galaxies dg{};
+    dg.n = n;
+    dg.pos = gs.pos;
+    dg.type = gs.type;
+    dg.fesc_weighted_gsm = gs.fesc;
+    dg.gross_stellar_mass = spin ? gs.gross : nullptr;
+    dg.black_hole_mass = flag_bh_feedback ? gs.bhm : nullptr;
+    dg.effective_bhm = flag_bh_feedback ? gs.ebhm : nullptr;
+    if (n > 0) {
+      MX_CUDA(cudaMemcpyAsync(gs.pos, galaxies->pos, 12 * (size_t)n, cudaMemcpyHostToDevice, s));
+      MX_CUDA(cudaMemcpyAsync(gs.type, galaxies->type, 4 * (size_t)n, cudaMemcpyHostToDevice, s));
+      MX_CUDA(cudaMemcpyAsync(gs.fesc, galaxies->fesc_weighted_gsm, 8 * (size_t)n, cudaMemcpyHostToDevice, s));
+      if (spin)
+        MX_CUDA(cudaMemcpyAsync(gs.gross, galaxies->gross_stellar_mass, 8 * (size_t)n, cudaMemcpyHostToDevice, s));
+      if (flag_bh_feedback) {
+        MX_CUDA(cudaMemcpyAsync(gs.bhm, galaxies->black_hole_mass, 8 * (size_t)n, cudaMemcpyHostToDevice, s));
+        MX_CUDA(cudaMemcpyAsync(gs.ebhm, galaxies->effective_bhm, 8 * (size_t)n, cudaMemcpyHostToDevice, s));
+      }
+    }
+    // older history slices move on the host; the newest goes through the
+    // device, which writes its cells and keeps its padding
+    const size_t slice = sizeof(float) * gd.P;
+    if (hist) {
+      std::memmove(grids->sfr_histories + gd.P, grids->sfr_histories, slice * (size_t)(ctx->n_hist - 1));
+      MX_CUDA(cudaMemcpyAsync(ctx->mirror.sfr_histories, grids->sfr_histories, slice, cudaMemcpyHostToDevice, s));
+    }
+    run_deposit(ctx, snapshot, dg, gs, flag_bh_feedback, bh_limit, alpha_uv_bh, ctx->mirror.stars,
+                ctx->mirror.weighted_sfr, ctx->mirror.sfr, hist ? ctx->mirror.sfr_histories : nullptr, false, s);
+    MX_CUDA(cudaMemcpyAsync(grids->stars, ctx->mirror.stars, slice, cudaMemcpyDeviceToHost, s));
+    MX_CUDA(cudaMemcpyAsync(grids->weighted_sfr, ctx->mirror.weighted_sfr, slice, cudaMemcpyDeviceToHost, s));
+    if (spin)
+      MX_CUDA(cudaMemcpyAsync(grids->sfr, ctx->mirror.sfr, slice, cudaMemcpyDeviceToHost, s));
+    if (hist)
+      MX_CUDA(cudaMemcpyAsync(grids->sfr_histories, ctx->mirror.sfr_histories, slice, cudaMemcpyDeviceToHost, s));
+    MX_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int mx_construct_baryon_grids_device(mx_ctx* ctx, int32_t snapshot, const mx_galaxies* galaxies,
+                                     int32_t flag_bh_feedback, double bh_limit, double alpha_uv_bh, mx_grids* grids,
+                                     void* stream)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    const mx_params& p = ctx->p;
+    check_galaxies(p, galaxies, flag_bh_feedback);
+    const bool spin = p.flag_spin_temp != 0;
+    const bool hist = spin && ctx->n_hist > 0;
+    if (!grids || !grids->stars || !grids->weighted_sfr || (spin && !grids->sfr) || (hist && !grids->sfr_histories))
+      throw CudaError{ MX_EINVAL, "construct_baryon_grids: an output grid is NULL" };
+    const void* dbl[] = { galaxies->fesc_weighted_gsm, galaxies->gross_stellar_mass, galaxies->black_hole_mass,
+                          galaxies->effective_bhm };
+    for (const void* q : dbl)
+      if ((uintptr_t)q % 8 != 0)
+        throw CudaError{ MX_EINVAL, "construct_baryon_grids: device galaxy arrays must be 8-byte aligned" };
+    cudaStream_t s = pick(ctx, stream);
+    const GalaxyScratch gs = galaxy_scratch(ctx, (int)galaxies->n, false, s);
+    run_deposit(ctx, snapshot, *galaxies, gs, flag_bh_feedback, bh_limit, alpha_uv_bh, grids->stars,
+                grids->weighted_sfr, grids->sfr, hist ? grids->sfr_histories : nullptr, true, s);
+  });
+}
+
+int mx_calculate_Mvir_crit(mx_ctx* ctx, double redshift, const double sm_params[5], const float* J_21_at_ionization,
+                           const float* z_at_ionization, float* Mvir_crit)
+{
+  return guarded(ctx, [&]() {
+    if (!sm_params || !J_21_at_ionization || !z_at_ionization || !Mvir_crit)
+      throw CudaError{ MX_EINVAL, "calculate_Mvir_crit: NULL pointer" };
+    ctx->ensure_mirror();
+    cudaStream_t s = ctx->stream;
+    const size_t bytes = sizeof(float) * ctx->gd.N;
+    float* d_out = reinterpret_cast<float*>(ctx->d_unf);
+    MX_CUDA(cudaMemcpyAsync(ctx->mirror.J_21_at_ionization, J_21_at_ionization, bytes, cudaMemcpyHostToDevice, s));
+    MX_CUDA(cudaMemcpyAsync(ctx->mirror.z_at_ionization, z_at_ionization, bytes, cudaMemcpyHostToDevice, s));
+    {
+      Prof pr(ctx, "k_Mvir_crit", 12.0 * ctx->gd.N, s);
+      launch_Mvir_crit(redshift, sm_params, ctx->p.hubble_h, ctx->mirror.J_21_at_ionization,
+                       ctx->mirror.z_at_ionization, d_out, ctx->gd, s);
+    }
+    MX_CUDA(cudaGetLastError());
+    MX_CUDA(cudaMemcpyAsync(Mvir_crit, d_out, bytes, cudaMemcpyDeviceToHost, s));
+    MX_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int mx_calculate_Mvir_crit_device(mx_ctx* ctx, double redshift, const double sm_params[5],
+                                  const float* J_21_at_ionization, const float* z_at_ionization, float* Mvir_crit,
+                                  void* stream)
+{
+  return guarded(ctx, [&]() {
+    if (!sm_params || !J_21_at_ionization || !z_at_ionization || !Mvir_crit)
+      throw CudaError{ MX_EINVAL, "calculate_Mvir_crit: NULL pointer" };
+    cudaStream_t s = pick(ctx, stream);
+    {
+      Prof pr(ctx, "k_Mvir_crit", 12.0 * ctx->gd.N, s);
+      launch_Mvir_crit(redshift, sm_params, ctx->p.hubble_h, J_21_at_ionization, z_at_ionization, Mvir_crit, ctx->gd,
+                       s);
+    }
+    MX_CUDA(cudaGetLastError());
+  });
 }
 
 int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out)

@@ -119,6 +119,15 @@ class MxGrids(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in GRID_NAMES]
 
 
+GALAXY_FIELDS = ["pos", "type", "fesc_weighted_gsm", "gross_stellar_mass", "black_hole_mass", "effective_bhm"]
+
+
+class MxGalaxies(ctypes.Structure):
+    """ctypes image of `mx_galaxies` (include/mx_reion.h)."""
+
+    _fields_ = [("n", ctypes.c_int64)] + [(n, ctypes.c_void_p) for n in GALAXY_FIELDS]
+
+
 @dataclasses.dataclass
 class ReionParams:
     """Hot-path parameters with the reference defaults (defaults.par)."""

@@ -10,6 +10,7 @@ grids and the per-snapshot global scalars.
     python tests/golden/make_golden.py full24     # one case
     python tests/golden/make_golden.py ps         # power spectrum fixture
     python tests/golden/make_golden.py lightcone  # light-cone fixture
+    python tests/golden/make_golden.py deposit    # galaxy deposit + Mvir_crit
 
 Each case runs in a fresh process because the reference keeps its state in
 globals.
@@ -110,6 +111,59 @@ def make_lightcone(D: int = 16, L: float = 64.0, end_z: float = 8.6):
     print("lightcone16 written")
 
 
+DEPOSIT_CASE = ("dep16", "full_256", 16, {"reion_efficiency": 31043.3, "clumping_factor": 2.0})
+DEPOSIT_BH = ((0, 0.0, 0.0), (1, 1e-5, 1.57))  # Flag_BHFeedback, BlackHoleMassLimitReion, ReionAlphaUVBH
+MVIR_SM = (0.049, 0.17, -2.1, 2.0, 2.5)  # ReionSMParam_m0, a, b, c, d
+
+
+def deposit_history_init(n_slices: int, npad: int):
+    """A non-zero starting sfr_histories, so that the shift is visible."""
+    import numpy as np
+
+    base = (np.arange(npad) % 97).astype(np.float32) * np.float32(1e-4)
+    return np.stack([base + np.float32(k) for k in range(n_slices)]).astype(np.float32)
+
+
+def mvir_inputs(D: int):
+    """Seeded J_21 and z at ionisation (60% of the cells ionised)."""
+    import numpy as np
+
+    rng = np.random.default_rng(2)
+    J = (10.0 ** rng.normal(-1, 0.5, (D,) * 3)).astype(np.float32)
+    zi = np.where(rng.random((D,) * 3) < 0.6, rng.uniform(9.0, 14.0, (D,) * 3), -1.0).astype(np.float32)
+    return J, zi
+
+
+def make_deposit(n: int = 2000):
+    """construct_baryon_grids of the reference for two snapshots (without,
+    then with BH feedback) on seeded galaxy lists, and calculate_Mvir_crit at
+    z = 10 on seeded ionisation histories."""
+    import numpy as np
+
+    from cases import Case, galaxies
+    from meraxes_gb300 import synthetic as syn
+    from oracle import RefBackend
+
+    name, kind, D, over = DEPOSIT_CASE
+    w = Case(name, kind, D, over, fesc=0.01).workload()
+    ref = RefBackend(w.params, w.redshifts, syn.TABLES_DIR)
+    npad = D * D * 2 * (D // 2 + 1)
+    st = {k: np.zeros(npad, np.float32).reshape(D, D, -1) for k in ("stars", "weighted_sfr", "sfr")}
+    st["sfr_histories"] = deposit_history_init(ref.n_sfr_histories, npad)
+    arrays = {"sfr_histories_init": st["sfr_histories"].copy()}
+    for s, bh in enumerate(DEPOSIT_BH):
+        gal = galaxies(D, w.params.box_size, n, 11 + s)
+        for k, v in gal.items():
+            arrays[f"gal{s}/{k}"] = v
+        ref.construct_baryon_grids(s, gal, st, bh)
+        for k in ("stars", "weighted_sfr", "sfr", "sfr_histories"):
+            arrays[f"out{s}/{k}"] = st[k].copy()
+    J, zi = mvir_inputs(D)
+    arrays.update(J_21_at_ionization=J, z_at_ionization=zi, Mvir_crit=ref.calculate_Mvir_crit(10.0, MVIR_SM, J, zi))
+    np.savez_compressed(os.path.join(HERE, "deposit16.npz"), **arrays)
+    print("deposit16 written")
+
+
 if __name__ == "__main__":
     from cases import CASES
 
@@ -118,6 +172,9 @@ if __name__ == "__main__":
         sys.exit(0)
     if sys.argv[1:2] == ["lightcone"]:
         make_lightcone()
+        sys.exit(0)
+    if sys.argv[1:2] == ["deposit"]:
+        make_deposit()
         sys.exit(0)
     names = sys.argv[1:] or list(CASES)
     if len(names) == 1:

@@ -255,3 +255,171 @@ def test_gpu_lightcone_matches_reference_fixture_and_oracle(device, tables_dir):
     assert np.array_equal(lg, lo) and np.array_equal(zg, zo) and np.array_equal(pg, po)
     np.testing.assert_allclose(lg, d["lightcone"], rtol=2 ** -23, atol=0)
     np.testing.assert_allclose(zg, d["redshifts"], rtol=2 ** -23, atol=0)
+
+
+# galaxy arrays: the oracle's names -> the mx_galaxies names of the API
+GAL_API = {"pos": "pos", "type": "type", "fesc_gsm": "fesc_weighted_gsm", "gross_sm": "gross_stellar_mass",
+           "bhm": "black_hole_mass", "ebhm": "effective_bhm"}
+DEPOSIT_GRIDS = ("stars", "weighted_sfr", "sfr", "sfr_histories")
+
+
+def _deposit_state(D, hist0):
+    npad = D * D * 2 * (D // 2 + 1)
+    st = {k: np.zeros(npad, np.float32).reshape(D, D, -1) for k in ("stars", "weighted_sfr", "sfr")}
+    if hist0 is not None:
+        st["sfr_histories"] = hist0.copy()
+    return st
+
+
+def _deposit_gpu(step, D, hist0, gal_list, bhs, device):
+    """construct_baryon_grids through the API for snapshots 0, 1, ...; the
+    grids after each snapshot as numpy arrays."""
+    import torch
+
+    st = _deposit_state(D, hist0)
+    if device:
+        st = {k: torch.from_numpy(v).cuda() for k, v in st.items()}
+    outs = []
+    for s, (gal, bh) in enumerate(zip(gal_list, bhs)):
+        g = {GAL_API[k]: np.ascontiguousarray(v) for k, v in gal.items()}
+        if device:
+            g = {k: torch.from_numpy(v).cuda() for k, v in g.items()}
+        step.construct_baryon_grids(s, g, st, *bh)
+        if device:
+            torch.cuda.synchronize()
+        outs.append({k: (v.cpu().numpy() if device else v.copy()) for k, v in st.items()})
+    return outs
+
+
+def _deposit_oracle(orc, D, hist0, gal_list, bhs):
+    st = _deposit_state(D, hist0)
+    outs = []
+    for s, (gal, bh) in enumerate(zip(gal_list, bhs)):
+        orc.construct_baryon_grids(s, gal, st, bh)
+        outs.append({k: v.copy() for k, v in st.items()})
+    return outs
+
+
+def _within_one_ulp(a, b):
+    """Equal, or one float32 rounding apart (CUDA's pow against glibc's)."""
+    return bool(np.all((a == b) | (np.abs(a - b) <= np.spacing(np.maximum(np.abs(a), np.abs(b))))))
+
+
+def _mvir_gpu(step, z, sm, J, zi, device):
+    import torch
+
+    if device:
+        out = torch.zeros(J.shape, dtype=torch.float32, device="cuda")
+        step.calculate_Mvir_crit(z, sm, torch.from_numpy(J).cuda(), torch.from_numpy(zi).cuda(), out)
+        torch.cuda.synchronize()
+        return out.cpu().numpy()
+    out = np.zeros_like(J)
+    step.calculate_Mvir_crit(z, sm, J, zi, out)
+    return out
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_gpu_deposit_and_Mvir_crit_match_reference_fixture(device):
+    """The reference's own deposit (two snapshots: without, then with BH
+    feedback; the SFR history shift included) bit for bit, and its
+    Mvir_crit grid within one float ulp."""
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_golden import DEPOSIT_BH, DEPOSIT_CASE, MVIR_SM
+
+    from meraxes_gb300.api import ReionGridStep
+
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "deposit16.npz"))
+    name, kind, D, over = DEPOSIT_CASE
+    w = Case(name, kind, D, over, fesc=0.01).workload()
+    step = ReionGridStep(w.params, w.redshifts)
+    assert step.n_sfr_histories == d["sfr_histories_init"].shape[0]
+    gal_list = [{k: d[f"gal{s}/{k}"] for k in GAL_API} for s in range(len(DEPOSIT_BH))]
+    outs = _deposit_gpu(step, D, d["sfr_histories_init"], gal_list, DEPOSIT_BH, device)
+    for s in range(len(DEPOSIT_BH)):
+        for k in DEPOSIT_GRIDS:
+            assert np.array_equal(outs[s][k], d[f"out{s}/{k}"]), (s, k)
+    got = _mvir_gpu(step, 10.0, MVIR_SM, d["J_21_at_ionization"], d["z_at_ionization"], device)
+    ref = d["Mvir_crit"]
+    assert np.array_equal(got > 0, ref > 0) and _within_one_ulp(got, ref)
+
+
+@pytest.mark.parametrize("D,n,base,clustered", [(64, 400000, "full_256", True), (48, 60000, "plain_64", False)])
+def test_gpu_deposit_matches_oracle(D, n, base, clustered, tables_dir):
+    """Against the oracle at larger sizes; `clustered` puts 400k galaxies in
+    1/64 of the box (about 100 per occupied cell: long float sums in galaxy
+    order)."""
+    from cases import galaxies
+    from meraxes_gb300.api import ReionGridStep
+    from oracle import OracleBackend
+
+    w = Case("dep", base, D, {"reion_efficiency": 3000.0}, fesc=0.01).workload()
+    orc = OracleBackend(w.params, w.redshifts, tables_dir)
+    step = ReionGridStep(w.params, w.redshifts)
+    assert step.n_sfr_histories == orc.n_sfr_histories
+    spin = bool(w.params.flag_spin_temp)
+    npad = D * D * 2 * (D // 2 + 1)
+    hist0 = (np.random.default_rng(5).random((orc.n_sfr_histories, npad)).astype(np.float32) if spin else None)
+    gal_list = []
+    for s in range(2):
+        g = galaxies(D, w.params.box_size, n, 40 + s)
+        if clustered:
+            g["pos"] = np.ascontiguousarray((g["pos"] * np.float32(0.25)).astype(np.float32))
+        gal_list.append(g)
+    bhs = ((1, 1e-5, 1.57), (0, 0.0, 0.0))
+    want = _deposit_oracle(orc, D, hist0, gal_list, bhs)
+    for device in (False, True):
+        got = _deposit_gpu(step, D, hist0, gal_list, bhs, device)
+        for s in range(2):
+            for k in want[s]:
+                assert np.array_equal(got[s][k], want[s][k]), (device, s, k)
+    occupied = (want[0]["stars"] > 0).sum()
+    assert occupied > (1000 if clustered else 10000)
+    rng = np.random.default_rng(7)
+    J = (10.0 ** rng.normal(-1, 0.5, (D,) * 3)).astype(np.float32)
+    zi = np.where(rng.random((D,) * 3) < 0.5, rng.uniform(8.0, 15.0, (D,) * 3), -1.0).astype(np.float32)
+    sm = (0.049, 0.17, -2.1, 2.0, 2.5)
+    ref = orc.calculate_Mvir_crit(9.0, sm, J, zi)
+    for device in (False, True):
+        got = _mvir_gpu(step, 9.0, sm, J, zi, device)
+        assert np.array_equal(got > 0, ref > 0) and _within_one_ulp(got, ref), device
+
+
+def test_gpu_deposit_edge_cases():
+    """No galaxies, only dead galaxies (Type 3), and a galaxy below the box:
+    empty grids with the history shifted; MX_EINVAL for the last, after which
+    the context still works."""
+    from meraxes_gb300._lib import MxError
+    from meraxes_gb300.api import ReionGridStep
+
+    D = 16
+    w = Case("dep", "full_256", D, {}, fesc=0.01).workload()
+    step = ReionGridStep(w.params, w.redshifts)
+    nh = step.n_sfr_histories
+    assert nh >= 2
+    npad = D * D * 2 * (D // 2 + 1)
+    hist0 = np.random.default_rng(3).random((nh, npad)).astype(np.float32)
+    empty = {"pos": np.zeros((0, 3), np.float32), "type": np.zeros(0, np.int32),
+             "fesc_gsm": np.zeros(0), "gross_sm": np.zeros(0)}
+    dead = {"pos": np.full((100, 3), 10.0, np.float32), "type": np.full(100, 3, np.int32),
+            "fesc_gsm": np.ones(100), "gross_sm": np.ones(100)}
+    for gal in (empty, dead):
+        for device in (False, True):
+            out = _deposit_gpu(step, D, hist0, [gal], [(0, 0.0, 0.0)], device)[0]
+            for k in ("stars", "weighted_sfr", "sfr"):
+                assert not out[k].any(), (k, device)
+            h = out["sfr_histories"]
+            assert np.array_equal(h[1:], hist0[:-1])
+            cells = h[0].reshape(D, D, -1)
+            assert not cells[:, :, :D].any()
+            assert np.array_equal(cells[:, :, D:], hist0[0].reshape(D, D, -1)[:, :, D:])
+    below = {"pos": np.array([[-w.params.box_size / D, 1.0, 1.0]], np.float32), "type": np.zeros(1, np.int32),
+             "fesc_gsm": np.ones(1), "gross_sm": np.ones(1)}
+    with pytest.raises(MxError) as e:
+        _deposit_gpu(step, D, hist0, [below], [(0, 0.0, 0.0)], False)
+    assert e.value.code == -1
+    ok = {"pos": np.array([[1.0, 1.0, 1.0]], np.float32), "type": np.zeros(1, np.int32),
+          "fesc_gsm": np.ones(1), "gross_sm": np.ones(1)}
+    out = _deposit_gpu(step, D, hist0, [ok], [(0, 0.0, 0.0)], False)[0]
+    assert out["stars"].sum() == np.float32(1.0)

@@ -108,3 +108,33 @@ def test_oracle_lightcone_matches_reference_fixture():
         orc.construct_lightcone(s, dT, prev, lc, lz)
     assert np.array_equal(lc, d["lightcone"]) and np.array_equal(lz, d["redshifts"])
     assert np.array_equal(prev, d["delta_T_prev"])
+
+
+def test_oracle_deposit_and_Mvir_crit_match_reference_fixture():
+    """construct_baryon_grids (two snapshots, without and with BH feedback)
+    and calculate_Mvir_crit restated == the reference's, bit for bit."""
+    import os
+    import sys
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden"))
+    from make_golden import DEPOSIT_BH, DEPOSIT_CASE, MVIR_SM
+
+    from cases import Case
+
+    d = np.load(os.path.join(here, "golden", "deposit16.npz"))
+    name, kind, D, over = DEPOSIT_CASE
+    w = Case(name, kind, D, over, fesc=0.01).workload()
+    orc = OracleBackend(w.params, w.redshifts, syn.TABLES_DIR)
+    npad = D * D * 2 * (D // 2 + 1)
+    st = {k: np.zeros(npad, np.float32).reshape(D, D, -1) for k in ("stars", "weighted_sfr", "sfr")}
+    st["sfr_histories"] = d["sfr_histories_init"].copy()
+    assert st["sfr_histories"].shape[0] == orc.n_sfr_histories
+    for s, bh in enumerate(DEPOSIT_BH):
+        gal = {k: d[f"gal{s}/{k}"] for k in ("pos", "type", "fesc_gsm", "gross_sm", "bhm", "ebhm")}
+        orc.construct_baryon_grids(s, gal, st, bh)
+        for k in ("stars", "weighted_sfr", "sfr", "sfr_histories"):
+            assert np.array_equal(st[k], d[f"out{s}/{k}"]), (s, k)
+    assert (d["out1/stars"] > 0).sum() > 1000
+    out = orc.calculate_Mvir_crit(10.0, MVIR_SM, d["J_21_at_ionization"], d["z_at_ionization"])
+    assert np.array_equal(out, d["Mvir_crit"]) and (out > 0).sum() > 1000
