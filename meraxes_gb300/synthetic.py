@@ -58,7 +58,7 @@ def gaussian_field(D: int, L: float, seed: int, sigma: float = 0.6) -> np.ndarra
     k_ny = np.pi * D / L
     with np.errstate(divide="ignore"):
         pk = np.where(k2 > 0, np.exp(-k2 / k_ny ** 2) / k2, 0.0)
-    field = np.fft.irfftn(fk * np.sqrt(pk), s=(D, D, D))
+    field = np.fft.irfftn(fk * np.sqrt(pk), s=(D, D, D), axes=(0, 1, 2))
     field *= sigma / field.std()
     return field
 

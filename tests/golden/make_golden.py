@@ -111,7 +111,7 @@ def make_lightcone(D: int = 16, L: float = 64.0, end_z: float = 8.6):
     print("lightcone16 written")
 
 
-DEPOSIT_CASE = ("dep16", "full_256", 16, {"reion_efficiency": 31043.3, "clumping_factor": 2.0})
+DEPOSIT_CASE = ("dep16", "evolve_512", 16, {"reion_efficiency": 31043.3, "clumping_factor": 2.0})
 DEPOSIT_BH = ((0, 0.0, 0.0), (1, 1e-5, 1.57))  # Flag_BHFeedback, BlackHoleMassLimitReion, ReionAlphaUVBH
 MVIR_SM = (0.049, 0.17, -2.1, 2.0, 2.5)  # ReionSMParam_m0, a, b, c, d
 

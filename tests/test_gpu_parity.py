@@ -345,7 +345,8 @@ def test_gpu_deposit_and_Mvir_crit_match_reference_fixture(device):
     assert np.array_equal(got > 0, ref > 0) and _within_one_ulp(got, ref)
 
 
-@pytest.mark.parametrize("D,n,base,clustered", [(64, 400000, "full_256", True), (48, 60000, "plain_64", False)])
+@pytest.mark.parametrize("D,n,base,clustered",
+                         [(64, 400000, "evolve_512", True), (48, 60000, "plain_64", False)])
 def test_gpu_deposit_matches_oracle(D, n, base, clustered, tables_dir):
     """Against the oracle at larger sizes; `clustered` puts 400k galaxies in
     1/64 of the box (about 100 per occupied cell: long float sums in galaxy
@@ -394,7 +395,7 @@ def test_gpu_deposit_edge_cases():
     from meraxes_gb300.api import ReionGridStep
 
     D = 16
-    w = Case("dep", "full_256", D, {}, fesc=0.01).workload()
+    w = Case("dep", "evolve_512", D, {}, fesc=0.01).workload()
     step = ReionGridStep(w.params, w.redshifts)
     nh = step.n_sfr_histories
     assert nh >= 2
