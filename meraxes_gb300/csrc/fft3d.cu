@@ -199,91 +199,140 @@ int fft_kernel_launches() { return fft_launches; }
 //      twiddle w_M^{n3 k2};
 //   C: per (column, k1, k2): DFT_R3 over n3, output k = k1 + R1 (k2 + R2 k3).
 // Every work item holds R points (R <= 8), so a block of 256 threads keeps
-// few registers and a 52 KB tile at D = 512, and four blocks fit an SM.
-constexpr int TXC = 8;  // columns per tile
+// few registers and a 64 KB tile at D = 512.
+//
+// Sixteen columns are 128 bytes: a half-warp moves one aligned 128-byte run
+// per access.  The spectra between the passes are stored with rows of
+// HP = D/2 + 1 rounded up to 16 complex values (272 at D = 512).  Every
+// x-pass store is then one whole aligned 128-byte line at a 1 MB stride.
+// Stores of that kind run at the HBM copy rate, whereas the unaligned
+// 64-byte runs of 257-value rows ran at a third of it.  Rows are also 128-byte
+// aligned for the y-pass and for the bulk copies of the z-pass.
+constexpr int TXC = 16;  // columns per tile
+
+// row pitch (complex values) of the spectra between the passes
+template <int D>
+struct Pitch
+{
+  static constexpr int H = D / 2 + 1;
+  static constexpr int HP = (H + TXC - 1) / TXC * TXC;
+};
 
 template <int D>
 struct Split3;
 template <>
 struct Split3<32>
 {
-  static constexpr int R1 = 4, R2 = 4, R3 = 2, PAD = 4;
+  static constexpr int R1 = 4, R2 = 4, R3 = 2;
 };
 template <>
 struct Split3<64>
 {
-  static constexpr int R1 = 4, R2 = 4, R3 = 4, PAD = 2;
+  static constexpr int R1 = 4, R2 = 4, R3 = 4;
 };
 template <>
 struct Split3<128>
 {
-  static constexpr int R1 = 8, R2 = 4, R3 = 4, PAD = 2;
+  static constexpr int R1 = 8, R2 = 4, R3 = 4;
 };
 template <>
 struct Split3<256>
 {
-  static constexpr int R1 = 8, R2 = 8, R3 = 4, PAD = 2;
+  static constexpr int R1 = 8, R2 = 8, R3 = 4;
 };
 template <>
 struct Split3<512>
 {
-  static constexpr int R1 = 8, R2 = 8, R3 = 8, PAD = 1;
+  static constexpr int R1 = 8, R2 = 8, R3 = 8;
 };
 
 template <int D>
 struct TilePlan
 {
   static constexpr int R1 = Split3<D>::R1, R2 = Split3<D>::R2, R3 = Split3<D>::R3, M = R2 * R3;
-  static constexpr int BUF = D * TXC + (D / 2) * Split3<D>::PAD;  // float2, padded
-  static constexpr int NT = (D / 2 + 1 + TXC - 1) / TXC;          // tiles over kz
+  static constexpr int BUF = D * TXC;         // float2
+  static constexpr int NT = Pitch<D>::HP / TXC;  // tiles over kz
   static_assert(R1 * R2 * R3 == D, "split");
-  // position of (line, column) in the padded tile: one pad slot per two lines
-  // keeps all three steps free of bank conflicts
-  static __device__ __forceinline__ int at(int line, int t) { return line * TXC + t + (line >> 1) * Split3<D>::PAD; }
+  // position of (line, column) in the tile: a half-warp always reads or
+  // writes the 16 columns of one line, 128 bytes over all 32 banks, so no
+  // padding is needed
+  static __device__ __forceinline__ int at(int line, int t) { return line * TXC + t; }
 };
 
 // Inverse DFT of the tile's columns.  load(n, t) returns input point n of
 // column t; store(k, t, v) takes output point k.  Ends without a barrier:
 // the caller synchronises before reusing buf.
+//
+// Thread roles are fixed: column t = tid % TXC and slot s = tid / TXC of
+// S = FFT_THREADS / TXC slots.  A half-warp is the 16 columns of one slot,
+// so every shared and global access of a half-warp is one 128-byte line.
+// Slot s takes the work items s, s + S, s + 2S, ... of each step; the loops
+// over them are unrolled, so their index arithmetic is constant offsets.
 template <int D, class Load, class Store>
 __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load load, Store store)
 {
   using P = TilePlan<D>;
   constexpr int R1 = P::R1, R2 = P::R2, R3 = P::R3, M = P::M;
-  for (int item = threadIdx.x; item < TXC * M; item += FFT_THREADS) {
-    const int t = item % TXC, np = item / TXC;
-    float2 v[R1];
+  constexpr int S = FFT_THREADS / TXC;
+  static_assert(S % R2 == 0 && S % R3 == 0, "slot split");
+  const int t = threadIdx.x % TXC, s = threadIdx.x / TXC;
+  float2* col = buf + t;
+  // step A: items n' = s + S j
 #pragma unroll
-    for (int n1 = 0; n1 < R1; n1++)
-      v[n1] = load(np + M * n1, t);
-    dft_bwd<R1>(v);
+  for (int j = 0; j < (M + S - 1) / S; j++) {
+    const int np = s + S * j;
+    if (M % S == 0 || np < M) {
+      float2 v[R1];
 #pragma unroll
-    for (int k1 = 0; k1 < R1; k1++)
-      buf[P::at(k1 * M + np, t)] = (k1 == 0 || np == 0) ? v[k1] : cmul(v[k1], tw[(np * k1) % D]);
+      for (int n1 = 0; n1 < R1; n1++)
+        v[n1] = load(np + M * n1, t);
+      dft_bwd<R1>(v);
+      col[np * TXC] = v[0];
+#pragma unroll
+      for (int k1 = 1; k1 < R1; k1++)
+        col[(k1 * M + np) * TXC] = cmul(v[k1], tw[(np * k1) & (D - 1)]);
+    }
   }
   __syncthreads();
-  for (int item = threadIdx.x; item < TXC * R1 * R3; item += FFT_THREADS) {
-    const int t = item % TXC, n3 = (item / TXC) % R3, k1 = item / (TXC * R3);
-    float2 v[R2];
+  // step B: items (n3, k1) with n3 = s % R3 fixed
+  {
+    const int n3 = s % R3;
 #pragma unroll
-    for (int n2 = 0; n2 < R2; n2++)
-      v[n2] = buf[P::at(k1 * M + n3 + R3 * n2, t)];
-    dft_bwd<R2>(v);
+    for (int j = 0; j < (R1 * R3 + S - 1) / S; j++) {
+      const int k1 = s / R3 + (S / R3) * j;
+      if ((R1 * R3) % S == 0 || k1 < R1) {
+        float2* line = col + (k1 * M + n3) * TXC;
+        float2 v[R2];
 #pragma unroll
-    for (int k2 = 0; k2 < R2; k2++)
-      buf[P::at(k1 * M + n3 + R3 * k2, t)] = (k2 == 0 || n3 == 0) ? v[k2] : cmul(v[k2], tw[(R1 * n3 * k2) % D]);
+        for (int n2 = 0; n2 < R2; n2++)
+          v[n2] = line[R3 * n2 * TXC];
+        dft_bwd<R2>(v);
+        line[0] = v[0];
+#pragma unroll
+        for (int k2 = 1; k2 < R2; k2++)
+          line[R3 * k2 * TXC] = cmul(v[k2], tw[(R1 * n3 * k2) & (D - 1)]);
+      }
+    }
   }
   __syncthreads();
-  for (int item = threadIdx.x; item < TXC * R1 * R2; item += FFT_THREADS) {
-    const int t = item % TXC, k2 = (item / TXC) % R2, k1 = item / (TXC * R2);
-    float2 v[R3];
+  // step C: items (k2, k1) with k2 = s % R2 fixed; output k = k1 + R1 (k2 + R2 k3)
+  {
+    const int k2 = s % R2;
 #pragma unroll
-    for (int n3 = 0; n3 < R3; n3++)
-      v[n3] = buf[P::at(k1 * M + n3 + R3 * k2, t)];
-    dft_bwd<R3>(v);
+    for (int j = 0; j < (R1 * R2 + S - 1) / S; j++) {
+      const int k1 = s / R2 + (S / R2) * j;
+      if ((R1 * R2) % S == 0 || k1 < R1) {
+        const float2* line = col + (k1 * M + R3 * k2) * TXC;
+        float2 v[R3];
 #pragma unroll
-    for (int k3 = 0; k3 < R3; k3++)
-      store(k1 + R1 * (k2 + R2 * k3), t, v[k3]);
+        for (int n3 = 0; n3 < R3; n3++)
+          v[n3] = line[n3 * TXC];
+        dft_bwd<R3>(v);
+#pragma unroll
+        for (int k3 = 0; k3 < R3; k3++)
+          store(k1 + R1 * (k2 + R2 * k3), t, v[k3]);
+      }
+    }
   }
 }
 
@@ -292,11 +341,12 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
 // fastest, so that the blocks of all radii of a tile run together and its
 // unfiltered columns are read from HBM once and from L2 by the others.  A
 // block computes the filter weights of its tile for its radius (shared by all
-// fields), then for every field loads the unfiltered columns, scales by 1/N,
-// multiplies by W(|k| R), inverse-DFTs along x and stores to
-// out[(r*G + g) * C + (x*D + ky)*H + kz].
+// fields), then for every field loads the unfiltered columns (rows of H),
+// scales by 1/N, multiplies by W(|k| R), inverse-DFTs along x and stores to
+// out[(r*G + g) * C + (x*D + ky)*HP + kz], all HP columns (those past H are
+// zero in, zero out).
 template <int D>
-__global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_x_filter(XPassArgs a)
+__global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_x_filter(XPassArgs a)
 {
   using P = TilePlan<D>;
   constexpr int H = D / 2 + 1;
@@ -311,8 +361,8 @@ __global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_x_filter(XPassArgs a)
   const int kz0 = (tile % P::NT) * TXC;
   const float kyv = kcomp(ky, D, a.delta_k);
   // filter weights of the tile times the 1/N scale (a power of two, so
-  // x * (scale * W) == (x * scale) * W exactly), wsm[kx * TXC + t]; a zeroed
-  // sharp-k mode is a weight of 0.  |kx| and |D - kx| share a weight.
+  // x * (scale * W) == (x * scale) * W exactly), wsm[|kx| * TXC + t] for
+  // |kx| = min(kx, D - kx) <= D/2; a zeroed sharp-k mode is a weight of 0.
   for (int i = threadIdx.x; i < (D / 2 + 1) * TXC; i += FFT_THREADS) {
     const int kx = i / TXC, t = i % TXC, kz = kz0 + t;
     float wv = 1.0f;
@@ -327,42 +377,40 @@ __global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_x_filter(XPassArgs a)
     }
     wv *= a.scale;
     wsm[i] = wv;
-    if (kx > 0 && kx < D / 2)
-      wsm[(D - kx) * TXC + t] = wv;
   }
   __syncthreads();
+  // this thread's column: kz = kz0 + t, the same in every step
+  const int t0 = threadIdx.x % TXC;
+  const bool live = kz0 + t0 < H;
+  const float* wcol = wsm + t0;
   for (int g = 0; g < a.G; g++) {
-    const float2* __restrict__ src = a.in[g];
-    float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C;
+    const float2* __restrict__ src = a.in[g] + (long long)ky * H + kz0 + t0;
+    float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C + (long long)ky * Pitch<D>::HP + kz0 + t0;
     tile_dft<D>(
       buf, tw,
-      [&](int kx, int t) {
-        const int kz = kz0 + t;
+      [&](int kx, int) {
         float2 x = make_float2(0.f, 0.f);
-        if (kz < H) {
-          x = src[((long long)kx * D + ky) * H + kz];
-          const float wv = wsm[kx * TXC + t];
+        if (live) {
+          x = src[(long long)kx * (D * H)];
+          const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
           x.x *= wv;
           x.y *= wv;
         }
         return x;
       },
-      [&](int x, int t, float2 v) {
-        const int kz = kz0 + t;
-        if (kz < H)
-          dst[((long long)x * D + ky) * H + kz] = v;
-      });
+      [&](int x, int, float2 v) { dst[(long long)x * (D * Pitch<D>::HP)] = v; });
     __syncthreads();
   }
 }
 
 // ------------------------------------------------------------------ y-pass
-// Grid: (spectrum, x, tile of TXC kz columns).  In-place inverse DFT along y.
+// Grid: (spectrum, x, tile of TXC kz columns).  In-place inverse DFT along y
+// over all HP columns of the pitch.
 template <int D>
-__global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_y(float2* data, long long C, int n_spectra)
+__global__ void __launch_bounds__(FFT_THREADS, 3) k_fft_y(float2* data, long long C, int n_spectra)
 {
   using P = TilePlan<D>;
-  constexpr int H = D / 2 + 1;
+  constexpr int HP = Pitch<D>::HP;
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* buf = smem + D;
@@ -372,24 +420,16 @@ __global__ void __launch_bounds__(FFT_THREADS, 4) k_fft_y(float2* data, long lon
   const int x = (int)((blk / P::NT) % D);
   const long long s = blk / ((long long)P::NT * D);
   const int kz0 = tile * TXC;
-  float2* plane = data + s * C + (long long)x * D * H;
+  float2* col = data + s * C + (long long)x * D * HP + kz0 + threadIdx.x % TXC;
   __syncthreads();
   tile_dft<D>(
-    buf, tw,
-    [&](int ky, int t) {
-      const int kz = kz0 + t;
-      return kz < H ? plane[(long long)ky * H + kz] : make_float2(0.f, 0.f);
-    },
-    [&](int y, int t, float2 v) {
-      const int kz = kz0 + t;
-      if (kz < H)
-        plane[(long long)y * H + kz] = v;
-    });
+    buf, tw, [&](int ky, int) { return col[ky * HP]; }, [&](int y, int, float2 v) { col[y * HP] = v; });
 }
 
 // ------------------------------------------------------------------ z-pass
 // The z-pass reads, per block, TZ consecutive rows (row = x * D + y) of every
-// spectrum of the batch: TZ*H contiguous complex values.  These row groups are
+// spectrum of the batch: TZ rows at the pitch HP, TZ*HP contiguous complex
+// values.  These row groups are
 // streamed into shared memory by bulk asynchronous copies (cp.async.bulk,
 // completion on an mbarrier) through a ZSTAGES-deep ring, so that the copies
 // of the next spectra are in flight while the current one is transformed.
@@ -506,7 +546,8 @@ struct ZPlan
   static constexpr int L1 = P1 / 4, L2 = P2 / 4;
   static constexpr int RS = P2 + ZS<D>::PAD;  // padded row of the transpose buffer
   static constexpr int BROW = P1 * RS;
-  static constexpr int STAGE = TZ * H;  // complex values per stage
+  static constexpr int HP = Pitch<D>::HP;
+  static constexpr int STAGE = TZ * HP;  // complex values per stage
   static constexpr int BUF = TZ * BROW;
   static constexpr size_t OFF_STAGE = 64;  // after the barriers
   static constexpr size_t OFF_BUF = OFF_STAGE + sizeof(float2) * (size_t)ZSTAGES * STAGE;
@@ -617,7 +658,7 @@ __device__ __forceinline__ void z_issue(char* smem, const float2* spectra, long 
   using P = ZPlan<D>;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   float2* st = reinterpret_cast<float2*>(smem + P::OFF_STAGE) + (size_t)(it % ZSTAGES) * P::STAGE;
-  bulk_load(st, spectra + (long long)it * C + row0 * P::H, (unsigned)(sizeof(float2) * P::STAGE),
+  bulk_load(st, spectra + (long long)it * C + row0 * P::HP, (unsigned)(sizeof(float2) * P::STAGE),
             &bars[it % ZSTAGES]);
 }
 
@@ -639,7 +680,7 @@ __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const flo
   {
     // step A: row t, column n2, lane-part l of the P1-point DFT over n1
     const int l = threadIdx.x % L1, n2 = (threadIdx.x / L1) % P2, t = threadIdx.x / (L1 * P2);
-    const float2* row = st + t * H;
+    const float2* row = st + t * P::HP;
     float2 v[4];
     float2 tk = w.kb;
 #pragma unroll
@@ -900,6 +941,8 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_store(const float2* sp
 // ----------------------------------------------------------------- launch
 bool fft3d_supported(int D) { return D == 32 || D == 64 || D == 128 || D == 256 || D == 512; }
 
+int fft_pitch(int D) { return (D / 2 + 1 + TXC - 1) / TXC * TXC; }
+
 template <int D>
 constexpr size_t smem_y()
 {
@@ -908,7 +951,7 @@ constexpr size_t smem_y()
 template <int D>
 constexpr size_t smem_x()
 {
-  return smem_y<D>() + sizeof(float) * (size_t)D * TXC;
+  return smem_y<D>() + sizeof(float) * (size_t)(D / 2 + 1) * TXC;
 }
 
 template <int D>

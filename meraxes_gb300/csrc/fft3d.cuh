@@ -14,7 +14,7 @@ struct XPassArgs
   int G;                          // fields
   int n;                          // radii in the batch
   float2* out;                    // spectrum (r*G + g) at out + (r*G + g)*C
-  long long C;
+  long long C;                    // D * D * fft_pitch(D)
   float R[MAX_RADII];
   int apply[MAX_RADII];
   int filter_type;
@@ -47,6 +47,9 @@ struct ZThresholdArgs
 };
 
 bool fft3d_supported(int D);
+// Row pitch (complex values) of the spectra between the fused passes: D/2 + 1
+// rounded up to whole 128-byte lines.  A batch spectrum holds D * D * pitch.
+int fft_pitch(int D);
 bool launch_fft_x_filter(int D, const XPassArgs& a, cudaStream_t s);
 bool launch_fft_y(int D, float2* data, long long C, int n_spectra, cudaStream_t s);
 bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s);

@@ -80,8 +80,9 @@ struct mx_ctx
 
   // scratch
   float2* d_unf = nullptr;      // MAX_FIELDS x C
-  float2* d_work = nullptr;     // batch x C
+  float2* d_work = nullptr;     // batch x work_C
   long long work_fields = 0;    // capacity in spectra
+  long long work_C = 0;         // complex values per batch spectrum: D*D*fft_pitch(D) fused, C otherwise
   float2** d_in_ptrs = nullptr; // device array of MAX_FIELDS pointers
   // light cone (Initialise_ConstructLightcone / ConstructLightcone state)
   long long lc_length = -1, lc_pos = 0;
@@ -204,7 +205,8 @@ void mx_ctx::alloc_scratch()
   const std::vector<double> radii = filter_radii(p);
   size_t free_b = 0, total_b = 0;
   MX_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  const double spectrum = (double)sizeof(float2) * gd.C;
+  work_C = fused_fft ? (long long)gd.D * gd.D * fft_pitch(gd.D) : gd.C;
+  const double spectrum = (double)sizeof(float2) * work_C;
   const long long want = (long long)radii.size() * G;
   long long fit = (long long)(0.45 * (double)free_b / spectrum);
   if (const char* env = std::getenv("MX_MAX_BATCH_SPECTRA"))
@@ -378,7 +380,7 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
         xa.G = G;
         xa.n = nf;
         xa.out = c->d_work;
-        xa.C = gd.C;
+        xa.C = c->work_C;
         for (int r = 0; r < nf; r++) {
           xa.R[r] = (float)radii[r0 + r];
           xa.apply[r] = 1;
@@ -391,11 +393,11 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
           launch_fft_x_filter(gd.D, xa, s);
         }
         Prof pr(c, "fft_y", 2.0 * G * nf * B8C, s);
-        launch_fft_y(gd.D, c->d_work, gd.C, nf * G, s);
+        launch_fft_y(gd.D, c->d_work, c->work_C, nf * G, s);
       }
       ZThresholdArgs za;
       za.spectra = c->d_work;
-      za.C = gd.C;
+      za.C = c->work_C;
       za.G = G;
       za.idx_xe = idx_xe;
       za.idx_nr = idx_nr;
@@ -739,7 +741,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
             xa.G = 1;
             xa.n = nb;
             xa.out = c->d_work;
-            xa.C = gd.C;
+            xa.C = c->work_C;
             for (int q = 0; q < nb; q++) {
               xa.R[q] = (float)sp.R[q0 + q];
               xa.apply[q] = 1;
@@ -753,11 +755,11 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
             }
             {
               Prof pr(c, "fft_y", 16.0 * (double)gd.C * nb, s);
-              launch_fft_y(gd.D, c->d_work, gd.C, nb, s);
+              launch_fft_y(gd.D, c->d_work, c->work_C, nb, s);
             }
             {
               Prof pr(c, "fft_z_store", (8.0 * (double)gd.C + 4.0 * (double)gd.N) * nb, s);
-              launch_fft_z_store(gd.D, c->d_work, gd.C, nb, q0, c->d_shells, gd.N, c->d_err, s);
+              launch_fft_z_store(gd.D, c->d_work, c->work_C, nb, q0, c->d_shells, gd.N, c->d_err, s);
             }
             q0 += nb;
             continue;
