@@ -16,16 +16,19 @@
 //            chip, or the clamped store of ComputeTs shells.
 //
 // The x- and y-passes run a three-step Cooley-Tukey transform over a tile of
-// 8 columns (radix-8 or radix-4 DFTs in registers with compile-time twiddles,
-// inter-step twiddles from a shared table filled with sincospi, transposes
-// through a padded shared tile).  The z-pass computes each row's C2R as a
+// 16 columns (radix-8 or radix-4 DFTs in registers with compile-time
+// twiddles, inter-step twiddles from a shared table filled with sincospi,
+// transposes through the shared tile).  The z-pass computes each row's C2R as a
 // half-length complex transform split over 4-lane groups (see below).
 #include <cmath>
 #include <cstdint>
 
+#include "bulk.cuh"
 #include "fft3d.cuh"
 
 namespace mx {
+
+using namespace bulk;
 
 // Compile-time cos and sin of 2 pi j / n, by Taylor series on [-pi, pi] (30
 // terms; the truncation error is far below double rounding).  Used only to
@@ -435,70 +438,6 @@ __global__ void __launch_bounds__(FFT_THREADS, 3) k_fft_y(float2* data, long lon
 // of the next spectra are in flight while the current one is transformed.
 namespace {
 constexpr int ZSTAGES = 4;
-constexpr unsigned ERR_PIPELINE_TIMEOUT = 2u;
-constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;  // 2 s
-constexpr long long WAIT_LIMIT_ITERS = 1LL << 26;
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
-{
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_init_fence()
-{
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-// Arms the barrier for `bytes` and issues one bulk copy global -> shared.
-// dst, src and bytes are multiples of 16.
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar)
-{
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-  asm volatile(
-    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
-    "l"(src), "r"(bytes), "r"(smem_addr(bar))
-    : "memory");
-}
-
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned parity)
-{
-  uint32_t ok;
-  asm volatile(
-    "{\n\t.reg .pred p;\n\t"
-    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-    "selp.u32 %0, 1, 0, p;\n\t}"
-    : "=r"(ok)
-    : "r"(smem_addr(bar)), "r"(parity)
-    : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ unsigned long long global_ns()
-{
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Waits for phase `parity` of the barrier; false after about WAIT_LIMIT_NS.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
-{
-  if (mbar_test(bar, parity))
-    return true;
-  const unsigned long long t0 = global_ns();
-  for (long long it = 1; it < WAIT_LIMIT_ITERS; it++) {
-    if (mbar_test(bar, parity))
-      return true;
-    if ((it & 255) == 0 && global_ns() - t0 > WAIT_LIMIT_NS)
-      return false;
-  }
-  return false;
-}
-
 // Geometry of the z-pass.  A block of 256 threads owns TZ = 2048 / D rows
 // (2048 cells, 8 per thread).  Each row's C2R of D points is computed as one
 // complex inverse DFT of D/2 points: with w = exp(2 pi i / D),

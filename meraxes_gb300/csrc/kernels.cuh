@@ -164,7 +164,8 @@ struct EvolveArgs
   float* TS;            // REAL
   const TsDevConst* cst;  // device copy
   double* partials;       // RED_BLOCKS x 4 (J_alpha, xalpha, Xheat, Xion)
-  unsigned int* err;      // error word (iteration cap)
+  unsigned int* err;      // error word: bit 1 iteration cap, bit 2 a shell-copy wait timed out
+  int n_shells;           // S of *cst (sizes the shared-memory shell ring)
 };
 void launch_evolve(const EvolveArgs& a, const GridDims& gd, cudaStream_t s);
 

@@ -10,6 +10,7 @@
 // stop after the same iteration as the reference).
 #include <cmath>
 
+#include "bulk.cuh"
 #include "kernels.cuh"
 
 namespace mx {
@@ -46,6 +47,11 @@ __device__ void block_sum_store(double (&v)[NV], double* partials)
     partials[(long long)blockIdx.x * NV + threadIdx.x] = s;
   }
 }
+
+// floats of the frequency tables at the start of the evolve kernel's shared
+// memory (one float4 per x_HII node and shell), whole 16-byte units for the
+// shell ring behind them
+__host__ __device__ constexpr int ev_tables_floats(int S) { return 4 * NXHII * S; }
 
 __device__ __forceinline__ long long pad_index(long long ir, int D, int H)
 {
@@ -90,7 +96,7 @@ __device__ double kappa_d(const TsDevConst& c, int which, double T)
   return exp(ans);
 }
 
-__device__ float get_Ts_d(const TsDevConst& c, float z, float delta, float TK, float xe, float Jalpha, float* xalpha,
+__device__ __noinline__ float get_Ts_d(const TsDevConst& c, float z, float delta, float TK, float xe, float Jalpha, float* xalpha,
                           unsigned int* err)
 {
   const double zd = z, TKd = TK, dd = delta, xd = xe;
@@ -224,31 +230,67 @@ __device__ bool get_Ts_f(const TsDevConst& c, float delta, float TK, float xe, f
 }
 }  // namespace
 
-__global__ void k_evolve_f32(EvolveArgs a, int D, int H, long long N)
+// Per-cell update.  A block owns tiles of EV_TILE consecutive cells (one per
+// thread), tile k at cell (blockIdx.x + k gridDim.x) EV_TILE.  The 40 shell
+// values of a tile (40 rows of EV_TILE floats, one per shell) are streamed
+// into shared memory by bulk copies through a two-stage ring, so the shell
+// reads do not depend on how many loads each thread keeps in flight; the next
+// tile's copies run while the current tile is computed.
+constexpr int EV_TILE = RED_THREADS;
+
+__device__ __forceinline__ void ev_issue(uint64_t* bars, float* stages, const float* shells, int S, long long N,
+                                         long long tile, int k)
+{
+  const long long c0 = tile * EV_TILE;
+  const int n = (int)((N - c0) < EV_TILE ? (N - c0) : EV_TILE);
+  float* st = stages + (size_t)(k & 1) * S * EV_TILE;
+  uint64_t* bar = &bars[k & 1];
+  bulk::mbar_arm(bar, (unsigned)(sizeof(float) * n * S));
+  for (int r = 0; r < S; r++)
+    bulk::bulk_copy(st + r * EV_TILE, shells + (long long)r * N + c0, (unsigned)(sizeof(float) * n), bar);
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_evolve_f32(EvolveArgs a, int D, int H, long long N)
 {
   const TsDevConst& c = *a.cst;
   const int S = c.S;
-  // scaled frequency tables and coefficients staged in shared memory
-  extern __shared__ float sm[];
-  float* s_tab = sm;                      // 3 * 14 * S
-  float* s_K = sm + 3 * NXHII * S;        // 4 * S
-  for (int i = threadIdx.x; i < 3 * NXHII * S; i += blockDim.x) {
-    const int t = i / (NXHII * S), rem = i % (NXHII * S);
-    s_tab[i] = c.ftab[t][rem / S][rem % S];
+  // frequency tables times the shell coefficients, P[x][r] = (K_H tab_H,
+  // K_I tab_I, K_L tab_L, K_S) at node x of the x_HII table, then the shell
+  // ring.  The interpolation in x_HII is linear, so a cell's sums are
+  // (1 - w) sum_r shell_r P[lo][r] + w sum_r shell_r P[hi][r].
+  extern __shared__ __align__(16) float sm[];
+  float4* s_P = reinterpret_cast<float4*>(sm);  // NXHII * S
+  float* stages = sm + ev_tables_floats(S);     // 2 * S * EV_TILE
+  __shared__ uint64_t bars[2];
+  for (int i = threadIdx.x; i < NXHII * S; i += blockDim.x) {
+    const int x = i / S, r = i % S;
+    s_P[i] = make_float4(c.fKH[r] * c.ftab[0][x][r], c.fKI[r] * c.ftab[1][x][r], c.fKL[r] * c.ftab[2][x][r],
+                         c.fKS[r]);
   }
-  for (int i = threadIdx.x; i < S; i += blockDim.x) {
-    s_K[i] = c.fKH[i];
-    s_K[S + i] = c.fKI[i];
-    s_K[2 * S + i] = c.fKL[i];
-    s_K[3 * S + i] = c.fKS[i];
+  const long long ntiles = (N + EV_TILE - 1) / EV_TILE;
+  const int my_tiles = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  const bool light = !c.no_light;
+  if (threadIdx.x == 0 && light) {
+    bulk::mbar_init(&bars[0], 1);
+    bulk::mbar_init(&bars[1], 1);
+    bulk::mbar_init_fence();
   }
   __syncthreads();
+  if (threadIdx.x == 0 && light)
+    for (int k = 0; k < 2 && k < my_tiles; k++)
+      ev_issue(bars, stages, a.shells, S, N, blockIdx.x + (long long)k * gridDim.x, k);
   double acc[4] = { 0, 0, 0, 0 };
-  for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long ip = pad_index(ir, D, H);
-    const float delta = a.deltax[ip];
-    float xe = a.x_e_prev[ip];
-    float T = a.Tk[ir];
+  for (int k = 0; k < my_tiles; k++) {
+    const long long tile = blockIdx.x + (long long)k * gridDim.x;
+    const long long ir = tile * EV_TILE + threadIdx.x;
+    const bool valid = ir < N;
+    const long long ip = valid ? pad_index(ir, D, H) : 0;
+    float delta = 0.f, xe = 0.f, T = 1.f;
+    if (valid) {
+      delta = a.deltax[ip];
+      xe = a.x_e_prev[ip];
+      T = a.Tk[ir];
+    }
     // interpolation bracket in x_HII (ComputeTs.c:761-773)
     float xcall = xe;
     if (xcall > c.xhii[NXHII - 1] * 0.999f)
@@ -256,27 +298,48 @@ __global__ void k_evolve_f32(EvolveArgs a, int D, int H, long long N)
     else if (xcall < c.xhii[0])
       xcall = 1.001f * c.xhii[0];
     int lo = NXHII - 1;
-    while (xcall < c.xhii[lo])
+    while (lo > 0 && xcall < c.xhii[lo])
       lo--;
     const int hi = lo + 1;
     const float w = (xcall - c.xhii[lo]) / (c.xhii[hi] - c.xhii[lo]);
     float heat = 0.f, ion = 0.f, lya = 0.f, star = 0.f;
-    if (!c.no_light) {
-      const float* tH = s_tab;
-      const float* tI = s_tab + NXHII * S;
-      const float* tL = s_tab + 2 * NXHII * S;
+    if (light) {
+      const bool arrived = bulk::mbar_wait(&bars[k & 1], (unsigned)(k >> 1) & 1u);
+      if (__syncthreads_or(!arrived)) {
+        if (threadIdx.x == 0) {
+          atomicOr(a.err, bulk::ERR_PIPELINE_TIMEOUT);
+          // copies of tiles k and k + 1 may still be in flight
+          for (int j = k; j < my_tiles && j < k + 2; j++)
+            bulk::mbar_wait(&bars[j & 1], (unsigned)(j >> 1) & 1u);
+        }
+        return;
+      }
+      const float* st = stages + (size_t)(k & 1) * S * EV_TILE + threadIdx.x;
+      const float4* Plo = s_P + lo * S;
+      const float4* Phi = s_P + hi * S;
+      float hl = 0.f, il = 0.f, ll = 0.f, hh = 0.f, ih = 0.f, lh = 0.f;
 #pragma unroll 4
       for (int r = 0; r < S; r++) {
-        const float sf = a.shells[(long long)r * N + ir];
-        const float fh = fmaf(w, tH[hi * S + r] - tH[lo * S + r], tH[lo * S + r]);
-        const float fi = fmaf(w, tI[hi * S + r] - tI[lo * S + r], tI[lo * S + r]);
-        const float fl = fmaf(w, tL[hi * S + r] - tL[lo * S + r], tL[lo * S + r]);
-        heat = fmaf(sf * s_K[r], fh, heat);
-        ion = fmaf(sf * s_K[S + r], fi, ion);
-        lya = fmaf(sf * s_K[2 * S + r], fl, lya);
-        star = fmaf(sf, s_K[3 * S + r], star);
+        const float sf = st[r * EV_TILE];
+        const float4 pl = Plo[r], ph = Phi[r];
+        hl = fmaf(sf, pl.x, hl);
+        il = fmaf(sf, pl.y, il);
+        ll = fmaf(sf, pl.z, ll);
+        star = fmaf(sf, pl.w, star);
+        hh = fmaf(sf, ph.x, hh);
+        ih = fmaf(sf, ph.y, ih);
+        lh = fmaf(sf, ph.z, lh);
       }
+      heat = fmaf(w, hh - hl, hl);
+      ion = fmaf(w, ih - il, il);
+      lya = fmaf(w, lh - ll, ll);
+      // every thread has read stage k & 1: refill it with tile k + 2
+      __syncthreads();
+      if (threadIdx.x == 0 && k + 2 < my_tiles)
+        ev_issue(bars, stages, a.shells, S, N, tile + 2LL * gridDim.x, k + 2);
     }
+    if (!valid)
+      continue;
     const float opd = 1.0f + delta;
     const float dxheat_dzp = heat / (1.0f + xe);
     const float dxe_dzp = ion - c.fksink * alpha_A_f(T) * xe * xe * opd;
@@ -314,7 +377,8 @@ __global__ void k_evolve_f32(EvolveArgs a, int D, int H, long long N)
 
 void launch_evolve(const EvolveArgs& a, const GridDims& gd, cudaStream_t s)
 {
-  const size_t smem = (3 * NXHII + 4) * MAX_SHELLS * sizeof(float);
+  const size_t smem = sizeof(float) * (ev_tables_floats(a.n_shells) + 2 * (size_t)a.n_shells * EV_TILE);
+  cudaFuncSetAttribute(k_evolve_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_evolve_f32<<<RED_BLOCKS, RED_THREADS, smem, s>>>(a, gd.D, gd.H, gd.N);
   ts_launches++;
 }

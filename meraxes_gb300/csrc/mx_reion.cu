@@ -833,6 +833,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     ea.cst = c->d_tsc;
     ea.partials = c->d_partials;
     ea.err = c->d_err;
+    ea.n_shells = S;
     {
       Prof pr(c, "k_evolve", ((double)S + 6.0) * 4.0 * (double)gd.N, s);
       launch_evolve(ea, gd, s);
@@ -862,7 +863,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
   MX_CUDA(cudaStreamSynchronize(s));
   if (errw) {
     MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
-    throw CudaError{ MX_ECUDA, (errw & 2u) ? "ComputeTs: a transform pipeline wait timed out"
+    throw CudaError{ MX_ECUDA, (errw & 2u) ? "ComputeTs: a pipeline wait (transform or shell copies) timed out"
                                            : "ComputeTs: spin-temperature iteration did not converge" };
   }
   if (out) {
