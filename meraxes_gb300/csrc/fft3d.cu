@@ -490,7 +490,9 @@ struct ZPlan
   static constexpr int BUF = TZ * BROW;
   static constexpr size_t OFF_STAGE = 64;  // after the barriers
   static constexpr size_t OFF_BUF = OFF_STAGE + sizeof(float2) * (size_t)ZSTAGES * STAGE;
-  static constexpr size_t BYTES = OFF_BUF + sizeof(float2) * 2 * (size_t)BUF;
+  static constexpr size_t OFF_XS = OFF_BUF + sizeof(float2) * 2 * (size_t)BUF;
+  static constexpr int XS_WARP = 4 * 33;  // float2 of lane-transpose scratch per warp
+  static constexpr size_t BYTES = OFF_XS + sizeof(float2) * (size_t)XS_WARP * (FFT_THREADS / 32);
   static_assert(P1 * P2 == DH, "split");
   static_assert(TZ * P2 * L1 == FFT_THREADS && TZ * P1 * L2 == FFT_THREADS, "one lane-part per thread");
   static_assert((sizeof(float2) * STAGE) % 16 == 0, "bulk copy size");
@@ -544,11 +546,32 @@ __device__ __forceinline__ void cross_lane(float2 (&u)[4], int l)
   }
 }
 
+// The 4-lane step of cross_lane<4> through the warp's shared scratch xs
+// (4 rows of 33 float2): lane l of 4-lane group g writes slot c at
+// xs[33 c + 4 g + l] and reads slot m from xs[33 l + 4 g + m].  Both are one
+// conflict-free pass over the banks (the row pad of one float2 separates the
+// four lanes of a group); eight memory operations replace three rounds of
+// shuffles and selects.
+__device__ __forceinline__ void cross_lane4_smem(float2 (&u)[4], float2* xs)
+{
+  const int lane = threadIdx.x & 31;
+  const int g4 = lane & ~3, l = lane & 3;
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+    xs[33 * c + lane] = u[c];
+  __syncwarp();
+#pragma unroll
+  for (int m = 0; m < 4; m++)
+    u[m] = xs[33 * l + g4 + m];
+  dft4_bwd(u);
+}
+
 // One 4-point lane-part of a P-point DFT whose 4 points (stride L = P/4) are
 // in v: 4-point DFT, twiddles exp(2 pi i l c / P) = w1^c (w1 = exp(2 pi i l /
-// P)), cross-lane step.
+// P)), cross-lane step (through the warp scratch xs for 4 lanes).
 template <int P>
-__device__ __forceinline__ void lane_dft(float2 (&v)[4], int l, float2 w1)
+__device__ __forceinline__ void lane_dft(float2 (&v)[4], int l, float2 w1, float2* xs)
 {
   dft4_bwd(v);
   if (P > 4) {
@@ -557,7 +580,10 @@ __device__ __forceinline__ void lane_dft(float2 (&v)[4], int l, float2 w1)
     v[2] = cmul(v[2], w2);
     v[3] = cmul(v[3], cmul(w2, w1));
   }
-  cross_lane<P / 4>(v, l);
+  if constexpr (P / 4 == 4)
+    cross_lane4_smem(v, xs);
+  else
+    cross_lane<P / 4>(v, l);
 }
 
 __device__ __forceinline__ float2 unit(int j, int n)
@@ -615,6 +641,7 @@ __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const flo
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   const float2* st = reinterpret_cast<const float2*>(smem + P::OFF_STAGE) + (size_t)(it % ZSTAGES) * P::STAGE;
   float2* buf = reinterpret_cast<float2*>(smem + P::OFF_BUF) + (size_t)(it & 1) * P::BUF;
+  float2* xs = reinterpret_cast<float2*>(smem + P::OFF_XS) + (threadIdx.x / 32) * P::XS_WARP;
   const bool arrived = mbar_wait(&bars[it % ZSTAGES], (unsigned)(it / ZSTAGES) & 1u);
   {
     // step A: row t, column n2, lane-part l of the P1-point DFT over n1
@@ -638,7 +665,7 @@ __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const flo
       if (i < 3)
         tk = cmul(tk, w.kr);
     }
-    lane_dft<P1>(v, l, w.la);
+    lane_dft<P1>(v, l, w.la, xs);
     float2 tf = w.fb;
 #pragma unroll
     for (int e = 0; e < 4; e++) {
@@ -658,7 +685,7 @@ __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const flo
 #pragma unroll
     for (int i = 0; i < 4; i++)
       z[i] = buf[t * P::BROW + k1 * P::RS + l + L2 * i];
-    lane_dft<P2>(z, l, w.lb);
+    lane_dft<P2>(z, l, w.lb, xs);
   }
   return true;
 }
