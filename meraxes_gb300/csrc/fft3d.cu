@@ -267,16 +267,16 @@ struct TilePlan
 // the caller synchronises before reusing buf.
 //
 // Thread roles are fixed: column t = tid % TXC and slot s = tid / TXC of
-// S = FFT_THREADS / TXC slots.  A half-warp is the 16 columns of one slot,
+// S = NTHR / TXC slots (NTHR threads in the block).  A half-warp is the 16 columns of one slot,
 // so every shared and global access of a half-warp is one 128-byte line.
 // Slot s takes the work items s, s + S, s + 2S, ... of each step; the loops
 // over them are unrolled, so their index arithmetic is constant offsets.
-template <int D, class Load, class Store>
+template <int D, int NTHR, class Load, class Store>
 __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load load, Store store)
 {
   using P = TilePlan<D>;
   constexpr int R1 = P::R1, R2 = P::R2, R3 = P::R3, M = P::M;
-  constexpr int S = FFT_THREADS / TXC;
+  constexpr int S = NTHR / TXC;
   static_assert(S % R2 == 0 && S % R3 == 0, "slot split");
   const int t = threadIdx.x % TXC, s = threadIdx.x / TXC;
   float2* col = buf + t;
@@ -348,8 +348,9 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
 // scales by 1/N, multiplies by W(|k| R), inverse-DFTs along x and stores to
 // out[(r*G + g) * C + (x*D + ky)*HP + kz], all HP columns (those past H are
 // zero in, zero out).
+constexpr int XTHREADS = 512;
 template <int D>
-__global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_x_filter(XPassArgs a)
+__global__ void __launch_bounds__(XTHREADS, 2) k_fft_x_filter(XPassArgs a)
 {
   using P = TilePlan<D>;
   constexpr int H = D / 2 + 1;
@@ -366,7 +367,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_x_filter(XPassArgs a)
   // filter weights of the tile times the 1/N scale (a power of two, so
   // x * (scale * W) == (x * scale) * W exactly), wsm[|kx| * TXC + t] for
   // |kx| = min(kx, D - kx) <= D/2; a zeroed sharp-k mode is a weight of 0.
-  for (int i = threadIdx.x; i < (D / 2 + 1) * TXC; i += FFT_THREADS) {
+  for (int i = threadIdx.x; i < (D / 2 + 1) * TXC; i += XTHREADS) {
     const int kx = i / TXC, t = i % TXC, kz = kz0 + t;
     float wv = 1.0f;
     if (a.apply[r]) {
@@ -389,7 +390,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_x_filter(XPassArgs a)
   for (int g = 0; g < a.G; g++) {
     const float2* __restrict__ src = a.in[g] + (long long)ky * H + kz0 + t0;
     float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C + (long long)ky * Pitch<D>::HP + kz0 + t0;
-    tile_dft<D>(
+    tile_dft<D, XTHREADS>(
       buf, tw,
       [&](int kx, int) {
         float2 x = make_float2(0.f, 0.f);
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 3) k_fft_y(float2* data, long lon
   const int kz0 = tile * TXC;
   float2* col = data + s * C + (long long)x * D * HP + kz0 + threadIdx.x % TXC;
   __syncthreads();
-  tile_dft<D>(
+  tile_dft<D, FFT_THREADS>(
     buf, tw, [&](int ky, int) { return col[ky * HP]; }, [&](int y, int, float2 v) { col[y * HP] = v; });
 }
 
@@ -925,7 +926,7 @@ static void launch_x(const XPassArgs& a, cudaStream_t s)
 {
   cudaFuncSetAttribute(k_fft_x_filter<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x<D>());
   const long long blocks = (long long)D * TilePlan<D>::NT * a.n;
-  k_fft_x_filter<D><<<(unsigned)blocks, FFT_THREADS, smem_x<D>(), s>>>(a);
+  k_fft_x_filter<D><<<(unsigned)blocks, XTHREADS, smem_x<D>(), s>>>(a);
 }
 template <int D>
 static void launch_y(float2* data, long long C, int n_spectra, cudaStream_t s)
