@@ -572,14 +572,13 @@ __device__ __forceinline__ void cross_lane4_smem(float2 (&u)[4], float2* xs)
 // in v: 4-point DFT, twiddles exp(2 pi i l c / P) = w1^c (w1 = exp(2 pi i l /
 // P)), cross-lane step (through the warp scratch xs for 4 lanes).
 template <int P>
-__device__ __forceinline__ void lane_dft(float2 (&v)[4], int l, float2 w1, float2* xs)
+__device__ __forceinline__ void lane_dft(float2 (&v)[4], int l, const float2 (&w)[3], float2* xs)
 {
   dft4_bwd(v);
   if (P > 4) {
-    const float2 w2 = cmul(w1, w1);
-    v[1] = cmul(v[1], w1);
-    v[2] = cmul(v[2], w2);
-    v[3] = cmul(v[3], cmul(w2, w1));
+    v[1] = cmul(v[1], w[0]);
+    v[2] = cmul(v[2], w[1]);
+    v[3] = cmul(v[3], w[2]);
   }
   if constexpr (P / 4 == 4)
     cross_lane4_smem(v, xs);
@@ -602,7 +601,7 @@ struct ZTw
 {
   float2 kb, kr;  // w_D^k for the 4 points: kb * kr^i
   float2 fb, fs;  // four-step w_{D/2}^{n2 k1} for slot e: fb * fs^e
-  float2 la, lb;  // lane twiddles of steps A and B
+  float2 la[3], lb[3];  // lane twiddles w, w^2, w^3 of steps A and B
   __device__ __forceinline__ void init()
   {
     constexpr int P1 = ZS<D>::P1, P2 = ZS<D>::P2, L1 = P1 / 4, L2 = P2 / 4, DH = D / 2;
@@ -612,8 +611,12 @@ struct ZTw
     const int k10 = lane_out(L1, 0, l), dk1 = lane_out(L1, 1, l) - k10;
     fb = unit((n2 * k10) % DH, DH);
     fs = unit((n2 * dk1) % DH, DH);
-    la = unit(l, P1);
-    lb = unit(threadIdx.x % L2, P2);
+    const int l2 = threadIdx.x % L2;
+#pragma unroll
+    for (int c = 1; c <= 3; c++) {
+      la[c - 1] = unit((l * c) % P1, P1);
+      lb[c - 1] = unit((l2 * c) % P2, P2);
+    }
   }
 };
 
@@ -655,7 +658,7 @@ __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const flo
       const int k = n2 + P2 * (l + L1 * i);
       float2 A = row[k];
       float2 B = row[DH - k];
-      if (k == 0) {
+      if (i == 0 && k == 0) {
         A.y = 0.0f;  // imaginary parts of kz = 0 and kz = D/2 are ignored
         B.y = 0.0f;
       }
@@ -738,14 +741,20 @@ constexpr int ST_RB_SHIFT = 8;       // radius index of the last ionising radius
 // ionising radius.  J_21, Gamma12, z_at_ionization and J_21_at_ionization
 // change at most once per cell per launch (at the first crossing) and are
 // stored when that happens; xH and r_bubble are stored at the end.
-template <int D>
+//
+// SPIN and RECOMB fix the fields at compile time: deltax, stars,
+// weighted_sfr, then x_e with the spin temperature, then N_rec with
+// recombinations (the order find_HII_bubbles transforms them in).
+template <int D, bool SPIN, bool RECOMB>
 __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdArgs a)
 {
   using P = ZPlan<D>;
+  constexpr int G = 3 + (SPIN ? 1 : 0) + (RECOMB ? 1 : 0);
+  constexpr int IXE = 3, INR = SPIN ? 4 : 3;
   extern __shared__ __align__(128) unsigned char zsmem[];
   char* smem = reinterpret_cast<char*>(zsmem);
   const long long row0 = (long long)blockIdx.x * P::TZ;
-  const int n_items = a.n_f * a.G;
+  const int n_items = a.n_f * G;
   z_setup<D>(smem, a.spectra, a.C, row0, n_items);
   ZTw<D> w;
   w.init();
@@ -769,34 +778,31 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
   for (int r = 0; r < a.n_r; r++) {
     const RadiusParams rp = a.rp[r];
     const bool direct = rp.last != 0;
-    float2 f[MAX_FIELDS][4];
+    float2 f[G][4];
     if (!direct) {
 #pragma unroll
-      for (int g = 0; g < MAX_FIELDS; g++) {
-        if (g < a.G) {
-          if (!z_c2r<D>(smem, it, n_items, a.spectra, a.C, row0, w, f[g])) {
-            z_abort<D>(smem, it, n_items, a.err);
-            return;
-          }
-          it++;
+      for (int g = 0; g < G; g++) {
+        if (!z_c2r<D>(smem, it, n_items, a.spectra, a.C, row0, w, f[g])) {
+          z_abort<D>(smem, it, n_items, a.err);
+          return;
         }
+        it++;
       }
     } else {
 #pragma unroll
-      for (int g = 0; g < MAX_FIELDS; g++)
-        if (g < a.G)
+      for (int g = 0; g < G; g++)
 #pragma unroll
-          for (int e = 0; e < 4; e++)
-            f[g][e] = *reinterpret_cast<const float2*>(a.direct[g] + rowc * 2LL * P::H + zc[e]);
+        for (int e = 0; e < 4; e++)
+          f[g][e] = *reinterpret_cast<const float2*>(a.direct[g] + rowc * 2LL * P::H + zc[e]);
     }
 #pragma unroll
     for (int c = 0; c < 8; c++) {
       const int e = c >> 1;
       const bool hi = c & 1;
-      float fv[MAX_FIELDS];
+      float fv[G];
 #pragma unroll
-      for (int g = 0; g < MAX_FIELDS; g++)
-        fv[g] = g < a.G ? (hi ? f[g][e].y : f[g][e].x) : 0.0f;
+      for (int g = 0; g < G; g++)
+        fv[g] = hi ? f[g][e].y : f[g][e].x;
       const float dx = fmaxf(fv[0], -1 + REL_TOL_F);
       float stv = fmaxf(fv[1], 0.0f);
       if (stv < ABS_TOL_F)
@@ -805,14 +811,14 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
       if (ws < ABS_TOL_F)
         ws = 0;
       float nr = 0.0f, xe = 0.0f;
-      if (a.recomb) {
-        nr = a.idx_nr == 3 ? fv[3] : fv[4];
+      if constexpr (RECOMB) {
+        nr = fv[INR];
         nr = fmaxf(nr, 0.0f);
         if (nr < ABS_TOL_F)
           nr = 0;
       }
-      if (a.spin) {
-        xe = a.idx_xe == 3 ? fv[3] : fv[4];
+      if constexpr (SPIN) {
+        xe = fv[IXE];
         xe = fmaxf(xe, 0.0f);
         if (xe < ABS_TOL_F)
           xe = 0;
@@ -831,8 +837,8 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
         xpart = nf_f - lhs_f;
       } else {
         const double dom = 1.0 + (double)dx;
-        const double rec = a.recomb ? (double)nr / dom : 0.0;
-        const double nf = a.spin ? 1.0 - (double)xe : 1.0;
+        const double rec = RECOMB ? (double)nr / dom : 0.0;
+        const double nf = SPIN ? 1.0 - (double)xe : 1.0;
         const double f_coll = (double)stv / (rp.M_mean * dom) * (4.0 / 3.0) * PI_D * rp.R_cubed / a.pixel_volume;
         ionised = f_coll * a.eff > nf * (1. + rec);
         xpart = (float)__dsub_rn(nf, __dmul_rn(f_coll, a.eff));
@@ -846,7 +852,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
         if (xr_high) {
           if (a.uvb)
             a.J21[ir] = J21_aux;
-          if (a.recomb)
+          if (RECOMB)
             a.Gamma12[ir] = ws * rp.kg;
         }
         s = (s & ((1u << ST_RB_SHIFT) - 1)) | ST_ION | ((unsigned)r << ST_RB_SHIFT);
@@ -935,12 +941,20 @@ static void launch_y(float2* data, long long C, int n_spectra, cudaStream_t s)
   cudaFuncSetAttribute(k_fft_y<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y<D>());
   k_fft_y<D><<<(unsigned)blocks, FFT_THREADS, smem_y<D>(), s>>>(data, C, n_spectra);
 }
+template <int D, bool SPIN, bool RECOMB>
+static void launch_zt_cfg(const ZThresholdArgs& a, cudaStream_t s)
+{
+  const size_t bytes = ZPlan<D>::BYTES;
+  cudaFuncSetAttribute(k_fft_z_threshold<D, SPIN, RECOMB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_fft_z_threshold<D, SPIN, RECOMB><<<D * D / ZPlan<D>::TZ, FFT_THREADS, bytes, s>>>(a);
+}
 template <int D>
 static void launch_zt(const ZThresholdArgs& a, cudaStream_t s)
 {
-  const size_t bytes = ZPlan<D>::BYTES;
-  cudaFuncSetAttribute(k_fft_z_threshold<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  k_fft_z_threshold<D><<<D * D / ZPlan<D>::TZ, FFT_THREADS, bytes, s>>>(a);
+  if (a.spin)
+    a.recomb ? launch_zt_cfg<D, true, true>(a, s) : launch_zt_cfg<D, true, false>(a, s);
+  else
+    a.recomb ? launch_zt_cfg<D, false, true>(a, s) : launch_zt_cfg<D, false, false>(a, s);
 }
 template <int D>
 static void launch_zs(const float2* spectra, long long C, int n, int r0, float* shells, long long N, unsigned* err,
@@ -997,6 +1011,10 @@ bool launch_fft_y(int D, float2* data, long long C, int n_spectra, cudaStream_t 
 
 bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s)
 {
+  // the kernel's fixed field order
+  if (a.G != 3 + (a.spin ? 1 : 0) + (a.recomb ? 1 : 0) || a.idx_xe != (a.spin ? 3 : -1) ||
+      a.idx_nr != (a.recomb ? (a.spin ? 4 : 3) : -1))
+    return false;
   switch (D) {
     case 32: launch_zt<32>(a, s); break;
     case 64: launch_zt<64>(a, s); break;

@@ -28,7 +28,7 @@ struct ZThresholdArgs
 {
   const float2* spectra;  // batch spectra after the x and y passes
   long long C;
-  int G, idx_xe, idx_nr;
+  int G, idx_xe, idx_nr;  // fields deltax, stars, weighted_sfr, [x_e if spin], [N_rec if recomb]
   int n_r;  // radii of the batch
   int n_f;  // of which filtered (spectra r*G + g for r < n_f); a last radius
             // with rp.last set reads the input grids directly

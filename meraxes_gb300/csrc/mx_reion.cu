@@ -425,7 +425,8 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
       // J_21_at_ionization, Gamma12 written) counted with the first batch
       Prof pr(c, "fft_z_threshold",
               (double)G * nf * B8C + (double)(nb - nf) * G * B4N + (r0 == 0 ? 8.0 * B4N : 0.0), s);
-      launch_fft_z_threshold(gd.D, za, s);
+      if (!launch_fft_z_threshold(gd.D, za, s))
+        throw CudaError{ MX_ECUDA, "find_HII_bubbles: field layout does not match the fused z-pass" };
       continue;
     }
     FilterBatch fb;
