@@ -494,6 +494,7 @@ struct ZPlan
   static constexpr size_t OFF_XS = OFF_BUF + sizeof(float2) * 2 * (size_t)BUF;
   static constexpr int XS_WARP = 4 * 33;  // float2 of lane-transpose scratch per warp
   static constexpr size_t BYTES = OFF_XS + sizeof(float2) * (size_t)XS_WARP * (FFT_THREADS / 32);
+  static constexpr size_t BYTES_NO_XS = OFF_XS;  // shuffles instead of the warp scratch
   static_assert(P1 * P2 == DH, "split");
   static_assert(TZ * P2 * L1 == FFT_THREADS && TZ * P1 * L2 == FFT_THREADS, "one lane-part per thread");
   static_assert((sizeof(float2) * STAGE) % 16 == 0, "bulk copy size");
@@ -571,7 +572,7 @@ __device__ __forceinline__ void cross_lane4_smem(float2 (&u)[4], float2* xs)
 // One 4-point lane-part of a P-point DFT whose 4 points (stride L = P/4) are
 // in v: 4-point DFT, twiddles exp(2 pi i l c / P) = w1^c (w1 = exp(2 pi i l /
 // P)), cross-lane step (through the warp scratch xs for 4 lanes).
-template <int P>
+template <int P, bool XS>
 __device__ __forceinline__ void lane_dft(float2 (&v)[4], int l, const float2 (&w)[3], float2* xs)
 {
   dft4_bwd(v);
@@ -580,7 +581,7 @@ __device__ __forceinline__ void lane_dft(float2 (&v)[4], int l, const float2 (&w
     v[2] = cmul(v[2], w[1]);
     v[3] = cmul(v[3], w[2]);
   }
-  if constexpr (P / 4 == 4)
+  if constexpr (P / 4 == 4 && XS)
     cross_lane4_smem(v, xs);
   else
     cross_lane<P / 4>(v, l);
@@ -636,7 +637,7 @@ __device__ __forceinline__ void z_issue(char* smem, const float2* spectra, long 
 // m = k1 + P1 * lane_out(L2, e, l), k1 = (threadIdx.x / L2) % P1,
 // l = threadIdx.x % L2.  Returns false (for every thread) if the copy did not
 // arrive.  One block barrier per call: the transpose buffer alternates.
-template <int D>
+template <int D, bool XS>
 __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const float2* spectra, long long C,
                                       long long row0, const ZTw<D>& w, float2 (&z)[4])
 {
@@ -669,7 +670,7 @@ __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const flo
       if (i < 3)
         tk = cmul(tk, w.kr);
     }
-    lane_dft<P1>(v, l, w.la, xs);
+    lane_dft<P1, XS>(v, l, w.la, xs);
     float2 tf = w.fb;
 #pragma unroll
     for (int e = 0; e < 4; e++) {
@@ -689,7 +690,7 @@ __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const flo
 #pragma unroll
     for (int i = 0; i < 4; i++)
       z[i] = buf[t * P::BROW + k1 * P::RS + l + L2 * i];
-    lane_dft<P2>(z, l, w.lb, xs);
+    lane_dft<P2, XS>(z, l, w.lb, xs);
   }
   return true;
 }
@@ -782,7 +783,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
     if (!direct) {
 #pragma unroll
       for (int g = 0; g < G; g++) {
-        if (!z_c2r<D>(smem, it, n_items, a.spectra, a.C, row0, w, f[g])) {
+        if (!z_c2r<D, true>(smem, it, n_items, a.spectra, a.C, row0, w, f[g])) {
           z_abort<D>(smem, it, n_items, a.err);
           return;
         }
@@ -898,7 +899,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_store(const float2* sp
   const long long base = (row0 + t) * D;
   for (int r = 0; r < n; r++) {
     float2 z[4];
-    if (!z_c2r<D>(smem, r, n, spectra, C, row0, w, z)) {
+    if (!z_c2r<D, false>(smem, r, n, spectra, C, row0, w, z)) {
       z_abort<D>(smem, r, n, err);
       return;
     }
@@ -960,7 +961,7 @@ template <int D>
 static void launch_zs(const float2* spectra, long long C, int n, int r0, float* shells, long long N, unsigned* err,
                       cudaStream_t s)
 {
-  const size_t bytes = ZPlan<D>::BYTES;
+  const size_t bytes = ZPlan<D>::BYTES_NO_XS;
   cudaFuncSetAttribute(k_fft_z_store<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   k_fft_z_store<D><<<D * D / ZPlan<D>::TZ, FFT_THREADS, bytes, s>>>(spectra, C, n, r0, shells, N, err);
 }
