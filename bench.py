@@ -38,18 +38,23 @@ UNIT = "ms/snapshot"
 REION_EFF = 1.0 / 0.15714 * 4000.0 / (1.0 - 0.75 * 0.24)
 FESC = 0.01
 # DRAM bytes (read + write) per algorithmic byte of each kernel, from one ncu
-# capture per kernel of the same workload at 256^3 (10 spectra per batch):
-# `ncu --set full -k regex:<kernel> -s 1 -c 1` on
-# `python bench.py --grid 256 --steps 1 --warmup 1 --no-cpu --no-e2e` with
+# capture of the same workload at 256^3 (profiles/*_256.md):
+# `ncu --set full -k regex:"k_fft_x_filter|k_fft_y|k_fft_z_threshold|k_fft_z_store|k_evolve_f32" -s 10 -c 7`
+# on `python bench.py --grid 256 --steps 1 --warmup 1 --no-cpu --no-e2e` with
 # MX_MAX_BATCH_SPECTRA=10.  Each kernel's DRAM traffic grows in proportion to
 # the spectra (or cells) it processes, so traffic per launch at 512^3 is this
-# ratio times the launch's algorithmic bytes.
+# ratio times the launch's algorithmic bytes.  The transforms also move the
+# row padding of the batch spectra (rows of 144 complex values for 129 at
+# 256^3, 272 for 257 at 512^3): PAD_512_OVER_256 rescales that share.
+_C256, _N256 = 256 * 256 * 129, 256 ** 3
+PAD_512_OVER_256 = (272 / 257) / (144 / 129)
 DRAM_PER_ALGORITHMIC = {
-    "fft_x_filter": 690.67e6 / (8 * 256 * 256 * 129 * 10),   # TS launch, 1 field, 9 radii
-    "fft_y": 1296.72e6 / (16 * 256 * 256 * 129 * 10),        # 10 spectra
-    "fft_z_threshold": 813.95e6 / (8 * 256 * 256 * 129 * 10 + 2 * 4 * 256 ** 3),  # 10 spectra + xH, z_at_ion reads
-    "fft_z_store": 1301.92e6 / ((8 * 256 * 256 * 129 + 4 * 256 ** 3) * 10),
-    "k_evolve": 3084.37e6 / (46 * 4 * 256 ** 3),
+    # find_HII_bubbles launch: 5 fields x 2 radii (5 unfiltered spectra read, 10 written)
+    "fft_x_filter": 1040.73e6 / (8 * _C256 * 5 * (1 + 2)) * PAD_512_OVER_256,
+    "fft_y": 1298.69e6 / (16 * _C256 * 9) * PAD_512_OVER_256,                      # 9 spectra
+    "fft_z_threshold": 892.79e6 / (8 * _C256 * 10 + 2 * 4 * _N256) * PAD_512_OVER_256,  # 10 spectra + xH, z_at_ion
+    "fft_z_store": 1236.80e6 / ((8 * _C256 + 4 * _N256) * 9),                       # 9 shells
+    "k_evolve": 3084.0e6 / (46 * 4 * _N256),
 }
 
 
