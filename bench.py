@@ -377,8 +377,12 @@ def run_e2e(args, step, w, fields, used, n_hist, device, world):
         h = torch.zeros((n_hist, D * D * 2 * (D // 2 + 1)), dtype=torch.float32).pin_memory()
         h[0] = fields[s]["sfr"].reshape(-1).cpu()
         host["sfr_histories"] = h.numpy()
-    in_names = ["deltax", "stars", "weighted_sfr", "x_e_box", "N_rec", "z_at_ionization", "J_21_at_ionization",
+    # mx_step uploads each input once; x_e_box is not uploaded when ComputeTs
+    # runs (it writes x_e_box on the device before find_HII_bubbles reads it)
+    in_names = ["deltax", "stars", "weighted_sfr", "N_rec", "z_at_ionization", "J_21_at_ionization",
                 "Gamma12", "sfr", "x_e_box_prev", "Tk_box"]
+    if not p.flag_spin_temp:
+        in_names.append("x_e_box")
     out_names = ["N_rec", "xH", "z_at_ionization", "r_bubble", "J_21", "J_21_at_ionization", "Gamma12", "sfr",
                  "x_e_box", "x_e_box_prev", "Tk_box", "TS_box", "delta_T"]
     nb = lambda n: host[n].nbytes  # noqa: E731

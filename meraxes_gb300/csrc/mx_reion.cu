@@ -67,6 +67,8 @@ struct mx_ctx
   int n_hist = 0;
   double stored_fcoll[1000];
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host-pointer mx_step: copies that overlap the compute
+  cudaEvent_t ev_a = nullptr, ev_b = nullptr;
   int device = 0;
   int nthreads = 4;
   // inverse transforms: fused three-pass kernels for power-of-two grids
@@ -190,6 +192,12 @@ mx_ctx::~mx_ctx()
   cudaFree(d_rr_c);
   for (void* q : mirror_allocs)
     cudaFree(q);
+  if (ev_a)
+    cudaEventDestroy(ev_a);
+  if (ev_b)
+    cudaEventDestroy(ev_b);
+  if (copy_stream)
+    cudaStreamDestroy(copy_stream);
   if (stream)
     cudaStreamDestroy(stream);
 }
@@ -1616,6 +1624,9 @@ int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out)
     if (cudaGetDevice(&c->device) != cudaSuccess)
       throw CudaError{ MX_ECUDA, "no CUDA device" };
     MX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    MX_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    MX_CUDA(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
+    MX_CUDA(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
     if (p.filter_type != 0 && p.filter_type != 1 && p.filter_type != 2)
       throw CudaError{ MX_EINVAL, "invalid filter type" };
     if (p.flag_spin_temp) {
@@ -1917,6 +1928,16 @@ int mx_ComputeBrightnessTemperatureBox(mx_ctx* ctx, int32_t snapshot, const mx_g
   });
 }
 
+// mx_step on host grids.  The grids cross in three groups so that the copies
+// overlap the compute of the other stages:
+//   1. ComputeTs inputs (and the SFR histories), on the compute stream;
+//   2. find_HII_bubbles inputs that ComputeTs does not touch, on the copy
+//      stream while ComputeTs runs; find_HII_bubbles waits for them;
+//   3. ComputeTs outputs (final once it ends: find_HII_bubbles and the 21cm
+//      box only read them), back on the copy stream while find_HII_bubbles
+//      runs; the find_HII_bubbles outputs and delta_T at the end.
+// x_e_box is not uploaded when ComputeTs runs: it writes x_e_box before
+// find_HII_bubbles reads it.  Each grid crosses at most once per direction.
 int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out)
 {
   return guarded(ctx, [&]() {
@@ -1924,33 +1945,60 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
     if (!host)
       throw CudaError{ MX_EINVAL, "NULL grids" };
     ctx->ensure_mirror();
-    cudaStream_t s = ctx->stream;
-    // union of the inputs of the three stages
-    std::vector<FieldIO> all = fhb_fields();
-    if (ctx->p.flag_spin_temp)
-      for (const FieldIO& f : ts_fields())
-        all.push_back(f);
-    if (ctx->p.flag_21cm)
-      all.push_back({ &mx_grids::vel, true, IN | OUT });  // peculiar-velocity modes only
-    copy_fields(ctx, host, all, IN, s);
-    if (ctx->p.flag_spin_temp)
+    cudaStream_t s = ctx->stream, cs = ctx->copy_stream;
+    const bool spin = ctx->p.flag_spin_temp != 0, b21 = ctx->p.flag_21cm != 0;
+    auto has = [](const std::vector<FieldIO>& v, float* mx_grids::*m) {
+      for (const FieldIO& f : v)
+        if (f.member == m)
+          return true;
+      return false;
+    };
+    std::vector<FieldIO> ts_in, fhb_in, ts_out, late_out;
+    if (spin) {
+      for (const FieldIO& f : ts_fields()) {
+        if (f.dir & IN)
+          ts_in.push_back({ f.member, f.padded, IN });
+        if (f.dir & OUT)
+          ts_out.push_back({ f.member, f.padded, OUT });
+      }
+    }
+    for (const FieldIO& f : fhb_fields()) {
+      if ((f.dir & IN) && !has(ts_in, f.member) && !(spin && has(ts_out, f.member)))
+        fhb_in.push_back({ f.member, f.padded, IN });
+      if ((f.dir & OUT) && !has(ts_out, f.member))
+        late_out.push_back({ f.member, f.padded, OUT });
+    }
+    if (b21) {
+      fhb_in.push_back({ &mx_grids::vel, true, IN });  // peculiar-velocity modes only
+      late_out.push_back({ &mx_grids::vel, true, OUT });
+      late_out.push_back({ &mx_grids::delta_T, false, OUT });
+    }
+    // the copy stream starts after the compute stream's earlier work
+    MX_CUDA(cudaEventRecord(ctx->ev_a, s));
+    MX_CUDA(cudaStreamWaitEvent(cs, ctx->ev_a, 0));
+    copy_fields(ctx, host, ts_in, IN, s);
+    if (spin)
       copy_histories(ctx, host, s);
+    copy_fields(ctx, host, fhb_in, IN, cs);
+    MX_CUDA(cudaEventRecord(ctx->ev_b, cs));
     mx_grids m = mirror_for(ctx, host);
     int launches = 0;
-    if (ctx->p.flag_spin_temp) {
+    if (spin) {
       run_ComputeTs(ctx, snapshot, &m, out, s);
       launches += out ? out->gpu_launches : 0;
+      MX_CUDA(cudaEventRecord(ctx->ev_a, s));
+      MX_CUDA(cudaStreamWaitEvent(cs, ctx->ev_a, 0));
+      copy_fields(ctx, host, ts_out, OUT, cs);
     }
+    MX_CUDA(cudaStreamWaitEvent(s, ctx->ev_b, 0));
     run_find_HII_bubbles(ctx, snapshot, &m, out, s);
     launches += out ? out->gpu_launches : 0;
-    if (ctx->p.flag_21cm) {
+    if (b21) {
       run_delta_T(ctx, snapshot, &m, out, s);
       launches += out ? out->gpu_launches : 0;
     }
-    std::vector<FieldIO> outs = all;
-    if (ctx->p.flag_21cm)
-      outs.push_back({ &mx_grids::delta_T, false, OUT });
-    copy_fields(ctx, host, outs, OUT, s);
+    copy_fields(ctx, host, late_out, OUT, s);
+    MX_CUDA(cudaStreamSynchronize(cs));
     MX_CUDA(cudaStreamSynchronize(s));
     if (out)
       out->gpu_launches = launches;
