@@ -330,7 +330,56 @@ int mx_calculate_Mvir_crit_device(mx_ctx* ctx,
                                   float* Mvir_crit,
                                   void* stream);
 
-/* Build information: returns a static string. */
+/* ---------------------------------------------------------------------------
+ * Differentiation (no counterpart in the reference's C code: the gradients of
+ * a 21 cm power-spectrum loss through ComputeTs and the 21cm box, with the
+ * ionisation flags of find_HII_bubbles held fixed).
+ *
+ * mx_set_xray_params sets LXrayGal and NuXrayGalThreshold (E0, eV) for the
+ * following calls (the parameters a gradient is taken for).
+ *
+ * mx_ps_loss_device: L = sum_b (P_b - target_b)^2 over nbins bins
+ * [edges[b], edges[b+1]) (1/Mpc, host arrays, increasing, edges[0] > 0) of
+ * the power spectrum of f = delta_T * V / N (V = (BoxSize/h)^3), where
+ * P_b = sum k^3 |F_k|^2 / (2 pi^2 V) / n_b over the half-spectrum modes of the
+ * bin, each counted once (the binning of Compute_PS,
+ * ComputePowerSpectrum.c:160-215).  Writes *loss, P[nbins] (host, may be
+ * NULL) and, if grad_delta_T is not NULL, dL/d(delta_T) (device, REAL).
+ *
+ * mx_adjoint_device: the adjoint of ComputeTs (ComputeTs.c:78-1045, one
+ * snapshot, not the homogeneous branch) and of the 21cm box without peculiar
+ * velocities (BrightnessTemperature.c:495-545), given dL/d(delta_T).  `saved`
+ * holds device grids of the forward step: deltax, stars (as find_HII_bubbles
+ * read them), sfr (before ComputeTs reweighted it), sfr_histories,
+ * x_e_box_prev and Tk_box (the state before the step), x_e_box, xH and TS_box
+ * (after the step).  The 40 shells are recomputed, not stored.  xH enters
+ * through the partial ionisation of the last, unfiltered step
+ * (find_HII_bubbles.c:416-428) where 0 < xH < 1; the flags are fixed.
+ * Outputs (device): grad_sfr (PADDED), grad_stars (PADDED), and grad_params
+ * (host, 2 doubles) = {dL/dLXrayGal, dL/dNuXrayGalThreshold}.  The E0
+ * derivative of the frequency tables is a central difference (relative step
+ * 1e-3) of the host-built tables.
+ * ------------------------------------------------------------------------- */
+int mx_set_xray_params(mx_ctx* ctx, double lx_gal, double nu_xray_gal_threshold);
+int mx_ps_loss_device(mx_ctx* ctx,
+                      const float* delta_T,
+                      int32_t nbins,
+                      const float* edges,
+                      const float* target,
+                      double* loss,
+                      float* P,
+                      float* grad_delta_T,
+                      void* stream);
+int mx_adjoint_device(mx_ctx* ctx,
+                      int32_t snapshot,
+                      const mx_grids* saved,
+                      const float* grad_delta_T,
+                      float* grad_sfr,
+                      float* grad_stars,
+                      double* grad_params,
+                      void* stream);
+
+/* Build information: returns a static string. *//* Build information: returns a static string. */
 const char* mx_build_info(void);
 
 /* Brightness-temperature box without any device allocation.  No counterpart

@@ -26,7 +26,7 @@ EXPORTS = [
     "mx_brightness_temperature_noalloc", "mx_ps_length", "mx_Compute_PS", "mx_Compute_PS_device",
     "mx_lightcone_init", "mx_ConstructLightcone", "mx_ConstructLightcone_device",
     "mx_construct_baryon_grids", "mx_construct_baryon_grids_device", "mx_calculate_Mvir_crit",
-    "mx_calculate_Mvir_crit_device",
+    "mx_calculate_Mvir_crit_device", "mx_set_xray_params", "mx_ps_loss_device", "mx_adjoint_device",
 ]
 
 
@@ -112,5 +112,14 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mx_calculate_Mvir_crit.restype = ctypes.c_int
         L.mx_calculate_Mvir_crit_device.argtypes = mvir + [P]
         L.mx_calculate_Mvir_crit_device.restype = ctypes.c_int
+        L.mx_set_xray_params.argtypes = [P, ctypes.c_double, ctypes.c_double]
+        L.mx_set_xray_params.restype = ctypes.c_int
+        L.mx_ps_loss_device.argtypes = [P, P, ctypes.c_int32, ctypes.POINTER(ctypes.c_float),
+                                        ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_float), P, P]
+        L.mx_ps_loss_device.restype = ctypes.c_int
+        L.mx_adjoint_device.argtypes = [P, ctypes.c_int32, ctypes.POINTER(MxGrids), P, P, P,
+                                        ctypes.POINTER(ctypes.c_double), P]
+        L.mx_adjoint_device.restype = ctypes.c_int
         _LIB = L
         return L

@@ -253,3 +253,42 @@ class ReionGridStep:
                     raise ValueError("need C-contiguous float32 numpy arrays")
             rc = self.lib.mx_calculate_Mvir_crit(self.ctx, redshift, sm, *[a.ctypes.data for a in arrays])
         self._check(rc)
+
+    # ------------------------------------------------------- differentiation
+    def set_xray(self, lx_gal: float, nu_xray_gal_threshold: float):
+        """LXrayGal and NuXrayGalThreshold (E0, eV) for the following calls."""
+        self._check(self.lib.mx_set_xray_params(self.ctx, float(lx_gal), float(nu_xray_gal_threshold)))
+        self.params.lx_gal = float(lx_gal)
+        self.params.nu_xray_gal_threshold = float(nu_xray_gal_threshold)
+
+    def ps_loss(self, delta_T, edges, target, grad: bool = True):
+        """Binned power-spectrum loss of a REAL delta_T CUDA tensor (see
+        mx_ps_loss_device): (loss, P per bin, dL/d(delta_T) or None)."""
+        import torch
+
+        nb = len(target)
+        e = (ctypes.c_float * (nb + 1))(*[float(v) for v in edges])
+        t = (ctypes.c_float * nb)(*[float(v) for v in target])
+        loss = ctypes.c_double()
+        P = (ctypes.c_float * nb)()
+        g = torch.empty_like(delta_T) if grad else None
+        stream = torch.cuda.current_stream().cuda_stream
+        self._check(self.lib.mx_ps_loss_device(self.ctx, delta_T.data_ptr(), nb, e, t, ctypes.byref(loss), P,
+                                               g.data_ptr() if grad else None, ctypes.c_void_p(stream)))
+        return loss.value, list(P), g
+
+    def adjoint(self, snapshot: int, saved, grad_delta_T):
+        """Adjoint of ComputeTs + the 21cm box (see mx_adjoint_device) on CUDA
+        tensors: (dL/dsfr, dL/dstars, dL/dLXrayGal, dL/dE0)."""
+        import torch
+
+        g, device = self._grids(saved)
+        if not device:
+            raise ValueError("adjoint: device grids only")
+        gs = torch.zeros_like(saved["sfr"])
+        gst = torch.zeros_like(saved["stars"])
+        par = (ctypes.c_double * 2)()
+        stream = torch.cuda.current_stream().cuda_stream
+        self._check(self.lib.mx_adjoint_device(self.ctx, snapshot, ctypes.byref(g), grad_delta_T.data_ptr(),
+                                               gs.data_ptr(), gst.data_ptr(), par, ctypes.c_void_p(stream)))
+        return gs, gst, par[0], par[1]

@@ -912,10 +912,40 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_store(const float2* sp
   }
 }
 
+// ------------------------------------------------- adjoint filter (k-space)
+// acc = (first ? 0 : acc) + W(|k| R) * scale * U over a half spectrum [D][D][D/2+1]
+// with the weights of the x-pass (the filtered shells are a real, symmetric
+// convolution, so their adjoint is the same filter).
+__global__ void k_filter_accumulate(float2* __restrict__ acc, const float2* __restrict__ U, int D, float R,
+                                    int filter_type, float delta_k, float scale, float sharpk_max, int first)
+{
+  const int H = D / 2 + 1;
+  const long long n = (long long)D * D * H;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int kz = (int)(i % H);
+    const long long row = i / H;
+    const int kx = (int)(row / D), ky = (int)(row % D);
+    const float kxv = kcomp(kx, D, delta_k), kyv = kcomp(ky, D, delta_k);
+    const float kzv = __fmul_rn((float)kz, delta_k);
+    const float kmag = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(kyv, kyv)), __fmul_rn(kzv, kzv)));
+    bool zero = false;
+    float wv = filter_weight(filter_type, kmag, R, sharpk_max, &zero);
+    if (zero)
+      wv = 0.0f;
+    wv *= scale;
+    const float2 u = U[i];
+    float2 v = first ? make_float2(0.f, 0.f) : acc[i];
+    v.x += u.x * wv;
+    v.y += u.y * wv;
+    acc[i] = v;
+  }
+}
+
 // ----------------------------------------------------------------- launch
 bool fft3d_supported(int D) { return D == 32 || D == 64 || D == 128 || D == 256 || D == 512; }
 
 int fft_pitch(int D) { return (D / 2 + 1 + TXC - 1) / TXC * TXC; }
+
 
 template <int D>
 constexpr size_t smem_y()
@@ -977,6 +1007,14 @@ static float sharpk_threshold()
   while ((float)((double)std::nextafter(x, INFINITY) * c) <= 1.0f)
     x = std::nextafter(x, INFINITY);
   return x;
+}
+
+void launch_filter_accumulate(int D, float2* acc, const float2* U, float R, int filter_type, float delta_k,
+                              float scale, bool first, cudaStream_t s)
+{
+  static const float kmax = sharpk_threshold();
+  k_filter_accumulate<<<RED_BLOCKS, RED_THREADS, 0, s>>>(acc, U, D, R, filter_type, delta_k, scale, kmax, first ? 1 : 0);
+  fft_launches++;
 }
 
 bool launch_fft_x_filter(int D, const XPassArgs& args, cudaStream_t s)

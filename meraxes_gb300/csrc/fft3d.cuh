@@ -50,6 +50,10 @@ bool fft3d_supported(int D);
 // Row pitch (complex values) of the spectra between the fused passes: D/2 + 1
 // rounded up to whole 128-byte lines.  A batch spectrum holds D * D * pitch.
 int fft_pitch(int D);
+// acc = (first ? 0 : acc) + W(|k| R) * scale * U on a half spectrum (any D);
+// the filter of the x-pass
+void launch_filter_accumulate(int D, float2* acc, const float2* U, float R, int filter_type, float delta_k,
+                              float scale, bool first, cudaStream_t s);
 bool launch_fft_x_filter(int D, const XPassArgs& a, cudaStream_t s);
 bool launch_fft_y(int D, float2* data, long long C, int n_spectra, cudaStream_t s);
 bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s);

@@ -70,6 +70,31 @@ __device__ __forceinline__ long long pad_of(long long ir, int D, int H)
 
 }  // namespace
 
+// grad_sfr (PADDED) += alpha_half * (v (PADDED, may be NULL) + u0 (REAL, may be
+// NULL)) at the cells; alpha_half = a_first for padded indices below D*D*(D/2+1)
+// (the half of the array the SFR-history scalings touch), else a_second.
+__global__ void k_adjoint_axpy(float* __restrict__ grad, const float* __restrict__ v, const float* __restrict__ u0,
+                               float a_first, float a_second, int D, int H, long long N, long long C)
+{
+  for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
+    const long long row = ir / D;
+    const long long ip = row * 2LL * H + (ir - row * D);
+    float x = 0.0f;
+    if (v)
+      x += v[ip];
+    if (u0)
+      x += u0[ir];
+    grad[ip] += (ip < C ? a_first : a_second) * x;
+  }
+}
+
+void launch_adjoint_axpy(float* grad, const float* v, const float* u0, float a_first, float a_second,
+                         const GridDims& gd, cudaStream_t s)
+{
+  k_adjoint_axpy<<<RED_BLOCKS, RED_THREADS, 0, s>>>(grad, v, u0, a_first, a_second, gd.D, gd.H, gd.N, gd.C);
+  g_launches++;
+}
+
 int kernel_launch_count()
 {
   return g_launches + ts_kernel_launches() + fft_kernel_launches() + ps_kernel_launches() + pecvel_kernel_launches() +

@@ -169,6 +169,34 @@ struct EvolveArgs
 };
 void launch_evolve(const EvolveArgs& a, const GridDims& gd, cudaStream_t s);
 
+// Adjoint of the per-cell spin-temperature update and of the 21cm box.
+struct AdjointArgs
+{
+  float* shells;          // S x N: shell values in, dL/d(shell) out
+  const float* deltax;    // PADDED
+  const float* x_e_prev;  // PADDED, state before the step
+  const float* Tk;        // REAL, state before the step
+  const float* x_e_new;   // PADDED, x_e after the step (x_e_box)
+  const float* stars;     // PADDED, as find_HII_bubbles read it
+  const float* xH;        // REAL, after the step
+  const float* TS;        // REAL, after the step
+  const float* grad_dT;   // REAL, dL/d(delta_T)
+  float* grad_stars;      // PADDED, dL/d(stars) at the cells (padding untouched)
+  const TsDevConst* cst;
+  const float4* dP_dE0;   // 14 x S: d/dE0 of (K_H tab_H, K_I tab_I, K_L tab_L, -)
+  float dT_factor;        // 21cm box constant
+  float dT_trad;          // T_CMB (1 + z) of the 21cm box
+  float kfc_last;         // f_coll * eff = stars * kfc_last / (1 + dx) at the last step
+  double* partials;       // RED_BLOCKS x 2: L_X and E0 terms
+  unsigned int* err;
+  int n_shells;
+};
+void launch_evolve_adjoint(const AdjointArgs& a, const GridDims& gd, cudaStream_t s);
+// grad (PADDED) += alpha * (v (PADDED) + u0 (REAL)) at the cells, alpha = a_first
+// on the first D*D*(D/2+1) floats of the padded array, a_second after
+void launch_adjoint_axpy(float* grad, const float* v, const float* u0, float a_first, float a_second,
+                         const GridDims& gd, cudaStream_t s);
+
 // Homogeneous branch: fill x_e, T_K and compute T_S with J_alpha = 0.
 struct HomogArgs
 {

@@ -383,6 +383,320 @@ void launch_evolve(const EvolveArgs& a, const GridDims& gd, cudaStream_t s)
   ts_launches++;
 }
 
+// ======================================================================
+// Adjoint of the spin-temperature update and of the 21cm box
+// ======================================================================
+namespace {
+
+// d ln kappa / d ln T of kappa_f (the spline's derivative inside the table,
+// the extrapolation slopes outside it).
+__device__ float dlnkappa_dlnT(const TsDevConst& c, int which, float T)
+{
+  const int n = c.nk[which];
+  const float* x = c.fkx[which];
+  const float* y = c.fky[which];
+  const float* cc = c.fkc[which];
+  const float lt = logf(T);
+  if (lt < x[0])
+    return 0.0f;
+  if (lt > x[n - 1])
+    return which == 0 ? 0.381f : (y[n - 1] - y[n - 2]) / (x[n - 1] - x[n - 2]);
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (x[mid] > lt)
+      hi = mid;
+    else
+      lo = mid;
+  }
+  const float h = x[lo + 1] - x[lo];
+  const float dx = lt - x[lo];
+  const float b = (y[lo + 1] - y[lo]) / h - h * (cc[lo + 1] + 2.0f * cc[lo]) * (1.0f / 3.0f);
+  const float d = (cc[lo + 1] - cc[lo]) / (3.0f * h);
+  return b + dx * (2.0f * cc[lo] + 3.0f * d * dx);
+}
+
+// Value and gradient (d/dTK, d/dxe, d/dJ) of get_Ts_f, by forward-mode
+// differentiation of the same iteration (the number of iterations is that of
+// the FP32 forward; its stopping test is not differentiated).
+struct TsGrad
+{
+  float TS, dT, dxe, dJ;
+};
+
+__device__ TsGrad get_Ts_grad(const TsDevConst& c, float delta, float TK, float xe, float J)
+{
+  const float Trad = c.ftrad;
+  const float opd = 1.0f + delta;
+  float k[3], dk[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    k[i] = kappa_f(c, i, TK);
+    dk[i] = k[i] * dlnkappa_dlnT(c, i, TK) / TK;  // d kappa / d TK
+  }
+  const float xc = c.fxc[0] * ((1.0f - xe) * opd) * k[0] + c.fxc[1] * (xe * opd) * k[1] + c.fxc[2] * (xe * opd) * k[2];
+  const float xc_T = c.fxc[0] * ((1.0f - xe) * opd) * dk[0] + c.fxc[1] * (xe * opd) * dk[1] + c.fxc[2] * (xe * opd) * dk[2];
+  const float xc_x = opd * (-c.fxc[0] * k[0] + c.fxc[1] * k[1] + c.fxc[2] * k[2]);
+  const float iTK = 1.0f / TK;
+  TsGrad g;
+  if (J > 1.0e-20f) {
+    const float tgp = c.ftgp * opd * (1.0f - xe);
+    const float q = 1.0e-7f * tgp / TK / TK;
+    const float xi = cbrtf(q);
+    // d xi: xi = q^(1/3); dq/dTK = -2 q / TK, dq/dxe = -1e-7 ftgp opd / TK^2
+    const float xi_q = q > 0.0f ? xi / (3.0f * q) : 0.0f;
+    const float xi_T = xi_q * (-2.0f * q / TK);
+    const float xi_x = xi_q * (-1.0e-7f * c.ftgp * opd / TK / TK);
+    const float den = 1.0f + 2.98394f * xi + 1.53583f * xi * xi + 3.85289f * xi * xi * xi;
+    const float den_xi = 2.98394f + 2.0f * 1.53583f * xi + 3.0f * 3.85289f * xi * xi;
+    const float den_T = den_xi * xi_T, den_x = den_xi * xi_x;
+    const float iTK_T = -iTK * iTK;
+    float TS = Trad, TSold = 0.0f;
+    float TS_T = 0.f, TS_x = 0.f, TS_J = 0.f;  // d TS
+    int it = 0;
+    for (;;) {
+      const float rel = fabsf(TS - TSold) / TS;
+      if (!(rel > 1.0e-3f) || ++it > TS_MAX_ITER)
+        break;
+      TSold = TS;
+      const float iTS = 1.0f / TS;
+      const float iTS_T = -iTS * iTS * TS_T, iTS_x = -iTS * iTS * TS_x, iTS_J = -iTS * iTS * TS_J;
+      const float num = 1.0f - 0.0631789f * iTK + 0.115995f * iTK * iTK - 0.401403f * iTS * iTK + 0.336463f * iTS * iTK * iTK;
+      const float num_iTK = -0.0631789f + 2.0f * 0.115995f * iTK - 0.401403f * iTS + 2.0f * 0.336463f * iTS * iTK;
+      const float num_iTS = -0.401403f * iTK + 0.336463f * iTK * iTK;
+      const float num_T = num_iTK * iTK_T + num_iTS * iTS_T;
+      const float num_x = num_iTS * iTS_x, num_J = num_iTS * iTS_J;
+      const float St = num / den;
+      const float St_T = (num_T - St * den_T) / den, St_x = (num_x - St * den_x) / den, St_J = num_J / den;
+      const float xa = c.fxa * St * J;
+      const float xa_T = c.fxa * St_T * J, xa_x = c.fxa * St_x * J, xa_J = c.fxa * (St_J * J + St);
+      // 1 / Tceff = iTK + 0.405535 iTK (iTS - iTK)
+      const float E = iTK + 0.405535f * iTK * (iTS - iTK);
+      const float E_T = iTK_T + 0.405535f * (iTK_T * (iTS - iTK) + iTK * (iTS_T - iTK_T));
+      const float E_x = 0.405535f * iTK * iTS_x, E_J = 0.405535f * iTK * iTS_J;
+      const float A = 1.0f / Trad + xa * E + xc * iTK;
+      const float A_T = xa_T * E + xa * E_T + xc_T * iTK + xc * iTK_T;
+      const float A_x = xa_x * E + xa * E_x + xc_x * iTK, A_J = xa_J * E + xa * E_J;
+      const float B = 1.0f + xa + xc;
+      const float B_T = xa_T + xc_T, B_x = xa_x + xc_x, B_J = xa_J;
+      TS = 1.0f / (A / B);
+      TS_T = (B_T - TS * A_T) / A;
+      TS_x = (B_x - TS * A_x) / A;
+      TS_J = (B_J - TS * A_J) / A;
+    }
+    g.TS = TS;
+    g.dT = TS_T;
+    g.dxe = TS_x;
+    g.dJ = TS_J;
+  } else {
+    // TS = (1 + xc) / (1/Trad + xc/TK)
+    const float A = 1.0f / Trad + xc * iTK, B = 1.0f + xc;
+    g.TS = 1.0f / (A / B);
+    const float A_T = xc_T * iTK - xc * iTK * iTK, A_x = xc_x * iTK;
+    g.dT = (xc_T - g.TS * A_T) / A;
+    g.dxe = (xc_x - g.TS * A_x) / A;
+    g.dJ = 0.0f;
+  }
+  if (g.TS < 0.0f) {
+    g.TS = -g.TS;
+    g.dT = -g.dT;
+    g.dxe = -g.dxe;
+    g.dJ = -g.dJ;
+  }
+  return g;
+}
+}  // namespace
+
+// One thread per cell, tiles of EV_TILE cells with the shell ring of
+// k_evolve_f32.  From dL/d(delta_T) of the cell: the 21cm box adjoint
+// (BrightnessTemperature.c:495-545) gives dL/dxH and dL/dT_S; dL/dxH reaches
+// x_e and stars through the partial ionisation of the last (unfiltered) step
+// (find_HII_bubbles.c:416-428) when 0 < xH < 1, the ionisation flags being
+// held fixed; dL/dT_S goes back through get_Ts, the x_e / T_K update and the
+// shell sums (ComputeTs.c:743-900).  The shell values are overwritten by
+// dL/d(shell), zero where the shell was clamped at 0.  Per block: sums of
+// heat_bar * heat + ion_bar * ion + lya_bar * lya (the L_X term) and of the
+// E0 term with the dP/dE0 tables.
+__global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, int D, int H, long long N)
+{
+  const TsDevConst& c = *a.cst;
+  const int S = c.S;
+  extern __shared__ __align__(16) float sm[];
+  float4* s_P = reinterpret_cast<float4*>(sm);              // NXHII * S
+  float4* s_dP = s_P + NXHII * S;                            // NXHII * S (d/dE0; w unused)
+  float* stages = sm + 2 * ev_tables_floats(S);              // 2 * S * EV_TILE
+  __shared__ uint64_t bars[2];
+  for (int i = threadIdx.x; i < NXHII * S; i += blockDim.x) {
+    const int x = i / S, r = i % S;
+    s_P[i] = make_float4(c.fKH[r] * c.ftab[0][x][r], c.fKI[r] * c.ftab[1][x][r], c.fKL[r] * c.ftab[2][x][r],
+                         c.fKS[r]);
+    s_dP[i] = a.dP_dE0[i];
+  }
+  const long long ntiles = (N + EV_TILE - 1) / EV_TILE;
+  const int my_tiles = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  const bool light = !c.no_light;
+  if (threadIdx.x == 0 && light) {
+    bulk::mbar_init(&bars[0], 1);
+    bulk::mbar_init(&bars[1], 1);
+    bulk::mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && light)
+    for (int k = 0; k < 2 && k < my_tiles; k++)
+      ev_issue(bars, stages, a.shells, S, N, blockIdx.x + (long long)k * gridDim.x, k);
+  double acc[2] = { 0, 0 };
+  for (int k = 0; k < my_tiles; k++) {
+    const long long tile = blockIdx.x + (long long)k * gridDim.x;
+    const long long ir = tile * EV_TILE + threadIdx.x;
+    const bool valid = ir < N;
+    const long long ip = valid ? pad_index(ir, D, H) : 0;
+    float delta = 0.f, xe = 0.f, T = 1.f, gT = 0.f, xH = 1.f, TSf = 1.f;
+    if (valid) {
+      delta = a.deltax[ip];
+      xe = a.x_e_prev[ip];
+      T = a.Tk[ir];
+      gT = a.grad_dT[ir];
+      xH = a.xH[ir];
+      TSf = a.TS[ir];
+    }
+    // 21cm box: dT = cf * xH * (1 + delta) * (1 - Trad / TS)
+    const float opd = 1.0f + delta;
+    const float A1 = a.dT_factor * xH * opd;
+    const float xH_bar = gT * a.dT_factor * opd * (1.0f - a.dT_trad / TSf);
+    const float TS_bar = gT * A1 * a.dT_trad / (TSf * TSf);
+    // partial ionisation of the last step: xH = (1 - x_e) - stars * kfc / (1 + dx)
+    float xe_new_bar = 0.0f, stars_bar = 0.0f;
+    if (valid && xH > 0.0f && xH < 1.0f) {
+      const float xraw = a.x_e_new[ip];
+      if (xraw >= 1e-8f && xraw < 0.999f)
+        xe_new_bar = -xH_bar;
+      const float sraw = a.stars[ip];
+      if (sraw >= 1e-8f)
+        stars_bar = -xH_bar * a.kfc_last / (1.0f + fmaxf(delta, -1.0f + 1e-5f));
+    }
+    if (valid)
+      a.grad_stars[ip] = stars_bar;
+    // x_HII bracket (ComputeTs.c:761-773)
+    float xcall = xe;
+    if (xcall > c.xhii[NXHII - 1] * 0.999f)
+      xcall = c.xhii[NXHII - 1] * 0.999f;
+    else if (xcall < c.xhii[0])
+      xcall = 1.001f * c.xhii[0];
+    int lo = NXHII - 1;
+    while (lo > 0 && xcall < c.xhii[lo])
+      lo--;
+    const int hi = lo + 1;
+    const float w = (xcall - c.xhii[lo]) / (c.xhii[hi] - c.xhii[lo]);
+    float heat = 0.f, ion = 0.f, lya = 0.f, star = 0.f, dheat = 0.f, dion = 0.f, dlya = 0.f;
+    const float* st = nullptr;
+    if (light) {
+      const bool arrived = bulk::mbar_wait(&bars[k & 1], (unsigned)(k >> 1) & 1u);
+      if (__syncthreads_or(!arrived)) {
+        if (threadIdx.x == 0) {
+          atomicOr(a.err, bulk::ERR_PIPELINE_TIMEOUT);
+          for (int j = k; j < my_tiles && j < k + 2; j++)
+            bulk::mbar_wait(&bars[j & 1], (unsigned)(j >> 1) & 1u);
+        }
+        return;
+      }
+      st = stages + (size_t)(k & 1) * S * EV_TILE + threadIdx.x;
+      float hl = 0.f, il = 0.f, ll = 0.f, hh = 0.f, ih = 0.f, lh = 0.f;
+      float dhl = 0.f, dil = 0.f, dll = 0.f, dhh = 0.f, dih = 0.f, dlh = 0.f;
+      for (int r = 0; r < S; r++) {
+        const float sf = st[r * EV_TILE];
+        const float4 pl = s_P[lo * S + r], ph = s_P[hi * S + r];
+        const float4 ql = s_dP[lo * S + r], qh = s_dP[hi * S + r];
+        hl = fmaf(sf, pl.x, hl);
+        il = fmaf(sf, pl.y, il);
+        ll = fmaf(sf, pl.z, ll);
+        star = fmaf(sf, pl.w, star);
+        hh = fmaf(sf, ph.x, hh);
+        ih = fmaf(sf, ph.y, ih);
+        lh = fmaf(sf, ph.z, lh);
+        dhl = fmaf(sf, ql.x, dhl);
+        dil = fmaf(sf, ql.y, dil);
+        dll = fmaf(sf, ql.z, dll);
+        dhh = fmaf(sf, qh.x, dhh);
+        dih = fmaf(sf, qh.y, dih);
+        dlh = fmaf(sf, qh.z, dlh);
+      }
+      heat = fmaf(w, hh - hl, hl);
+      ion = fmaf(w, ih - il, il);
+      lya = fmaf(w, lh - ll, ll);
+      dheat = fmaf(w, dhh - dhl, dhl);
+      dion = fmaf(w, dih - dil, dil);
+      dlya = fmaf(w, dlh - dll, dll);
+    }
+    // forward of the cell (k_evolve_f32), keeping the clamp states
+    const float dxe_dzp = ion - c.fksink * alpha_A_f(T) * xe * xe * opd;
+    float dadia = c.fadia0;
+    if (fabsf(delta) > (float)FRACT_FLOAT_ERR)
+      dadia += c.fdgrowth / (1.0f / delta + c.fgrowth);
+    dadia *= (2.0f / 3.0f) * T;
+    const float dspec = -dxe_dzp * T / (1.0f + xe);
+    const float dcomp = c.fccomp * (xe / (1.0f + xe + c.ff_he)) * (c.ftrad - T);
+    const float d1 = heat / (1.0f + xe) + dcomp + dspec + dadia;
+    const float Jalpha = lya * opd + star;
+    float xn = xe + dxe_dzp * c.fdzp;
+    bool xe_free = true;
+    if (xn > 1.0f) {
+      xn = (float)(1 - FRACT_FLOAT_ERR);
+      xe_free = false;
+    } else if (xn < 0.0f) {
+      xn = 0.0f;
+      xe_free = false;
+    }
+    float Tn = T;
+    bool T_free = T < MAX_TK;
+    if (T_free)
+      Tn = T + d1 * c.fdzp;
+    if (Tn < 0.0f) {
+      Tn = c.ftk_floor;
+      T_free = false;
+    }
+    const TsGrad tg = get_Ts_grad(c, delta, Tn, xn, Jalpha);
+    // backward
+    const float Tn_bar = TS_bar * tg.dT;
+    xe_new_bar += TS_bar * tg.dxe;
+    const float J_bar = TS_bar * tg.dJ;
+    const float d1_bar = T_free ? Tn_bar * c.fdzp : 0.0f;
+    const float dxe_bar = (xe_free ? xe_new_bar * c.fdzp : 0.0f) + d1_bar * (-T / (1.0f + xe));
+    const float heat_bar = d1_bar / (1.0f + xe);
+    const float ion_bar = dxe_bar;
+    const float lya_bar = J_bar * opd;
+    const float star_bar = J_bar;
+    if (light) {
+      // dL/d(shell r), zero where the shell was clamped at 0
+      for (int r = 0; r < S; r++) {
+        const float sf = st[r * EV_TILE];
+        const float4 pl = s_P[lo * S + r], ph = s_P[hi * S + r];
+        float u = heat_bar * fmaf(w, ph.x - pl.x, pl.x) + ion_bar * fmaf(w, ph.y - pl.y, pl.y) +
+                  lya_bar * fmaf(w, ph.z - pl.z, pl.z) + star_bar * pl.w;
+        if (!(sf > 0.0f) || !valid)
+          u = 0.0f;
+        if (valid)
+          a.shells[(long long)r * N + ir] = u;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0 && k + 2 < my_tiles)
+        ev_issue(bars, stages, a.shells, S, N, tile + 2LL * gridDim.x, k + 2);
+    }
+    if (valid) {
+      acc[0] += (double)heat_bar * heat + (double)ion_bar * ion + (double)lya_bar * lya;
+      acc[1] += (double)heat_bar * dheat + (double)ion_bar * dion + (double)lya_bar * dlya;
+    }
+  }
+  block_sum_store<2>(acc, a.partials);
+}
+
+void launch_evolve_adjoint(const AdjointArgs& a, const GridDims& gd, cudaStream_t s)
+{
+  const size_t smem = sizeof(float) * (2 * ev_tables_floats(a.n_shells) + 2 * (size_t)a.n_shells * EV_TILE);
+  cudaFuncSetAttribute(k_evolve_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_evolve_adjoint<<<RED_BLOCKS, RED_THREADS, smem, s>>>(a, gd.D, gd.H, gd.N);
+  ts_launches++;
+}
+
 int ts_kernel_launches() { return ts_launches; }
 
 // Homogeneous branch, ComputeTs.c:189-262: x_e and T_K from RECFAST, T_S with

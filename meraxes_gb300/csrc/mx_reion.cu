@@ -111,6 +111,11 @@ struct mx_ctx
   std::vector<void*> mirror_allocs;
   std::map<long long, cufftHandle> c2r_plans;  // keyed by batch
   cufftHandle r2c_plan = 0;
+  // adjoint scratch (allocated by the first adjoint call)
+  cufftHandle r2c_real_plan = 0;  // R2C of a REAL-layout grid
+  float* d_adj_sfr = nullptr;     // PADDED copy of the SFR grid
+  float4* d_adj_dp = nullptr;     // 14 x MAX_SHELLS d/dE0 tables
+  double* d_adj_coef = nullptr;   // loss coefficients per bin
   int launches = 0;
 
   // per-kernel event timing (mx_profile_enable / mx_profile_read)
@@ -169,6 +174,11 @@ mx_ctx::~mx_ctx()
     cufftDestroy(kv.second);
   if (r2c_plan)
     cufftDestroy(r2c_plan);
+  if (r2c_real_plan)
+    cufftDestroy(r2c_real_plan);
+  cudaFree(d_adj_sfr);
+  cudaFree(d_adj_dp);
+  cudaFree(d_adj_coef);
   cudaFree(d_unf);
   cudaFree(d_work);
   cudaFree(d_in_ptrs);
@@ -626,6 +636,143 @@ static void fill_fast_evolve(mx_ctx* c, TsDevConst* t, const ShellPlan& sp, cons
         throw CudaError{ MX_ENOTSUP, "ComputeTs: coefficient outside the FP32 range" };
 }
 
+// Per-cell constants of the spin-temperature update (ComputeTs.c:666-724,
+// XRayHeatingFunctions.c:1241-1435) into *t, which fill_common_ts has set up.
+static void fill_ts_constants(mx_ctx* c, TsDevConst* t, const ShellPlan& sp, const FreqTables& ft, double zp,
+                              double prev_z, double collapse_fraction, double pixel_volume)
+{
+  const mx_params& p = c->p;
+  const int S = p.ts_num_filter_steps;
+  const float zpf = (float)zp;
+  t->S = S;
+  t->no_light = (collapse_fraction > 0.0) ? 0 : 1;
+  t->dzp = zp - prev_z;
+  t->dt_dzp = ft.dt_dzp;
+  t->growth = ft.growth_zp;
+  t->dgrowth = ft.dgrowth_dzp;
+  t->prefactor = ft.const_zp_prefactor;
+  t->conv = (k::C / (4. * k::PI)) / (k::PROTONMASS / k::SOLAR_MASS);
+  t->p2 = std::pow((double)(1.0f + zpf), 2);
+  t->p3 = std::pow((double)(1.0f + zpf), 3);
+  t->pixel_volume = pixel_volume;
+  t->sfr_a = p.unit_mass_g / c->d.unit_time_s;
+  t->sfr_b = std::pow(p.unit_length_cm, -3.);
+  for (int q = 0; q < S; q++) {
+    t->a[q] = sp.a_dt_dz[q];
+    t->b[q] = sp.b_pow[q];
+    t->zpp1[q] = sp.zpp1[q];
+    t->sum_lyn[q] = ft.sum_lyn[q];
+    t->dt_dzpp[q] = sp.dt_dzpp[q];
+    t->dzpp[q] = sp.dzpp[q];
+    for (int x = 0; x < 14; x++)
+      for (int w = 0; w < 3; w++)
+        t->tab[w][x][q] = ft.tab[((size_t)w * 14 + x) * S + q];
+  }
+  fill_fast_evolve(c, t, sp, ft, zp);
+}
+
+// Shells of ComputeTs (ComputeTs.c:276-503) into c->d_shells: apply the
+// SFR-history operations to `sfr` (in place, like the reference), forward
+// transform when the grid changed, then filter + inverse transform in
+// batches of shells sharing a spectrum.
+static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sfr_histories, cudaStream_t s)
+{
+  const mx_params& p = c->p;
+  const GridDims& gd = c->gd;
+  const int S = p.ts_num_filter_steps;
+  float2* sfr_unf = c->d_unf;
+  const long long nhalf = gd.C;
+  int r = 0;
+  while (r < S) {
+    for (const SfrOp& op : sp.ops[r]) {
+      Prof pr(c, "k_sfr_history", op.kind <= SfrOp::ZERO_HALF ? 8.0 * (double)nhalf : 12.0 * (double)gd.N, s);
+      if (op.kind == SfrOp::SCALE_HALF)
+        launch_sfr_scale_half(sfr, nhalf, op.dweight, s);
+      else if (op.kind == SfrOp::ZERO_HALF)
+        launch_sfr_zero_half(sfr, nhalf, s);
+      else
+        launch_sfr_load(sfr, sfr_histories + (long long)op.slice * gd.P, op.weight,
+                        op.kind == SfrOp::ADD, gd, s);
+    }
+    // shells r..r_end-1 share this spectrum (no operations in between)
+    int r_end = r + 1;
+    while (r_end < S && sp.ops[r_end].empty())
+      r_end++;
+    int q_first = r;
+    if (r == 0) {
+      // shell 0 is unfiltered: its transform pair is the identity, so the
+      // shell is the clamped grid itself
+      Prof pr(c, "k_shell_extract", 8.0 * (double)gd.N, s);
+      launch_shell_extract(sfr, gd.P, 1, 0, c->d_shells, gd, s);
+      q_first = 1;
+    }
+    if (q_first < r_end) {
+      MX_CUFFT(cufftSetStream(c->r2c_plan, s));
+      Prof pr(c, "cufft_r2c", 4.0 * (double)gd.N + 8.0 * (double)gd.C, s);
+      MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)sfr, (cufftComplex*)sfr_unf));
+    }
+    float2* in_ptr[1] = { sfr_unf };
+    MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, in_ptr, sizeof(float2*), cudaMemcpyHostToDevice, s));
+    for (int q0 = q_first; q0 < r_end;) {
+      const int nb = (int)std::min<long long>(std::min<long long>(c->work_fields, MAX_RADII), r_end - q0);
+      if (c->fused_fft) {
+        XPassArgs xa;
+        for (int f = 0; f < MAX_FIELDS; f++)
+          xa.in[f] = f == 0 ? sfr_unf : nullptr;
+        xa.G = 1;
+        xa.n = nb;
+        xa.out = c->d_work;
+        xa.C = c->work_C;
+        for (int q = 0; q < nb; q++) {
+          xa.R[q] = (float)sp.R[q0 + q];
+          xa.apply[q] = 1;
+        }
+        xa.filter_type = p.ts_heating_filter_type;
+        xa.delta_k = (float)(2.0 * k::PI / (float)p.box_size);
+        xa.scale = (float)(1.0 / (double)gd.N);
+        {
+          Prof pr(c, "fft_x_filter", 8.0 * (double)gd.C * (1 + nb), s);
+          launch_fft_x_filter(gd.D, xa, s);
+        }
+        {
+          Prof pr(c, "fft_y", 16.0 * (double)gd.C * nb, s);
+          launch_fft_y(gd.D, c->d_work, c->work_C, nb, s);
+        }
+        {
+          Prof pr(c, "fft_z_store", (8.0 * (double)gd.C + 4.0 * (double)gd.N) * nb, s);
+          launch_fft_z_store(gd.D, c->d_work, c->work_C, nb, q0, c->d_shells, gd.N, c->d_err, s);
+        }
+        q0 += nb;
+        continue;
+      }
+      FilterBatch fb;
+      fb.n = nb;
+      fb.filter_type = p.ts_heating_filter_type;
+      fb.scale_mode = 1;
+      for (int q = 0; q < nb; q++) {
+        fb.R[q] = (float)sp.R[q0 + q];
+        fb.apply[q] = (q0 + q) > 0;
+      }
+      {
+        Prof pr(c, "k_filter_ts", 8.0 * (double)gd.C * (1 + nb), s);
+        launch_filter((const float2* const*)c->d_in_ptrs, 1, c->d_work, gd.C, fb, gd, (float)p.box_size, s);
+      }
+      const cufftHandle plan = c->c2r_plan(1);
+      for (int q = 0; q < nb; q++) {
+        cufftComplex* w = (cufftComplex*)(c->d_work + (long long)q * gd.C);
+        Prof pr(c, "cufft_c2r", 8.0 * (double)gd.C + 4.0 * (double)gd.N, s);
+        MX_CUFFT(cufftExecC2R(plan, w, (cufftReal*)w));
+      }
+      {
+        Prof pr(c, "k_shell_extract", 8.0 * (double)gd.N * nb, s);
+        launch_shell_extract((const float*)c->d_work, gd.P, nb, q0, c->d_shells, gd, s);
+      }
+      q0 += nb;
+    }
+    r = r_end;
+  }
+}
+
 static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s)
 {
   const mx_params& p = c->p;
@@ -708,130 +855,14 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     // transform when the grid changed, then filter + inverse transform in
     // batches of shells sharing a spectrum.
     try {
-      float2* sfr_unf = c->d_unf;
-      const long long nhalf = gd.C;
-      int r = 0;
-      while (r < S) {
-        for (const SfrOp& op : sp.ops[r]) {
-          Prof pr(c, "k_sfr_history", op.kind <= SfrOp::ZERO_HALF ? 8.0 * (double)nhalf : 12.0 * (double)gd.N, s);
-          if (op.kind == SfrOp::SCALE_HALF)
-            launch_sfr_scale_half(g->sfr, nhalf, op.dweight, s);
-          else if (op.kind == SfrOp::ZERO_HALF)
-            launch_sfr_zero_half(g->sfr, nhalf, s);
-          else
-            launch_sfr_load(g->sfr, g->sfr_histories + (long long)op.slice * gd.P, op.weight,
-                            op.kind == SfrOp::ADD, gd, s);
-        }
-        // shells r..r_end-1 share this spectrum (no operations in between)
-        int r_end = r + 1;
-        while (r_end < S && sp.ops[r_end].empty())
-          r_end++;
-        int q_first = r;
-        if (r == 0) {
-          // shell 0 is unfiltered: its transform pair is the identity, so the
-          // shell is the clamped grid itself
-          Prof pr(c, "k_shell_extract", 8.0 * (double)gd.N, s);
-          launch_shell_extract(g->sfr, gd.P, 1, 0, c->d_shells, gd, s);
-          q_first = 1;
-        }
-        if (q_first < r_end) {
-          MX_CUFFT(cufftSetStream(c->r2c_plan, s));
-          Prof pr(c, "cufft_r2c", 4.0 * (double)gd.N + 8.0 * (double)gd.C, s);
-          MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)g->sfr, (cufftComplex*)sfr_unf));
-        }
-        float2* in_ptr[1] = { sfr_unf };
-        MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, in_ptr, sizeof(float2*), cudaMemcpyHostToDevice, s));
-        for (int q0 = q_first; q0 < r_end;) {
-          const int nb = (int)std::min<long long>(std::min<long long>(c->work_fields, MAX_RADII), r_end - q0);
-          if (c->fused_fft) {
-            XPassArgs xa;
-            for (int f = 0; f < MAX_FIELDS; f++)
-              xa.in[f] = f == 0 ? sfr_unf : nullptr;
-            xa.G = 1;
-            xa.n = nb;
-            xa.out = c->d_work;
-            xa.C = c->work_C;
-            for (int q = 0; q < nb; q++) {
-              xa.R[q] = (float)sp.R[q0 + q];
-              xa.apply[q] = 1;
-            }
-            xa.filter_type = p.ts_heating_filter_type;
-            xa.delta_k = (float)(2.0 * k::PI / (float)p.box_size);
-            xa.scale = (float)(1.0 / (double)gd.N);
-            {
-              Prof pr(c, "fft_x_filter", 8.0 * (double)gd.C * (1 + nb), s);
-              launch_fft_x_filter(gd.D, xa, s);
-            }
-            {
-              Prof pr(c, "fft_y", 16.0 * (double)gd.C * nb, s);
-              launch_fft_y(gd.D, c->d_work, c->work_C, nb, s);
-            }
-            {
-              Prof pr(c, "fft_z_store", (8.0 * (double)gd.C + 4.0 * (double)gd.N) * nb, s);
-              launch_fft_z_store(gd.D, c->d_work, c->work_C, nb, q0, c->d_shells, gd.N, c->d_err, s);
-            }
-            q0 += nb;
-            continue;
-          }
-          FilterBatch fb;
-          fb.n = nb;
-          fb.filter_type = p.ts_heating_filter_type;
-          fb.scale_mode = 1;
-          for (int q = 0; q < nb; q++) {
-            fb.R[q] = (float)sp.R[q0 + q];
-            fb.apply[q] = (q0 + q) > 0;
-          }
-          {
-            Prof pr(c, "k_filter_ts", 8.0 * (double)gd.C * (1 + nb), s);
-            launch_filter((const float2* const*)c->d_in_ptrs, 1, c->d_work, gd.C, fb, gd, (float)p.box_size, s);
-          }
-          const cufftHandle plan = c->c2r_plan(1);
-          for (int q = 0; q < nb; q++) {
-            cufftComplex* w = (cufftComplex*)(c->d_work + (long long)q * gd.C);
-            Prof pr(c, "cufft_c2r", 8.0 * (double)gd.C + 4.0 * (double)gd.N, s);
-            MX_CUFFT(cufftExecC2R(plan, w, (cufftReal*)w));
-          }
-          {
-            Prof pr(c, "k_shell_extract", 8.0 * (double)gd.N * nb, s);
-            launch_shell_extract((const float*)c->d_work, gd.P, nb, q0, c->d_shells, gd, s);
-          }
-          q0 += nb;
-        }
-        r = r_end;
-      }
+      compute_shells(c, sp, g->sfr, g->sfr_histories, s);
     } catch (...) {
       tables.wait();
       throw;
     }
     tables.get();
 
-    // per-cell constants (ComputeTs.c:666-724, XRayHeatingFunctions.c:1241-1435)
-    const float zpf = (float)zp;
-    t->S = S;
-    t->no_light = (collapse_fraction > 0.0) ? 0 : 1;
-    t->dzp = zp - prev_z;
-    t->dt_dzp = ft.dt_dzp;
-    t->growth = ft.growth_zp;
-    t->dgrowth = ft.dgrowth_dzp;
-    t->prefactor = ft.const_zp_prefactor;
-    t->conv = (k::C / (4. * k::PI)) / (k::PROTONMASS / k::SOLAR_MASS);
-    t->p2 = std::pow((double)(1.0f + zpf), 2);
-    t->p3 = std::pow((double)(1.0f + zpf), 3);
-    t->pixel_volume = pixel_volume;
-    t->sfr_a = p.unit_mass_g / c->d.unit_time_s;
-    t->sfr_b = std::pow(p.unit_length_cm, -3.);
-    for (int q = 0; q < S; q++) {
-      t->a[q] = sp.a_dt_dz[q];
-      t->b[q] = sp.b_pow[q];
-      t->zpp1[q] = sp.zpp1[q];
-      t->sum_lyn[q] = ft.sum_lyn[q];
-      t->dt_dzpp[q] = sp.dt_dzpp[q];
-      t->dzpp[q] = sp.dzpp[q];
-      for (int x = 0; x < 14; x++)
-        for (int w = 0; w < 3; w++)
-          t->tab[w][x][q] = ft.tab[((size_t)w * 14 + x) * S + q];
-    }
-    fill_fast_evolve(c, t, sp, ft, zp);
+    fill_ts_constants(c, t, sp, ft, zp, prev_z, collapse_fraction, pixel_volume);
     MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
     EvolveArgs ea;
     ea.shells = c->d_shells;
@@ -1068,6 +1099,284 @@ static int run_power_spectrum(mx_ctx* c, const float* dT, float* ps_k, float* ps
     ps_error[i] = (float)((p_box / ct) / std::sqrt(ct));
   }
   return a.nb;
+}
+
+// ======================================================================
+// Power-spectrum loss and the adjoint of ComputeTs + the 21cm box
+// ======================================================================
+// L = sum_b (P_b - T_b)^2 over nbins bins [edges[b], edges[b+1]) of the
+// power spectrum of f = delta_T V / N, P_b = sum k^3 |X_k|^2 / (2 pi^2 V) / n_b
+// over the half-spectrum modes of the bin (each counted once, k and V in Mpc
+// units, the binning of Compute_PS).  With grad: dL/d(delta_T) (REAL).
+static double run_ps_loss(mx_ctx* c, const float* dT, int nbins, const float* edges, const float* target, float* P,
+                          float* grad, cudaStream_t s)
+{
+  const GridDims& gd = c->gd;
+  if (nbins < 1 || nbins + 1 > PS_MAX_BINS)
+    throw CudaError{ MX_EINVAL, "power-spectrum loss: 1 to 47 bins" };
+  PsArgs a;
+  float e0[PS_MAX_BINS + 1];
+  float dk = 0, vol = 0;
+  ps_edges(c->p, e0, PS_MAX_BINS, &dk, &vol);
+  a.delta_k = dk;
+  a.volume = vol;
+  // bin 0 collects the modes below edges[0] and is not part of the loss
+  a.nb = nbins + 1;
+  a.edges[0] = 0.0f;
+  for (int b = 0; b <= nbins; b++) {
+    if (!(edges[b] > (b ? edges[b - 1] : 0.0f)))
+      throw CudaError{ MX_EINVAL, "power-spectrum loss: edges must be positive and increasing" };
+    a.edges[b + 1] = edges[b];
+  }
+  a.D = gd.D;
+  a.partials = c->d_ps_partials;
+  float* field = reinterpret_cast<float*>(c->d_work);
+  const float scale = (float)((double)vol / (double)gd.N);
+  {
+    Prof pr(c, "k_ps_scale", 8.0 * (double)gd.N, s);
+    launch_ps_scale(dT, scale, gd, field, s);
+  }
+  MX_CUFFT(cufftSetStream(c->r2c_plan, s));
+  MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)field, (cufftComplex*)c->d_unf));
+  a.spec = c->d_unf;
+  {
+    Prof pr(c, "k_ps_bin", 8.0 * (double)gd.C, s);
+    launch_ps_bin(a, c->d_ps_sums, s);
+  }
+  MX_CUDA(cudaMemcpyAsync(c->h_ps_sums, c->d_ps_sums, sizeof(double) * 3 * a.nb, cudaMemcpyDeviceToHost, s));
+  MX_CUDA(cudaStreamSynchronize(s));
+  const double pdiv = 2.0 * k::PI * k::PI * (double)vol;
+  double loss = 0.0;
+  double coef[PS_MAX_BINS] = { 0 };
+  for (int b = 0; b < nbins; b++) {
+    const double sum = c->h_ps_sums[b + 1], ct = c->h_ps_sums[2 * a.nb + b + 1];
+    const double pb = ct > 0 ? sum / ct : 0.0;
+    if (P)
+      P[b] = (float)pb;
+    const double d = pb - (double)target[b];
+    loss += d * d;
+    // dL/dRe X_k = 2 c_k Re X_k (and Im) with c_k = 2 (P_b - T_b) k^3 / (pdiv n_b);
+    // k_ps_loss_grad multiplies by k^3
+    coef[b + 1] = ct > 0 ? 2.0 * d / (pdiv * ct) : 0.0;
+  }
+  if (grad) {
+    // dL/df = C2R(Y) with Y = coef' k^3 X (see k_ps_loss_grad); dL/d(delta_T) = scale dL/df
+    MX_CUDA(cudaMemcpyAsync(c->d_adj_coef, coef, sizeof(double) * a.nb, cudaMemcpyHostToDevice, s));
+    float2* spec = reinterpret_cast<float2*>(c->d_work);
+    MX_CUDA(cudaMemcpyAsync(spec, c->d_unf, sizeof(float2) * gd.C, cudaMemcpyDeviceToDevice, s));
+    {
+      Prof pr(c, "k_ps_loss_grad", 16.0 * (double)gd.C, s);
+      launch_ps_loss_grad(a, c->d_adj_coef, spec, s);
+    }
+    const cufftHandle plan = c->c2r_plan(1);
+    MX_CUFFT(cufftSetStream(plan, s));
+    MX_CUFFT(cufftExecC2R(plan, (cufftComplex*)spec, (cufftReal*)spec));
+    launch_padded_to_real(reinterpret_cast<const float*>(spec), scale, gd, grad, s);
+  }
+  return loss;
+}
+
+static void ensure_adjoint_scratch(mx_ctx* c)
+{
+  if (c->d_adj_sfr)
+    return;
+  const GridDims& gd = c->gd;
+  MX_CUDA(cudaMalloc(&c->d_adj_sfr, sizeof(float) * gd.P));
+  MX_CUDA(cudaMalloc(&c->d_adj_dp, sizeof(float4) * 14 * MAX_SHELLS));
+  MX_CUDA(cudaMalloc(&c->d_adj_coef, sizeof(double) * PS_MAX_BINS));
+  int n[3] = { gd.D, gd.D, gd.D };
+  int inembed[3] = { gd.D, gd.D, gd.D };
+  int onembed[3] = { gd.D, gd.D, gd.H };
+  MX_CUFFT(cufftPlanMany(&c->r2c_real_plan, 3, n, inembed, 1, (int)gd.N, onembed, 1, (int)gd.C, CUFFT_R2C, 1));
+}
+
+// (K_H tab_H, K_I tab_I, K_L tab_L) of every (x_HII node, shell) in double:
+// the per-cell sums of the FP32 evolve without the power-of-two rescaling.
+static std::vector<double> shell_products(mx_ctx* c, const TsDevConst* t, const ShellPlan& sp, const FreqTables& ft)
+{
+  const int S = t->S;
+  const double U = (1.0 / t->pixel_volume) * t->sfr_a * t->sfr_b / k::SOLAR_MASS;
+  std::vector<double> out((size_t)3 * 14 * S);
+  for (int r = 0; r < S; r++) {
+    const double base = U * sp.a_dt_dz[r] * sp.b_pow[r] * ft.const_zp_prefactor;
+    const double K[3] = { base * ft.dt_dzp * 2.0 / 3.0 / k::BOLTZMANN, base * ft.dt_dzp, base * c->d.n_b0 * t->p3 };
+    for (int w = 0; w < 3; w++)
+      for (int x = 0; x < 14; x++)
+        out[((size_t)w * 14 + x) * S + r] = K[w] * ft.tab[((size_t)w * 14 + x) * S + r];
+  }
+  return out;
+}
+
+// Adjoint of ComputeTs (one snapshot, not homogeneous) and of the 21cm box
+// without peculiar velocities, with the ionisation flags of find_HII_bubbles
+// held fixed.  `g` holds the forward's inputs and outputs: deltax, stars (as
+// find_HII_bubbles read them), sfr (before ComputeTs reweighted it),
+// sfr_histories, x_e_box_prev and Tk_box (the state before the step), x_e_box,
+// xH and TS_box (after it).  The shells are recomputed.  Out: dL/d(sfr)
+// (PADDED), dL/d(stars) (PADDED), grad_params = {dL/dL_X, dL/dE0}.
+static void run_adjoint(mx_ctx* c, int snapshot, const mx_grids* g, const float* grad_dT, float* grad_sfr,
+                        float* grad_stars, double* grad_params, cudaStream_t s)
+{
+  const mx_params& p = c->p;
+  const GridDims& gd = c->gd;
+  if (!p.flag_spin_temp)
+    throw CudaError{ MX_ENOTSUP, "adjoint: needs the spin temperature" };
+  if (p.flag_pecvel != 0)
+    throw CudaError{ MX_ENOTSUP, "adjoint: peculiar-velocity modes are not differentiated" };
+  if (!g || !g->deltax || !g->stars || !g->sfr || !g->x_e_box_prev || !g->Tk_box || !g->x_e_box || !g->xH ||
+      !g->TS_box || (c->n_hist > 0 && !g->sfr_histories) || !grad_dT || !grad_sfr || !grad_stars || !grad_params)
+    throw CudaError{ MX_EINVAL, "adjoint: a required pointer is NULL" };
+  ensure_adjoint_scratch(c);
+  const double box = p.box_size / p.hubble_h;
+  const double pixel_volume = std::pow(box / (double)gd.D, 3);
+  const double total = std::pow((double)gd.D, 3);
+  const double zp = c->zz[snapshot];
+  const double prev_z = snapshot == 0 ? c->zz[snapshot] : c->zz[snapshot - 1];
+  const ShellPlan sp = plan_shells(p, c->zz, snapshot);
+  const int S = p.ts_num_filter_steps;
+  if (S > MAX_SHELLS)
+    throw CudaError{ MX_ENOTSUP, "too many spin-temperature shells" };
+  if (sp.homogeneous)
+    throw CudaError{ MX_ENOTSUP, "adjoint: the homogeneous branch has no SFR dependence" };
+  TsDevConst* t = c->h_tsc;
+  std::memset(t, 0, sizeof(TsDevConst));
+  fill_common_ts(c, t, zp);
+  const double R0 = k::L_FACTOR * box / (float)gd.D;
+  const double RtoM_h2 = RtoM(p, c->d, R0) * p.hubble_h * p.hubble_h;
+  // collapse fraction and <x_e> of the state before the step (as the forward)
+  CfArgs ca;
+  ca.stars = g->stars;
+  ca.deltax = g->deltax;
+  ca.x_e_prev = g->x_e_box_prev;
+  ca.RtoM_h2 = RtoM_h2;
+  ca.R3 = std::pow(R0, 3.0);
+  ca.pixel_volume = pixel_volume;
+  ca.partials = c->d_partials;
+  launch_cf_xe(ca, gd, s);
+  launch_finalize(c->d_partials, 2, c->d_sums, s);
+  MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+  MX_CUDA(cudaStreamSynchronize(s));
+  const double collapse_fraction = c->h_sums[0] / total;
+  const double x_e_ave = c->h_sums[1] / total;
+  c->stored_fcoll[snapshot] = collapse_fraction;
+  // frequency tables at E0 and E0 (1 +- h) for d/dE0
+  const double h = 1e-3;
+  FreqTables ft, ftp, ftm;
+  mx_params pp = p, pm = p;
+  pp.nu_xray_gal_threshold = p.nu_xray_gal_threshold * (1 + h);
+  pm.nu_xray_gal_threshold = p.nu_xray_gal_threshold * (1 - h);
+  build_freq_tables(p, c->d, c->ht, c->zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads, &ft);
+  build_freq_tables(pp, c->d, c->ht, c->zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads,
+                    &ftp);
+  build_freq_tables(pm, c->d, c->ht, c->zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads,
+                    &ftm);
+  fill_ts_constants(c, t, sp, ft, zp, prev_z, collapse_fraction, pixel_volume);
+  MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
+  {
+    const std::vector<double> P1 = shell_products(c, t, sp, ftp), P0 = shell_products(c, t, sp, ftm);
+    std::vector<float4> dp((size_t)14 * S);
+    const double dE = 2 * h * p.nu_xray_gal_threshold;
+    for (int x = 0; x < 14; x++)
+      for (int r = 0; r < S; r++) {
+        float v[3];
+        for (int w = 0; w < 3; w++) {
+          const size_t i = ((size_t)w * 14 + x) * S + r;
+          v[w] = (float)((P1[i] - P0[i]) / dE);
+        }
+        dp[(size_t)x * S + r] = make_float4(v[0], v[1], v[2], 0.0f);
+      }
+    MX_CUDA(cudaMemcpyAsync(c->d_adj_dp, dp.data(), sizeof(float4) * dp.size(), cudaMemcpyHostToDevice, s));
+    MX_CUDA(cudaStreamSynchronize(s));  // dp leaves scope
+  }
+  // shells of the forward, from a copy of the SFR grid
+  MX_CUDA(cudaMemcpyAsync(c->d_adj_sfr, g->sfr, sizeof(float) * gd.P, cudaMemcpyDeviceToDevice, s));
+  compute_shells(c, sp, c->d_adj_sfr, g->sfr_histories, s);
+  // the 21cm box constants (run_delta_T)
+  const float redshift = (float)(float)zp;
+  const float Hubble_h = (float)(float)p.hubble_h;
+  const float OmegaM = (float)(float)p.omega_m;
+  const float OmegaB = (float)(OmegaM * p.baryon_frac);
+  const std::vector<double> radii = filter_radii(p);
+  const double R_last = radii.back();
+  const double pv_fhb = std::pow(p.box_size / (double)gd.D, 3);
+  AdjointArgs a;
+  a.shells = c->d_shells;
+  a.deltax = g->deltax;
+  a.x_e_prev = g->x_e_box_prev;
+  a.Tk = g->Tk_box;
+  a.x_e_new = g->x_e_box;
+  a.stars = g->stars;
+  a.xH = g->xH;
+  a.TS = g->TS_box;
+  a.grad_dT = grad_dT;
+  a.grad_stars = grad_stars;
+  a.cst = c->d_tsc;
+  a.dP_dE0 = c->d_adj_dp;
+  a.dT_factor = (float)(27.0 * (OmegaB * Hubble_h * Hubble_h / 0.023) *
+                        std::sqrt((0.15 / OmegaM / Hubble_h / Hubble_h) * (1.0 + redshift) / 10.0));
+  a.dT_trad = (float)(k::TCMB * (1. + redshift));
+  a.kfc_last = (float)(p.reion_efficiency * (4.0 / 3.0) * k::PI * R_last * R_last * R_last /
+                       (RtoM(p, c->d, R_last) * pv_fhb));
+  a.partials = c->d_partials;
+  a.err = c->d_err;
+  a.n_shells = S;
+  MX_CUDA(cudaMemsetAsync(grad_stars, 0, sizeof(float) * gd.P, s));
+  {
+    Prof pr(c, "k_evolve_adjoint", ((double)S * 2 + 10.0) * 4.0 * (double)gd.N, s);
+    launch_evolve_adjoint(a, gd, s);
+  }
+  launch_finalize(c->d_partials, 2, c->d_sums, s);
+  // dL/d(shell) -> dL/d(sfr): each group of shells sharing a spectrum is a sum
+  // of symmetric filter convolutions of the group's SFR field, which is
+  // alpha * sfr (+ history terms) with one alpha per half of the padded array
+  MX_CUDA(cudaMemsetAsync(grad_sfr, 0, sizeof(float) * gd.P, s));
+  float2* acc = c->d_work;
+  float2* U = c->d_work + c->work_C;
+  double alpha[2] = { 1.0, 1.0 };
+  const float delta_k = (float)(2.0 * k::PI / (float)p.box_size);
+  const float scale = (float)(1.0 / (double)gd.N);
+  int r = 0;
+  while (r < S) {
+    for (const SfrOp& op : sp.ops[r]) {
+      if (op.kind == SfrOp::SCALE_HALF)
+        alpha[0] *= op.dweight;
+      else if (op.kind == SfrOp::ZERO_HALF)
+        alpha[0] = 0.0;
+      else if (op.kind == SfrOp::LOAD)
+        alpha[0] = alpha[1] = 0.0;
+    }
+    int r_end = r + 1;
+    while (r_end < S && sp.ops[r_end].empty())
+      r_end++;
+    const bool has0 = r == 0;
+    bool first = true;
+    for (int q = has0 ? 1 : r; q < r_end; q++) {
+      MX_CUFFT(cufftSetStream(c->r2c_real_plan, s));
+      MX_CUFFT(cufftExecR2C(c->r2c_real_plan, (cufftReal*)(c->d_shells + (long long)q * gd.N), (cufftComplex*)U));
+      launch_filter_accumulate(gd.D, acc, U, (float)sp.R[q], p.ts_heating_filter_type, delta_k, scale, first, s);
+      first = false;
+    }
+    if (!first) {
+      const cufftHandle plan = c->c2r_plan(1);
+      MX_CUFFT(cufftSetStream(plan, s));
+      MX_CUFFT(cufftExecC2R(plan, (cufftComplex*)acc, (cufftReal*)acc));
+    }
+    if (alpha[0] != 0.0 || alpha[1] != 0.0)
+      launch_adjoint_axpy(grad_sfr, first ? nullptr : reinterpret_cast<const float*>(acc),
+                          has0 ? c->d_shells : nullptr, (float)alpha[0], (float)alpha[1], gd, s);
+    r = r_end;
+  }
+  double sums[2];
+  MX_CUDA(cudaMemcpyAsync(sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+  unsigned int errw = 0;
+  MX_CUDA(cudaMemcpyAsync(&errw, c->d_err, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+  MX_CUDA(cudaStreamSynchronize(s));
+  if (errw) {
+    MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
+    throw CudaError{ MX_ECUDA, "adjoint: a pipeline wait timed out" };
+  }
+  grad_params[0] = sums[0] / p.lx_gal;
+  grad_params[1] = sums[1];
 }
 
 // ======================================================================
@@ -1459,6 +1768,38 @@ int mx_Compute_PS_device(mx_ctx* ctx, const float* delta_T, float* ps_k, float* 
     nb = run_power_spectrum(ctx, delta_T, ps_k, ps_data, ps_error, cap, pick(ctx, stream));
   });
   return rc == MX_OK ? nb : rc;
+}
+
+int mx_set_xray_params(mx_ctx* ctx, double lx_gal, double nu_xray_gal_threshold)
+{
+  return guarded(ctx, [&]() {
+    if (!(lx_gal > 0) || !(nu_xray_gal_threshold > 0) || !(nu_xray_gal_threshold < ctx->p.nu_xray_max))
+      throw CudaError{ MX_EINVAL, "X-ray parameters out of range" };
+    ctx->p.lx_gal = lx_gal;
+    ctx->p.nu_xray_gal_threshold = nu_xray_gal_threshold;
+  });
+}
+
+int mx_ps_loss_device(mx_ctx* ctx, const float* delta_T, int32_t nbins, const float* edges, const float* target,
+                      double* loss, float* P, float* grad_delta_T, void* stream)
+{
+  return guarded(ctx, [&]() {
+    if (!delta_T || !edges || !target || !loss)
+      throw CudaError{ MX_EINVAL, "ps_loss: NULL pointer" };
+    ensure_adjoint_scratch(ctx);
+    *loss = run_ps_loss(ctx, delta_T, nbins, edges, target, P, grad_delta_T, pick(ctx, stream));
+    if (grad_delta_T)
+      MX_CUDA(cudaStreamSynchronize(pick(ctx, stream)));
+  });
+}
+
+int mx_adjoint_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* saved, const float* grad_delta_T,
+                      float* grad_sfr, float* grad_stars, double* grad_params, void* stream)
+{
+  return guarded(ctx, [&]() {
+    check_snapshot(ctx, snapshot);
+    run_adjoint(ctx, snapshot, saved, grad_delta_T, grad_sfr, grad_stars, grad_params, pick(ctx, stream));
+  });
 }
 
 int mx_construct_baryon_grids(mx_ctx* ctx, int32_t snapshot, const mx_galaxies* galaxies, int32_t flag_bh_feedback,

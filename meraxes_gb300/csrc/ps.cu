@@ -149,6 +149,51 @@ __global__ void __launch_bounds__(RED_THREADS) k_ps_bin(PsArgs a)
     __syncthreads();
   }
 }
+// f = dT * scale into the padded layout (the power-spectrum loss field)
+__global__ void k_ps_scale(const float* __restrict__ dT, float scale, int D, int H, long long N, float* __restrict__ out)
+{
+  for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
+    const long long row = ir / D;
+    out[row * 2LL * H + (ir - row * D)] = dT[ir] * scale;
+  }
+}
+
+// Gradient spectrum of the binned loss: Y_k = coef[b] k^3 X_k on the modes of
+// bin b (the binning of k_ps_bin), times 2 on the kz = 0 and kz = D/2 planes,
+// which a C2R counts once where it counts the others twice.  In place.
+__global__ void k_ps_loss_grad(PsArgs a, const double* __restrict__ coef, float2* __restrict__ spec)
+{
+  const int D = a.D, H = D / 2 + 1;
+  const long long n = (long long)D * D * H;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int nz = (int)(i % H);
+    const long long row = i / H;
+    const int nx = (int)(row / D), ny = (int)(row % D);
+    const float kx = kcomp_ps(nx, D, a.delta_k), ky = kcomp_ps(ny, D, a.delta_k);
+    const float kz = __fmul_rn((float)nz, a.delta_k);
+    const float kmag = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky)), __fmul_rn(kz, kz)));
+    float f = 0.0f;
+    if (kmag < a.edges[a.nb]) {
+      int b = 0;
+      while (!(kmag < a.edges[b + 1]))
+        b++;
+      const double k = (double)kmag;
+      f = (float)(coef[b] * k * k * k * ((nz == 0 || 2 * nz == D) ? 2.0 : 1.0));
+    }
+    float2 x = spec[i];
+    spec[i] = make_float2(x.x * f, x.y * f);
+  }
+}
+
+// REAL out = PADDED in * scale
+__global__ void k_padded_to_real(const float* __restrict__ in, float scale, int D, int H, long long N,
+                                 float* __restrict__ out)
+{
+  for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
+    const long long row = ir / D;
+    out[ir] = in[row * 2LL * H + (ir - row * D)] * scale;
+  }
+}
 }  // namespace
 
 void launch_ps_mean(const float* dT, long long N, double* partials, double* sum, cudaStream_t s)
@@ -170,6 +215,24 @@ void launch_ps_bin(const PsArgs& a, double* sums, cudaStream_t s)
   k_ps_bin<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a);
   k_ps_finalize<<<1, 3 * PS_MAX_BINS, 0, s>>>(a.partials, RED_BLOCKS, 3 * a.nb, sums);
   ps_launches += 2;
+}
+
+void launch_ps_scale(const float* dT, float scale, const GridDims& gd, float* out, cudaStream_t s)
+{
+  k_ps_scale<<<RED_BLOCKS, RED_THREADS, 0, s>>>(dT, scale, gd.D, gd.H, gd.N, out);
+  ps_launches++;
+}
+
+void launch_ps_loss_grad(const PsArgs& a, const double* coef, float2* spec, cudaStream_t s)
+{
+  k_ps_loss_grad<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, coef, spec);
+  ps_launches++;
+}
+
+void launch_padded_to_real(const float* in, float scale, const GridDims& gd, float* out, cudaStream_t s)
+{
+  k_padded_to_real<<<RED_BLOCKS, RED_THREADS, 0, s>>>(in, scale, gd.D, gd.H, gd.N, out);
+  ps_launches++;
 }
 
 int ps_kernel_launches() { return ps_launches; }

@@ -23,6 +23,11 @@ struct PsArgs
 void launch_ps_mean(const float* dT, long long N, double* partials, double* sum, cudaStream_t s);
 void launch_ps_field(const float* dT, const double* sum, float volume, const GridDims& gd, float* out, cudaStream_t s);
 void launch_ps_bin(const PsArgs& a, double* sums, cudaStream_t s);
+// power-spectrum loss: f = dT * scale (padded), gradient spectrum (in place:
+// Y_k = coef[bin] k^3 X_k, doubled on the kz = 0, D/2 planes), REAL = padded * scale
+void launch_ps_scale(const float* dT, float scale, const GridDims& gd, float* out, cudaStream_t s);
+void launch_ps_loss_grad(const PsArgs& a, const double* coef, float2* spec, cudaStream_t s);
+void launch_padded_to_real(const float* in, float scale, const GridDims& gd, float* out, cudaStream_t s);
 int ps_kernel_launches();
 
 }  // namespace mx

@@ -239,6 +239,8 @@ def workload(name: str, grid_dim: Optional[int] = None) -> Workload:
     full_256   : the full step at z=10, 256^3, L=100, seed 1: recombinations,
                  ComputeTs (40 shells, L_X=1e40, E0=500 eV) and delta_T; x_e sink
                  clumping factor 3.
+    diff_256   : the full step's physics at z=12, 256^3, L=100, seed 3: the
+                 power-spectrum-loss gradient case.
     evolve_512 : 20 snapshots z=15..6 at 512^3, L=200, seed 2, fields grown
                  linearly with the growth factor; recombinations (R_max 20),
                  ComputeTs and delta_T every snapshot.
@@ -253,6 +255,13 @@ def workload(name: str, grid_dim: Optional[int] = None) -> Workload:
                         flag_recombinations=1, flag_spin_temp=1, flag_21cm=1, lx_gal=1e40,
                         nu_xray_gal_threshold=500.0, clumping_factor=3.0)
         w = Workload(name, p, 1, [10.5, 10.0], [1])
+    elif name == "diff_256":
+        # the differentiation case: the full step's physics at z=12, seed 3; the
+        # loss target is made at L_X = 2e40 (autograd.py)
+        p = ReionParams(grid_dim=256, box_size=100.0, r_bubble_max=20.0, reion_efficiency=1.0,
+                        flag_recombinations=1, flag_spin_temp=1, flag_21cm=1, lx_gal=1e40,
+                        nu_xray_gal_threshold=500.0, clumping_factor=3.0)
+        w = Workload(name, p, 3, [12.5, 12.0], [1])
     elif name == "evolve_512":
         p = ReionParams(grid_dim=512, box_size=200.0, r_bubble_max=20.0, r_bubble_max_recomb=20.0,
                         reion_efficiency=1.0, flag_recombinations=1, flag_spin_temp=1, flag_21cm=1)
