@@ -69,6 +69,8 @@ def parse_args(argv=None):
     ap.add_argument("--cpu-sample-grid", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-grid", type=int, default=256)
     return ap.parse_args(argv)
 
 
@@ -352,9 +354,66 @@ def run_gb300(args, rank, world, local):
     }
     if e2e:
         out["e2e"] = e2e
+    if not args.no_adjoint and args.adjoint_grid > 0:
+        out["adjoint"] = run_adjoint_ratio(args)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
     return out, rank
+
+
+def run_adjoint_ratio(args, steps: int = 3):
+    """Forward and forward + adjoint of the power-spectrum loss on the
+    differentiation workload (diff_256: 256^3, L=100 Mpc/h, seed 3, z=12; the
+    20-bin loss against a target made at L_X = 2e40).  Forward: ComputeTs ->
+    find_HII_bubbles -> 21cm box -> loss; adjoint: the loss gradient, the
+    recomputed shells, the per-cell adjoint and the shell adjoint.  CUDA-event
+    times per step, after one warm-up."""
+    import numpy as np
+    import torch
+
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+    from meraxes_gb300.autograd import DeltaT21, PSLoss21, log_bins
+    from meraxes_gb300.params import workload
+
+    w = workload("diff_256", args.adjoint_grid)
+    p = w.params
+    step = ReionGridStep(p, w.redshifts)
+    gen = syn.FieldGenerator(w)
+    st = syn.initial_state(p, w.redshifts[0])
+    st.update(gen.inputs(1, step.n_sfr_histories))
+    D = p.grid_dim
+    st.setdefault("delta_T", np.zeros((D, D, D), np.float32))
+    dev = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in st.items()}
+    state = {k: v for k, v in dev.items() if k not in ("sfr", "stars")}
+    edges = log_bins(step, 20)
+    lx0 = torch.tensor(p.lx_gal, dtype=torch.float64)
+    e00 = torch.tensor(p.nu_xray_gal_threshold, dtype=torch.float64)
+    with torch.no_grad():
+        dT = DeltaT21.apply(dev["sfr"], dev["stars"], torch.tensor(2e40, dtype=torch.float64), e00, step, 1, state)
+        _, target, _ = step.ps_loss(dT, edges, [0.0] * 20, grad=False)
+    fwd, tot = [], []
+    for i in range(steps + 1):
+        sfr = dev["sfr"].clone().requires_grad_(True)
+        stars = dev["stars"].clone().requires_grad_(True)
+        lx = lx0.clone().requires_grad_(True)
+        e0 = e00.clone().requires_grad_(True)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        ev[0].record()
+        L = PSLoss21.apply(DeltaT21.apply(sfr, stars, lx, e0, step, 1, state), step, edges, target)
+        ev[1].record()
+        L.backward()
+        ev[2].record()
+        torch.cuda.synchronize()
+        if i > 0:
+            fwd.append(ev[0].elapsed_time(ev[1]))
+            tot.append(ev[0].elapsed_time(ev[2]))
+    f, t = sum(fwd) / len(fwd), sum(tot) / len(tot)
+    del step
+    return {"config": f"diff_256: {D}^3, L={p.box_size} Mpc/h, seed 3, z=12, 20-bin power-spectrum loss, "
+                      "gradients w.r.t. sfr, stars (escape fraction), L_X, E0",
+            "fwd_ms": round(f, 3), "fwd_adj_ms": round(t, 3), "ratio": round(t / f, 3), "steps": steps}
 
 
 def run_e2e(args, step, w, fields, used, n_hist, device, world):

@@ -1259,17 +1259,31 @@ static void run_adjoint(mx_ctx* c, int snapshot, const mx_grids* g, const float*
   const double collapse_fraction = c->h_sums[0] / total;
   const double x_e_ave = c->h_sums[1] / total;
   c->stored_fcoll[snapshot] = collapse_fraction;
-  // frequency tables at E0 and E0 (1 +- h) for d/dE0
+  // frequency tables at E0 and E0 (1 +- h) for d/dE0, on host threads while
+  // the shells are recomputed
   const double h = 1e-3;
   FreqTables ft, ftp, ftm;
   mx_params pp = p, pm = p;
   pp.nu_xray_gal_threshold = p.nu_xray_gal_threshold * (1 + h);
   pm.nu_xray_gal_threshold = p.nu_xray_gal_threshold * (1 - h);
-  build_freq_tables(p, c->d, c->ht, c->zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads, &ft);
-  build_freq_tables(pp, c->d, c->ht, c->zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads,
-                    &ftp);
-  build_freq_tables(pm, c->d, c->ht, c->zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads,
-                    &ftm);
+  const int nt = std::max(1, c->nthreads / 3);
+  auto build = [&](const mx_params& q, FreqTables* out) {
+    return std::async(std::launch::async, [&, out]() {
+      build_freq_tables(q, c->d, c->ht, c->zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, nt, out);
+    });
+  };
+  std::future<void> tables[3] = { build(p, &ft), build(pp, &ftp), build(pm, &ftm) };
+  try {
+    // shells of the forward, from a copy of the SFR grid
+    MX_CUDA(cudaMemcpyAsync(c->d_adj_sfr, g->sfr, sizeof(float) * gd.P, cudaMemcpyDeviceToDevice, s));
+    compute_shells(c, sp, c->d_adj_sfr, g->sfr_histories, s);
+  } catch (...) {
+    for (auto& f : tables)
+      f.wait();
+    throw;
+  }
+  for (auto& f : tables)
+    f.get();
   fill_ts_constants(c, t, sp, ft, zp, prev_z, collapse_fraction, pixel_volume);
   MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
   {
@@ -1288,9 +1302,6 @@ static void run_adjoint(mx_ctx* c, int snapshot, const mx_grids* g, const float*
     MX_CUDA(cudaMemcpyAsync(c->d_adj_dp, dp.data(), sizeof(float4) * dp.size(), cudaMemcpyHostToDevice, s));
     MX_CUDA(cudaStreamSynchronize(s));  // dp leaves scope
   }
-  // shells of the forward, from a copy of the SFR grid
-  MX_CUDA(cudaMemcpyAsync(c->d_adj_sfr, g->sfr, sizeof(float) * gd.P, cudaMemcpyDeviceToDevice, s));
-  compute_shells(c, sp, c->d_adj_sfr, g->sfr_histories, s);
   // the 21cm box constants (run_delta_T)
   const float redshift = (float)(float)zp;
   const float Hubble_h = (float)(float)p.hubble_h;
