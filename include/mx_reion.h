@@ -163,6 +163,11 @@ typedef struct mx_ctx mx_ctx;
  * x_int_tables/); it is only read when flag_spin_temp is set.  The context
  * owns all device scratch, cuFFT plans and physics tables. */
 int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out);
+/* mx_create with the transform work buffer capped at max_work_bytes (it
+ * holds at least the fields of one filter radius), for several contexts on
+ * one GPU, e.g. a batch of independent boxes.  mx_create takes up to 45% of
+ * the free device memory for it.  No reference counterpart. */
+int mx_create_limited(const mx_params* params, const char* tables_dir, size_t max_work_bytes, mx_ctx** out);
 void mx_destroy(mx_ctx* ctx);
 const char* mx_last_error(const mx_ctx* ctx); /* ctx may be NULL: last mx_create error */
 

@@ -27,6 +27,7 @@ EXPORTS = [
     "mx_lightcone_init", "mx_ConstructLightcone", "mx_ConstructLightcone_device",
     "mx_construct_baryon_grids", "mx_construct_baryon_grids_device", "mx_calculate_Mvir_crit",
     "mx_calculate_Mvir_crit_device", "mx_set_xray_params", "mx_ps_loss_device", "mx_adjoint_device",
+    "mx_create_limited",
 ]
 
 
@@ -112,6 +113,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mx_calculate_Mvir_crit.restype = ctypes.c_int
         L.mx_calculate_Mvir_crit_device.argtypes = mvir + [P]
         L.mx_calculate_Mvir_crit_device.restype = ctypes.c_int
+        L.mx_create_limited.argtypes = [ctypes.POINTER(MxParams), ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(P)]
+        L.mx_create_limited.restype = ctypes.c_int
         L.mx_set_xray_params.argtypes = [P, ctypes.c_double, ctypes.c_double]
         L.mx_set_xray_params.restype = ctypes.c_int
         L.mx_ps_loss_device.argtypes = [P, P, ctypes.c_int32, ctypes.POINTER(ctypes.c_float),

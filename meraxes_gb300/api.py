@@ -14,6 +14,7 @@ tensors select the device entry points on torch's current stream.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 from typing import Dict, Optional, Sequence
 
@@ -29,12 +30,19 @@ def _is_torch_cuda(a) -> bool:
 
 
 class ReionGridStep:
-    def __init__(self, params: ReionParams, redshifts: Sequence[float], tables_dir: str = TABLES_DIR):
+    def __init__(self, params: ReionParams, redshifts: Sequence[float], tables_dir: str = TABLES_DIR,
+                 max_work_bytes: int = 0):
+        """max_work_bytes caps the transform work buffer (mx_create_limited);
+        0 lets it take up to 45% of the free device memory."""
         self.lib = _lib.load()
         self.params = params
         self._pc = params.to_ctypes()
         self.ctx = ctypes.c_void_p()
-        rc = self.lib.mx_create(ctypes.byref(self._pc), tables_dir.encode(), ctypes.byref(self.ctx))
+        if max_work_bytes:
+            rc = self.lib.mx_create_limited(ctypes.byref(self._pc), tables_dir.encode(), int(max_work_bytes),
+                                            ctypes.byref(self.ctx))
+        else:
+            rc = self.lib.mx_create(ctypes.byref(self._pc), tables_dir.encode(), ctypes.byref(self.ctx))
         if rc != 0:
             raise _lib.MxError(rc, self.lib.mx_last_error(None).decode())
         zz = (ctypes.c_double * len(redshifts))(*[float(z) for z in redshifts])
@@ -44,6 +52,27 @@ class ReionGridStep:
         self.last_launches = 0
 
     # ------------------------------------------------------------------ utils
+    @contextlib.contextmanager
+    def _stream(self):
+        """The CUDA stream of a device call: torch's current stream; or, when
+        that is the default stream (handle 0, which the library reads as its
+        own non-blocking context stream), a side stream that starts after the
+        caller's pending default-stream work and that the default stream then
+        waits for."""
+        import torch
+
+        cur = torch.cuda.current_stream()
+        if cur.cuda_stream != 0:
+            yield cur.cuda_stream
+            return
+        if getattr(self, "_side", None) is None:
+            self._side = torch.cuda.Stream()
+        self._side.wait_stream(cur)
+        try:
+            yield self._side.cuda_stream
+        finally:
+            cur.wait_stream(self._side)
+
     def _check(self, rc: int):
         if rc != 0:
             raise _lib.MxError(rc, self.lib.mx_last_error(self.ctx).decode())
@@ -95,9 +124,9 @@ class ReionGridStep:
         if device:
             import torch
 
-            stream = torch.cuda.current_stream().cuda_stream
-            rc = getattr(self.lib, name + "_device")(self.ctx, snapshot, ctypes.byref(g), ctypes.byref(out),
-                                                    ctypes.c_void_p(stream))
+            with self._stream() as stream:
+                rc = getattr(self.lib, name + "_device")(self.ctx, snapshot, ctypes.byref(g), ctypes.byref(out),
+                                                        ctypes.c_void_p(stream))
         else:
             rc = getattr(self.lib, name)(self.ctx, snapshot, ctypes.byref(g), ctypes.byref(out))
         self._check(rc)
@@ -143,8 +172,8 @@ class ReionGridStep:
 
             if delta_T.dtype != torch.float32 or not delta_T.is_contiguous():
                 raise ValueError("delta_T: need contiguous float32")
-            stream = torch.cuda.current_stream().cuda_stream
-            rc = self.lib.mx_Compute_PS_device(self.ctx, delta_T.data_ptr(), *ptrs, n, ctypes.c_void_p(stream))
+            with self._stream() as stream:
+                rc = self.lib.mx_Compute_PS_device(self.ctx, delta_T.data_ptr(), *ptrs, n, ctypes.c_void_p(stream))
         else:
             d = np.ascontiguousarray(delta_T, dtype=np.float32)
             rc = self.lib.mx_Compute_PS(self.ctx, d.ctypes.data, *ptrs, n)
@@ -171,9 +200,9 @@ class ReionGridStep:
         if _is_torch_cuda(delta_T):
             import torch
 
-            stream = torch.cuda.current_stream().cuda_stream
-            rc = self.lib.mx_ConstructLightcone_device(self.ctx, snapshot, delta_T.data_ptr(), delta_T_prev.data_ptr(),
-                                                       lightcone.data_ptr(), z.ctypes.data, ctypes.c_void_p(stream))
+            with self._stream() as stream:
+                rc = self.lib.mx_ConstructLightcone_device(self.ctx, snapshot, delta_T.data_ptr(), delta_T_prev.data_ptr(),
+                                                           lightcone.data_ptr(), z.ctypes.data, ctypes.c_void_p(stream))
         else:
             for a in (delta_T, delta_T_prev, lightcone):
                 if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
@@ -224,10 +253,10 @@ class ReionGridStep:
         if device:
             import torch
 
-            stream = torch.cuda.current_stream().cuda_stream
-            rc = self.lib.mx_construct_baryon_grids_device(self.ctx, snapshot, ctypes.byref(gal), flag_bh_feedback,
-                                                          bh_limit, alpha_uv_bh, ctypes.byref(g),
-                                                          ctypes.c_void_p(stream))
+            with self._stream() as stream:
+                rc = self.lib.mx_construct_baryon_grids_device(self.ctx, snapshot, ctypes.byref(gal), flag_bh_feedback,
+                                                              bh_limit, alpha_uv_bh, ctypes.byref(g),
+                                                              ctypes.c_void_p(stream))
         else:
             rc = self.lib.mx_construct_baryon_grids(self.ctx, snapshot, ctypes.byref(gal), flag_bh_feedback, bh_limit,
                                                    alpha_uv_bh, ctypes.byref(g))
@@ -244,9 +273,9 @@ class ReionGridStep:
             for a in arrays:
                 if not _is_torch_cuda(a) or a.dtype != torch.float32 or not a.is_contiguous():
                     raise ValueError("need contiguous float32 CUDA tensors")
-            stream = torch.cuda.current_stream().cuda_stream
-            rc = self.lib.mx_calculate_Mvir_crit_device(self.ctx, redshift, sm, *[a.data_ptr() for a in arrays],
-                                                        ctypes.c_void_p(stream))
+            with self._stream() as stream:
+                rc = self.lib.mx_calculate_Mvir_crit_device(self.ctx, redshift, sm, *[a.data_ptr() for a in arrays],
+                                                            ctypes.c_void_p(stream))
         else:
             for a in arrays:
                 if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
@@ -272,9 +301,9 @@ class ReionGridStep:
         loss = ctypes.c_double()
         P = (ctypes.c_float * nb)()
         g = torch.empty_like(delta_T) if grad else None
-        stream = torch.cuda.current_stream().cuda_stream
-        self._check(self.lib.mx_ps_loss_device(self.ctx, delta_T.data_ptr(), nb, e, t, ctypes.byref(loss), P,
-                                               g.data_ptr() if grad else None, ctypes.c_void_p(stream)))
+        with self._stream() as stream:
+            self._check(self.lib.mx_ps_loss_device(self.ctx, delta_T.data_ptr(), nb, e, t, ctypes.byref(loss), P,
+                                                   g.data_ptr() if grad else None, ctypes.c_void_p(stream)))
         return loss.value, list(P), g
 
     def adjoint(self, snapshot: int, saved, grad_delta_T):
@@ -288,7 +317,7 @@ class ReionGridStep:
         gs = torch.zeros_like(saved["sfr"])
         gst = torch.zeros_like(saved["stars"])
         par = (ctypes.c_double * 2)()
-        stream = torch.cuda.current_stream().cuda_stream
-        self._check(self.lib.mx_adjoint_device(self.ctx, snapshot, ctypes.byref(g), grad_delta_T.data_ptr(),
-                                               gs.data_ptr(), gst.data_ptr(), par, ctypes.c_void_p(stream)))
+        with self._stream() as stream:
+            self._check(self.lib.mx_adjoint_device(self.ctx, snapshot, ctypes.byref(g), grad_delta_T.data_ptr(),
+                                                   gs.data_ptr(), gst.data_ptr(), par, ctypes.c_void_p(stream)))
         return gs, gst, par[0], par[1]

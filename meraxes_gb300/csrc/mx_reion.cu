@@ -84,6 +84,7 @@ struct mx_ctx
   float2* d_unf = nullptr;      // MAX_FIELDS x C
   float2* d_work = nullptr;     // batch x work_C
   long long work_fields = 0;    // capacity in spectra
+  size_t work_cap_bytes = 0;    // cap on d_work (0: 45% of free memory)
   long long work_C = 0;         // complex values per batch spectrum: D*D*fft_pitch(D) fused, C otherwise
   float2** d_in_ptrs = nullptr; // device array of MAX_FIELDS pointers
   // light cone (Initialise_ConstructLightcone / ConstructLightcone state)
@@ -227,6 +228,8 @@ void mx_ctx::alloc_scratch()
   const double spectrum = (double)sizeof(float2) * work_C;
   const long long want = (long long)radii.size() * G;
   long long fit = (long long)(0.45 * (double)free_b / spectrum);
+  if (work_cap_bytes)
+    fit = std::min(fit, (long long)((double)work_cap_bytes / spectrum));
   if (const char* env = std::getenv("MX_MAX_BATCH_SPECTRA"))
     fit = std::min(fit, (long long)std::atoll(env));
   long long cap = std::max<long long>(G, std::min(want, fit));
@@ -462,6 +465,7 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
     // one radius (G fields) per cuFFT execution keeps the cuFFT work area at
     // the size of one radius' spectra
     const cufftHandle plan = c->c2r_plan(G);
+    MX_CUFFT(cufftSetStream(plan, s));
     for (int r = 0; r < nf; r++) {
       cufftComplex* w = (cufftComplex*)(c->d_work + (long long)r * G * gd.C);
       Prof pr(c, "cufft_c2r", (double)G * (B8C + B4N), s);
@@ -758,6 +762,7 @@ static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sf
         launch_filter((const float2* const*)c->d_in_ptrs, 1, c->d_work, gd.C, fb, gd, (float)p.box_size, s);
       }
       const cufftHandle plan = c->c2r_plan(1);
+      MX_CUFFT(cufftSetStream(plan, s));
       for (int q = 0; q < nb; q++) {
         cufftComplex* w = (cufftComplex*)(c->d_work + (long long)q * gd.C);
         Prof pr(c, "cufft_c2r", 8.0 * (double)gd.C + 4.0 * (double)gd.N, s);
@@ -1931,7 +1936,19 @@ int mx_calculate_Mvir_crit_device(mx_ctx* ctx, double redshift, const double sm_
   });
 }
 
+static int create_ctx(const mx_params* params, const char* tables_dir, size_t work_cap_bytes, mx_ctx** out);
+
 int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out)
+{
+  return create_ctx(params, tables_dir, 0, out);
+}
+
+int mx_create_limited(const mx_params* params, const char* tables_dir, size_t max_work_bytes, mx_ctx** out)
+{
+  return create_ctx(params, tables_dir, max_work_bytes, out);
+}
+
+static int create_ctx(const mx_params* params, const char* tables_dir, size_t work_cap_bytes, mx_ctx** out)
 {
   g_create_error.clear();
   if (!params || !out) {
@@ -2010,6 +2027,7 @@ int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out)
       MX_CUDA(cudaMemcpy(c->d_rr_y, yf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
       MX_CUDA(cudaMemcpy(c->d_rr_c, cf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     }
+    c->work_cap_bytes = work_cap_bytes;
     c->alloc_scratch();
   } catch (const CudaError& e) {
     g_create_error = e.msg;
