@@ -70,6 +70,7 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--adjoint-grid", type=int, default=256)
     return ap.parse_args(argv)
 
@@ -356,6 +357,8 @@ def run_gb300(args, rank, world, local):
         out["e2e"] = e2e
     if not args.no_adjoint and args.adjoint_grid > 0:
         out["adjoint"] = run_adjoint_ratio(args)
+    if not args.no_batch and world == 1:
+        out["batch"] = run_batch()
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
     return out, rank
@@ -414,6 +417,22 @@ def run_adjoint_ratio(args, steps: int = 3):
     return {"config": f"diff_256: {D}^3, L={p.box_size} Mpc/h, seed 3, z=12, 20-bin power-spectrum loss, "
                       "gradients w.r.t. sfr, stars (escape fraction), L_X, E0",
             "fwd_ms": round(f, 3), "fwd_adj_ms": round(t, 3), "ratio": round(t / f, 3), "steps": steps}
+
+
+def run_batch():
+    """The uneven batch: 48 independent boxes (16 each at 96^3, 128^3, 192^3,
+    0.5 Mpc/h cells, seeds 10-57, L_X and escape fraction drawn per box), the
+    forward step and the adjoint of the power-spectrum loss for every box, on
+    concurrent workers (meraxes_gb300/batch.py).  Wall time of the 48 boxes;
+    inputs and loss targets are prepared before it."""
+    from meraxes_gb300.batch import BatchRunner, uneven_batch
+
+    runner = BatchRunner(uneven_batch())
+    plan = runner.make_plan()
+    out = runner.run()
+    return {"config": "48 boxes: 16 each at 96^3, 128^3, 192^3, 0.5 Mpc/h cells, forward + adjoint per box",
+            "wall_s": round(out["wall_s"], 3), "boxes_per_s": round(48 / out["wall_s"], 2),
+            "workers_per_size": {str(k): v for k, v in plan.items()}}
 
 
 def run_e2e(args, step, w, fields, used, n_hist, device, world):
