@@ -347,7 +347,8 @@ def run_gb300(args, rank, world, local):
                                "ComputeTs 40 shells + find_HII_bubbles 41 radii x 5 fields + 21cm box",
                    "grid": D, "snapshots_timed": [order[i] for i in range(args.warmup, total)],
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (each grid 0.54 GB at 512^3)"},
+                   "l2": "inputs larger than L2 (each grid 0.54 GB at 512^3)",
+                   "fft_block_sizes": list(step.fft_block_sizes())},
         "gpu_launches": launches, "clocks": clk, "roofline": roofline, "step_algorithmic_gbs": round(step_gbs, 1),
         "kernels": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
                     for k, v in kernels.items()},

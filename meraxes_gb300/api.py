@@ -93,6 +93,12 @@ class ReionGridStep:
         n = self.lib.mx_filter_radii(self.ctx, buf, 1024)
         return list(buf[:n])
 
+    def fft_block_sizes(self):
+        """Threads per block of the fused x- and y-pass chosen at creation."""
+        x, y = ctypes.c_int32(), ctypes.c_int32()
+        self._check(self.lib.mx_fft_block_sizes(self.ctx, ctypes.byref(x), ctypes.byref(y)))
+        return x.value, y.value
+
     def _grids(self, grids: Dict[str, object]):
         g = MxGrids()
         device = None

@@ -348,9 +348,9 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
 // scales by 1/N, multiplies by W(|k| R), inverse-DFTs along x and stores to
 // out[(r*G + g) * C + (x*D + ky)*HP + kz], all HP columns (those past H are
 // zero in, zero out).
-constexpr int XTHREADS = 512;
-template <int D>
-__global__ void __launch_bounds__(XTHREADS, 2) k_fft_x_filter(XPassArgs a)
+// XTHREADS threads per block: 256 or 512 (the context's autotuner picks).
+template <int D, int XTHREADS>
+__global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) k_fft_x_filter(XPassArgs a)
 {
   using P = TilePlan<D>;
   constexpr int H = D / 2 + 1;
@@ -410,8 +410,8 @@ __global__ void __launch_bounds__(XTHREADS, 2) k_fft_x_filter(XPassArgs a)
 // ------------------------------------------------------------------ y-pass
 // Grid: (spectrum, x, tile of TXC kz columns).  In-place inverse DFT along y
 // over all HP columns of the pitch.
-template <int D>
-__global__ void __launch_bounds__(FFT_THREADS, 3) k_fft_y(float2* data, long long C, int n_spectra)
+template <int D, int YTHREADS>
+__global__ void __launch_bounds__(YTHREADS, YTHREADS == 256 ? 3 : 2) k_fft_y(float2* data, long long C, int n_spectra)
 {
   using P = TilePlan<D>;
   constexpr int HP = Pitch<D>::HP;
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 3) k_fft_y(float2* data, long lon
   const int kz0 = tile * TXC;
   float2* col = data + s * C + (long long)x * D * HP + kz0 + threadIdx.x % TXC;
   __syncthreads();
-  tile_dft<D, FFT_THREADS>(
+  tile_dft<D, YTHREADS>(
     buf, tw, [&](int ky, int) { return col[ky * HP]; }, [&](int y, int, float2 v) { col[y * HP] = v; });
 }
 
@@ -958,19 +958,35 @@ constexpr size_t smem_x()
   return smem_y<D>() + sizeof(float) * (size_t)(D / 2 + 1) * TXC;
 }
 
-template <int D>
-static void launch_x(const XPassArgs& a, cudaStream_t s)
+template <int D, int T>
+static void launch_x_t(const XPassArgs& a, cudaStream_t s)
 {
-  cudaFuncSetAttribute(k_fft_x_filter<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x<D>());
+  cudaFuncSetAttribute(k_fft_x_filter<D, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x<D>());
   const long long blocks = (long long)D * TilePlan<D>::NT * a.n;
-  k_fft_x_filter<D><<<(unsigned)blocks, XTHREADS, smem_x<D>(), s>>>(a);
+  k_fft_x_filter<D, T><<<(unsigned)blocks, T, smem_x<D>(), s>>>(a);
 }
 template <int D>
-static void launch_y(float2* data, long long C, int n_spectra, cudaStream_t s)
+static void launch_x(const XPassArgs& a, int threads, cudaStream_t s)
+{
+  if (threads == 256)
+    launch_x_t<D, 256>(a, s);
+  else
+    launch_x_t<D, 512>(a, s);
+}
+template <int D, int T>
+static void launch_y_t(float2* data, long long C, int n_spectra, cudaStream_t s)
 {
   const long long blocks = (long long)n_spectra * D * TilePlan<D>::NT;
-  cudaFuncSetAttribute(k_fft_y<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y<D>());
-  k_fft_y<D><<<(unsigned)blocks, FFT_THREADS, smem_y<D>(), s>>>(data, C, n_spectra);
+  cudaFuncSetAttribute(k_fft_y<D, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y<D>());
+  k_fft_y<D, T><<<(unsigned)blocks, T, smem_y<D>(), s>>>(data, C, n_spectra);
+}
+template <int D>
+static void launch_y(float2* data, long long C, int n_spectra, int threads, cudaStream_t s)
+{
+  if (threads == 512)
+    launch_y_t<D, 512>(data, C, n_spectra, s);
+  else
+    launch_y_t<D, 256>(data, C, n_spectra, s);
 }
 template <int D, bool SPIN, bool RECOMB>
 static void launch_zt_cfg(const ZThresholdArgs& a, cudaStream_t s)
@@ -1017,31 +1033,31 @@ void launch_filter_accumulate(int D, float2* acc, const float2* U, float R, int 
   fft_launches++;
 }
 
-bool launch_fft_x_filter(int D, const XPassArgs& args, cudaStream_t s)
+bool launch_fft_x_filter(int D, const XPassArgs& args, int threads, cudaStream_t s)
 {
   static const float kmax = sharpk_threshold();
   XPassArgs a = args;
   a.sharpk_max = kmax;
   switch (D) {
-    case 32: launch_x<32>(a, s); break;
-    case 64: launch_x<64>(a, s); break;
-    case 128: launch_x<128>(a, s); break;
-    case 256: launch_x<256>(a, s); break;
-    case 512: launch_x<512>(a, s); break;
+    case 32: launch_x<32>(a, threads, s); break;
+    case 64: launch_x<64>(a, threads, s); break;
+    case 128: launch_x<128>(a, threads, s); break;
+    case 256: launch_x<256>(a, threads, s); break;
+    case 512: launch_x<512>(a, threads, s); break;
     default: return false;
   }
   fft_launches++;
   return true;
 }
 
-bool launch_fft_y(int D, float2* data, long long C, int n_spectra, cudaStream_t s)
+bool launch_fft_y(int D, float2* data, long long C, int n_spectra, int threads, cudaStream_t s)
 {
   switch (D) {
-    case 32: launch_y<32>(data, C, n_spectra, s); break;
-    case 64: launch_y<64>(data, C, n_spectra, s); break;
-    case 128: launch_y<128>(data, C, n_spectra, s); break;
-    case 256: launch_y<256>(data, C, n_spectra, s); break;
-    case 512: launch_y<512>(data, C, n_spectra, s); break;
+    case 32: launch_y<32>(data, C, n_spectra, threads, s); break;
+    case 64: launch_y<64>(data, C, n_spectra, threads, s); break;
+    case 128: launch_y<128>(data, C, n_spectra, threads, s); break;
+    case 256: launch_y<256>(data, C, n_spectra, threads, s); break;
+    case 512: launch_y<512>(data, C, n_spectra, threads, s); break;
     default: return false;
   }
   fft_launches++;

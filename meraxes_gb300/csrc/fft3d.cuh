@@ -54,8 +54,9 @@ int fft_pitch(int D);
 // the filter of the x-pass
 void launch_filter_accumulate(int D, float2* acc, const float2* U, float R, int filter_type, float delta_k,
                               float scale, bool first, cudaStream_t s);
-bool launch_fft_x_filter(int D, const XPassArgs& a, cudaStream_t s);
-bool launch_fft_y(int D, float2* data, long long C, int n_spectra, cudaStream_t s);
+// threads per block of the x- and y-pass: 256 or 512
+bool launch_fft_x_filter(int D, const XPassArgs& a, int threads, cudaStream_t s);
+bool launch_fft_y(int D, float2* data, long long C, int n_spectra, int threads, cudaStream_t s);
 bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s);
 bool launch_fft_z_store(int D, const float2* spectra, long long C, int n, int r0, float* shells, long long N,
                         unsigned* err, cudaStream_t s);

@@ -74,6 +74,8 @@ struct mx_ctx
   // inverse transforms: fused three-pass kernels for power-of-two grids
   // (fft3d.cu), cuFFT otherwise or when MX_TRANSFORM=cufft
   bool fused_fft = false;
+  // threads per block of the fused x- and y-pass, chosen by tune_fft()
+  int x_threads = 512, y_threads = 256;
 
   RecombTable rr;
   HeatTables ht;
@@ -411,10 +413,10 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
         xa.scale = (float)(1.0 / (double)gd.N);
         {
           Prof pr(c, "fft_x_filter", (double)G * B8C * (1 + nf), s);
-          launch_fft_x_filter(gd.D, xa, s);
+          launch_fft_x_filter(gd.D, xa, c->x_threads, s);
         }
         Prof pr(c, "fft_y", 2.0 * G * nf * B8C, s);
-        launch_fft_y(gd.D, c->d_work, c->work_C, nf * G, s);
+        launch_fft_y(gd.D, c->d_work, c->work_C, nf * G, c->y_threads, s);
       }
       ZThresholdArgs za;
       za.spectra = c->d_work;
@@ -736,11 +738,11 @@ static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sf
         xa.scale = (float)(1.0 / (double)gd.N);
         {
           Prof pr(c, "fft_x_filter", 8.0 * (double)gd.C * (1 + nb), s);
-          launch_fft_x_filter(gd.D, xa, s);
+          launch_fft_x_filter(gd.D, xa, c->x_threads, s);
         }
         {
           Prof pr(c, "fft_y", 16.0 * (double)gd.C * nb, s);
-          launch_fft_y(gd.D, c->d_work, c->work_C, nb, s);
+          launch_fft_y(gd.D, c->d_work, c->work_C, nb, c->y_threads, s);
         }
         {
           Prof pr(c, "fft_z_store", (8.0 * (double)gd.C + 4.0 * (double)gd.N) * nb, s);
@@ -1948,6 +1950,83 @@ int mx_create_limited(const mx_params* params, const char* tables_dir, size_t ma
   return create_ctx(params, tables_dir, max_work_bytes, out);
 }
 
+// Block-size autotuner of the fused x- and y-pass.  Both passes are
+// available with 256 and 512 threads per block and give identical results
+// (the thread count changes only which thread runs which column transform,
+// not the arithmetic).  Which one is faster depends on the grid size: at
+// small grids the larger block hides more latency, at 512^3 the smaller one
+// keeps more blocks resident.  The context times both on its own scratch at
+// creation (a zero spectrum, up to four radii, best of three launches) and
+// keeps the faster.  MX_XPASS_THREADS / MX_YPASS_THREADS (256 or 512) fix a
+// choice; MX_AUTOTUNE=0 keeps the defaults (x 512, y 256).
+static void tune_fft(mx_ctx* c)
+{
+  auto env_threads = [](const char* name) {
+    const char* v = std::getenv(name);
+    const int t = v ? std::atoi(v) : 0;
+    return (t == 256 || t == 512) ? t : 0;
+  };
+  const int fx = env_threads("MX_XPASS_THREADS"), fy = env_threads("MX_YPASS_THREADS");
+  if (fx)
+    c->x_threads = fx;
+  if (fy)
+    c->y_threads = fy;
+  const char* at = std::getenv("MX_AUTOTUNE");
+  if ((fx && fy) || (at && std::string(at) == "0") || !c->fused_fft)
+    return;
+  const GridDims& gd = c->gd;
+  cudaStream_t s = c->stream;
+  MX_CUDA(cudaMemsetAsync(c->d_unf, 0, sizeof(float2) * gd.C, s));
+  const int n = (int)std::min<long long>(std::min<long long>(c->work_fields, 4), MAX_RADII);
+  XPassArgs xa;
+  for (int f = 0; f < MAX_FIELDS; f++)
+    xa.in[f] = f == 0 ? c->d_unf : nullptr;
+  xa.G = 1;
+  xa.n = n;
+  xa.out = c->d_work;
+  xa.C = c->work_C;
+  for (int r = 0; r < n; r++) {
+    xa.R[r] = (float)(c->p.box_size / 8.0);
+    xa.apply[r] = 1;
+  }
+  xa.filter_type = c->p.filter_type;
+  xa.delta_k = (float)(2.0 * k::PI / c->p.box_size);
+  xa.scale = (float)(1.0 / (double)gd.N);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  MX_CUDA(cudaEventCreate(&e0));
+  MX_CUDA(cudaEventCreate(&e1));
+  auto best_ms = [&](auto&& launch) {
+    launch();  // warm-up
+    float best = 1e30f;
+    for (int i = 0; i < 3; i++) {
+      cudaEventRecord(e0, s);
+      launch();
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best = std::min(best, ms);
+    }
+    return best;
+  };
+  const int cand[2] = { 256, 512 };
+  float tx[2] = { 0, 0 }, ty[2] = { 0, 0 };
+  for (int i = 0; i < 2; i++) {
+    if (!fx)
+      tx[i] = best_ms([&] { launch_fft_x_filter(gd.D, xa, cand[i], s); });
+    if (!fy)
+      ty[i] = best_ms([&] { launch_fft_y(gd.D, c->d_work, c->work_C, n, cand[i], s); });
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  MX_CUDA(cudaGetLastError());
+  MX_CUDA(cudaStreamSynchronize(s));
+  if (!fx)
+    c->x_threads = tx[0] < tx[1] ? 256 : 512;
+  if (!fy)
+    c->y_threads = ty[0] < ty[1] ? 256 : 512;
+}
+
 static int create_ctx(const mx_params* params, const char* tables_dir, size_t work_cap_bytes, mx_ctx** out)
 {
   g_create_error.clear();
@@ -2029,6 +2108,7 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
     }
     c->work_cap_bytes = work_cap_bytes;
     c->alloc_scratch();
+    tune_fft(c.get());
   } catch (const CudaError& e) {
     g_create_error = e.msg;
     return e.code == MX_ECUDA && e.msg.find("memory") != std::string::npos ? MX_ENOMEM : e.code;
@@ -2058,6 +2138,15 @@ int mx_set_redshifts(mx_ctx* ctx, const double* zz, int32_t n_snaps)
 }
 
 int32_t mx_n_sfr_histories(const mx_ctx* ctx) { return ctx ? ctx->n_hist : -1; }
+
+int mx_fft_block_sizes(const mx_ctx* ctx, int32_t* x_threads, int32_t* y_threads)
+{
+  if (!ctx || !x_threads || !y_threads)
+    return MX_EINVAL;
+  *x_threads = ctx->fused_fft ? ctx->x_threads : 0;
+  *y_threads = ctx->fused_fft ? ctx->y_threads : 0;
+  return MX_OK;
+}
 
 int mx_profile_enable(mx_ctx* ctx, int32_t on)
 {

@@ -89,6 +89,44 @@ def test_both_transform_paths_match_oracle(name, D, transform, tables_dir, monke
     print(name, D, transform, _run_against_oracle(name, D, tables_dir))
 
 
+# The block-size autotuner may pick 256 or 512 threads for the x- and
+# y-pass; every choice must give bit-identical grids.
+@pytest.mark.parametrize("name,D", [("full24", 64), ("evolve16", 128)])
+def test_fft_block_sizes_give_identical_results(name, D, monkeypatch):
+    from cases import initial
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+
+    c = CASES[name]
+    w = Case(name, c.base, D, c.overrides, c.fesc, c.snapshots).workload()
+    runs = []
+    for tx, ty in ((256, 256), (512, 512), (256, 512), (512, 256)):
+        monkeypatch.setenv("MX_XPASS_THREADS", str(tx))
+        monkeypatch.setenv("MX_YPASS_THREADS", str(ty))
+        step = ReionGridStep(w.params, w.redshifts)
+        assert step.fft_block_sizes() == (tx, ty)
+        gen = syn.FieldGenerator(w)
+        st = initial(w, step.n_sfr_histories)
+        glob = []
+        for s in w.snapshots:
+            st.update(gen.inputs(s, step.n_sfr_histories))
+            glob.append(step.step(s, st))
+        runs.append((st, glob))
+        step.close()
+    st0, g0 = runs[0]
+    for st, g in runs[1:]:
+        for k in OUTPUT_GRIDS:
+            if k in st0:
+                assert np.array_equal(st0[k], st[k]), k
+        for a, b in zip(g0, g):
+            assert a["volume_weighted_global_xH"] == b["volume_weighted_global_xH"]
+    monkeypatch.delenv("MX_XPASS_THREADS")
+    monkeypatch.delenv("MX_YPASS_THREADS")
+    tuned = ReionGridStep(w.params, w.redshifts)
+    assert tuned.fft_block_sizes()[0] in (256, 512) and tuned.fft_block_sizes()[1] in (256, 512)
+    tuned.close()
+
+
 def test_device_entry_points_match_host_entry_points():
     import torch
 
