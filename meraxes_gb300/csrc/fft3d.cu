@@ -20,6 +20,7 @@
 // twiddles, inter-step twiddles from a shared table filled with sincospi,
 // transposes through the shared tile).  The z-pass computes each row's C2R as a
 // half-length complex transform split over 4-lane groups (see below).
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -188,6 +189,22 @@ __device__ __forceinline__ float kcomp(int n, int D, float delta_k)
 {
   return (n > D / 2) ? __fmul_rn((float)(n - D), delta_k) : __fmul_rn((float)n, delta_k);
 }
+
+// Weight of the x-pass at (kx <= D/2, ky, kz) with kyv = kcomp(ky): the
+// filter W(|k| R) times the 1/N scale (a power of two, so x * (scale * W) ==
+// (x * scale) * W exactly); a zeroed sharp-k mode is a weight of 0.
+__device__ __forceinline__ float x_weight(int kx, float kyv, int kz, int D, float delta_k, int filter_type, float R,
+                                          float sharpk_max, float scale)
+{
+  const float kxv = kcomp(kx, D, delta_k);
+  const float kzv = __fmul_rn((float)kz, delta_k);
+  const float kmag = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(kyv, kyv)), __fmul_rn(kzv, kzv)));
+  bool zero = false;
+  float wv = filter_weight(filter_type, kmag, R, sharpk_max, &zero);
+  if (zero)
+    wv = 0.0f;
+  return wv * scale;
+}
 }  // namespace
 
 int fft_kernel_launches() { return fft_launches; }
@@ -262,43 +279,72 @@ struct TilePlan
   static __device__ __forceinline__ int at(int line, int t) { return line * TXC + t; }
 };
 
-// Inverse DFT of the tile's columns.  load(n, t) returns input point n of
-// column t; store(k, t, v) takes output point k.  Ends without a barrier:
-// the caller synchronises before reusing buf.
+// Inverse DFT of the tile's columns in three steps, each a member of
+// TileSteps; the caller puts a barrier between them and after the last one
+// before it reuses buf.  tile_dft() runs all three.
 //
 // Thread roles are fixed: column t = tid % TXC and slot s = tid / TXC of
 // S = NTHR / TXC slots (NTHR threads in the block).  A half-warp is the 16 columns of one slot,
 // so every shared and global access of a half-warp is one 128-byte line.
 // Slot s takes the work items s, s + S, s + 2S, ... of each step; the loops
 // over them are unrolled, so their index arithmetic is constant offsets.
-template <int D, int NTHR, class Load, class Store>
-__device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load load, Store store)
+template <int D, int NTHR>
+struct TileSteps
 {
   using P = TilePlan<D>;
-  constexpr int R1 = P::R1, R2 = P::R2, R3 = P::R3, M = P::M;
-  constexpr int S = NTHR / TXC;
+  static constexpr int R1 = P::R1, R2 = P::R2, R3 = P::R3, M = P::M;
+  static constexpr int S = NTHR / TXC;
   static_assert(S % R2 == 0 && S % R3 == 0, "slot split");
-  const int t = threadIdx.x % TXC, s = threadIdx.x / TXC;
-  float2* col = buf + t;
-  // step A: items n' = s + S j
+  static constexpr int JA = (M + S - 1) / S;  // step-A items per thread
+  static constexpr int NPTS = JA * R1;        // input points per thread
+
+  // f(n, i) for every input point n this thread reads in step A, i its
+  // index 0..NPTS-1 (a compile-time constant once the loops are unrolled,
+  // so a register array indexed by i stays in registers)
+  template <class F>
+  static __device__ __forceinline__ void for_each_input(F f)
+  {
+    const int s = threadIdx.x / TXC;
 #pragma unroll
-  for (int j = 0; j < (M + S - 1) / S; j++) {
-    const int np = s + S * j;
-    if (M % S == 0 || np < M) {
-      float2 v[R1];
+    for (int j = 0; j < JA; j++) {
+      const int np = s + S * j;
+      if (M % S == 0 || np < M) {
 #pragma unroll
-      for (int n1 = 0; n1 < R1; n1++)
-        v[n1] = load(np + M * n1, t);
-      dft_bwd<R1>(v);
-      col[np * TXC] = v[0];
-#pragma unroll
-      for (int k1 = 1; k1 < R1; k1++)
-        col[(k1 * M + np) * TXC] = cmul(v[k1], tw[(np * k1) & (D - 1)]);
+        for (int n1 = 0; n1 < R1; n1++)
+          f(np + M * n1, j * R1 + n1);
+      }
     }
   }
-  __syncthreads();
-  // step B: items (n3, k1) with n3 = s % R3 fixed
+
+  // step A: items n' = s + S j; load(n, t, i) returns input point n of
+  // column t (i as in for_each_input)
+  template <class Load>
+  static __device__ __forceinline__ void a(float2* buf, const float2* tw, Load load)
   {
+    const int t = threadIdx.x % TXC, s = threadIdx.x / TXC;
+    float2* col = buf + t;
+#pragma unroll
+    for (int j = 0; j < JA; j++) {
+      const int np = s + S * j;
+      if (M % S == 0 || np < M) {
+        float2 v[R1];
+#pragma unroll
+        for (int n1 = 0; n1 < R1; n1++)
+          v[n1] = load(np + M * n1, t, j * R1 + n1);
+        dft_bwd<R1>(v);
+        col[np * TXC] = v[0];
+#pragma unroll
+        for (int k1 = 1; k1 < R1; k1++)
+          col[(k1 * M + np) * TXC] = cmul(v[k1], tw[(np * k1) & (D - 1)]);
+      }
+    }
+  }
+
+  // step B: items (n3, k1) with n3 = s % R3 fixed
+  static __device__ __forceinline__ void b(float2* buf, const float2* tw)
+  {
+    const int t = threadIdx.x % TXC, s = threadIdx.x / TXC;
+    float2* col = buf + t;
     const int n3 = s % R3;
 #pragma unroll
     for (int j = 0; j < (R1 * R3 + S - 1) / S; j++) {
@@ -317,9 +363,14 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
       }
     }
   }
-  __syncthreads();
+
   // step C: items (k2, k1) with k2 = s % R2 fixed; output k = k1 + R1 (k2 + R2 k3)
+  // goes to store(k, t, v)
+  template <class Store>
+  static __device__ __forceinline__ void c(const float2* buf, Store store)
   {
+    const int t = threadIdx.x % TXC, s = threadIdx.x / TXC;
+    const float2* col = buf + t;
     const int k2 = s % R2;
 #pragma unroll
     for (int j = 0; j < (R1 * R2 + S - 1) / S; j++) {
@@ -337,6 +388,17 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
       }
     }
   }
+};
+
+template <int D, int NTHR, class Load, class Store>
+__device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load load, Store store)
+{
+  using T = TileSteps<D, NTHR>;
+  T::a(buf, tw, load);
+  __syncthreads();
+  T::b(buf, tw);
+  __syncthreads();
+  T::c(buf, store);
 }
 
 // ------------------------------------------------------------------ x-pass
@@ -348,6 +410,11 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
 // scales by 1/N, multiplies by W(|k| R), inverse-DFTs along x and stores to
 // out[(r*G + g) * C + (x*D + ky)*HP + kz], all HP columns (those past H are
 // zero in, zero out).
+//
+// Per-radius weight tables built once per context (read instead of the
+// sincosf) measured slower: the table read before the block's barrier is a
+// DRAM wait that the weights' arithmetic is not (a 28-radius one-field batch
+// at 512^3 took 8.75 ms with tables, 5.90 ms without).
 // XTHREADS threads per block: 256 or 512 (the context's autotuner picks).
 template <int D, int XTHREADS>
 __global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) k_fft_x_filter(XPassArgs a)
@@ -364,46 +431,59 @@ __global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) 
   const int ky = tile / P::NT;
   const int kz0 = (tile % P::NT) * TXC;
   const float kyv = kcomp(ky, D, a.delta_k);
-  // filter weights of the tile times the 1/N scale (a power of two, so
-  // x * (scale * W) == (x * scale) * W exactly), wsm[|kx| * TXC + t] for
-  // |kx| = min(kx, D - kx) <= D/2; a zeroed sharp-k mode is a weight of 0.
-  for (int i = threadIdx.x; i < (D / 2 + 1) * TXC; i += XTHREADS) {
-    const int kx = i / TXC, t = i % TXC, kz = kz0 + t;
-    float wv = 1.0f;
-    if (a.apply[r]) {
-      const float kxv = kcomp(kx, D, a.delta_k);
-      const float kzv = __fmul_rn((float)kz, a.delta_k);
-      const float kmag = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(kyv, kyv)), __fmul_rn(kzv, kzv)));
-      bool zero = false;
-      wv = filter_weight(a.filter_type, kmag, a.R[r], a.sharpk_max, &zero);
-      if (zero)
-        wv = 0.0f;
-    }
-    wv *= a.scale;
-    wsm[i] = wv;
-  }
-  __syncthreads();
   // this thread's column: kz = kz0 + t, the same in every step
   const int t0 = threadIdx.x % TXC;
   const bool live = kz0 + t0 < H;
-  const float* wcol = wsm + t0;
-  for (int g = 0; g < a.G; g++) {
+  // the unfiltered points of step A, read into registers before the step
+  using T = TileSteps<D, XTHREADS>;
+  float2 pts[T::NPTS];
+  auto read_points = [&](int g) {
     const float2* __restrict__ src = a.in[g] + (long long)ky * H + kz0 + t0;
-    float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C + (long long)ky * Pitch<D>::HP + kz0 + t0;
-    tile_dft<D, XTHREADS>(
-      buf, tw,
-      [&](int kx, int) {
-        float2 x = make_float2(0.f, 0.f);
-        if (live) {
-          x = src[(long long)kx * (D * H)];
-          const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
-          x.x *= wv;
-          x.y *= wv;
-        }
-        return x;
-      },
-      [&](int x, int, float2 v) { dst[(long long)x * (D * Pitch<D>::HP)] = v; });
+    T::for_each_input([&](int kx, int i) {
+      pts[i] = live ? src[(long long)kx * (D * H)] : make_float2(0.f, 0.f);
+    });
+  };
+  // filter weights of the tile, wsm[|kx| * TXC + t] for |kx| = min(kx, D -
+  // kx) <= D/2, then the first field's points (read after the weights, whose
+  // sincosf would otherwise push them out of registers; the reads are in
+  // flight across the barrier)
+  for (int i = threadIdx.x; i < H * TXC; i += XTHREADS) {
+    const int kx = i / TXC, t = i % TXC;
+    wsm[i] = a.apply[r] ? x_weight(kx, kyv, kz0 + t, D, a.delta_k, a.filter_type, a.R[r], a.sharpk_max, a.scale)
+                        : a.scale;
+  }
+  read_points(0);
+  __syncthreads();
+  const float* wcol = wsm + t0;
+  // steps B and C of field g after its step A
+  auto finish = [&](int g) {
     __syncthreads();
+    T::b(buf, tw);
+    __syncthreads();
+    float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C + (long long)ky * Pitch<D>::HP + kz0 + t0;
+    T::c(buf, [&](int x, int, float2 v) { dst[(long long)x * (D * Pitch<D>::HP)] = v; });
+    __syncthreads();
+  };
+  // field 0 from the points already read (outside the loop, so that they are
+  // dead after this step A), the others straight from memory
+  T::a(buf, tw, [&](int kx, int, int i) {
+    float2 x = pts[i];
+    const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
+    x.x *= wv;
+    x.y *= wv;
+    return x;
+  });
+  finish(0);
+  for (int g = 1; g < a.G; g++) {
+    read_points(g);
+    T::a(buf, tw, [&](int kx, int, int i) {
+      float2 x = pts[i];
+      const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
+      x.x *= wv;
+      x.y *= wv;
+      return x;
+    });
+    finish(g);
   }
 }
 
@@ -418,16 +498,24 @@ __global__ void __launch_bounds__(YTHREADS, YTHREADS == 256 ? 3 : 2) k_fft_y(flo
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* buf = smem + D;
-  fill_twiddles<D>(tw);
   const long long blk = blockIdx.x;
   const int tile = (int)(blk % P::NT);
   const int x = (int)((blk / P::NT) % D);
   const long long s = blk / ((long long)P::NT * D);
   const int kz0 = tile * TXC;
   float2* col = data + s * C + (long long)x * D * HP + kz0 + threadIdx.x % TXC;
+  // the points of step A are read first, so that the reads are in flight
+  // while the twiddle table is filled
+  using T = TileSteps<D, YTHREADS>;
+  float2 pts[T::NPTS];
+  T::for_each_input([&](int ky, int i) { pts[i] = col[ky * HP]; });
+  fill_twiddles<D>(tw);
   __syncthreads();
-  tile_dft<D, YTHREADS>(
-    buf, tw, [&](int ky, int) { return col[ky * HP]; }, [&](int y, int, float2 v) { col[y * HP] = v; });
+  T::a(buf, tw, [&](int, int, int i) { return pts[i]; });
+  __syncthreads();
+  T::b(buf, tw);
+  __syncthreads();
+  T::c(buf, [&](int y, int, float2 v) { col[y * HP] = v; });
 }
 
 // ------------------------------------------------------------------ z-pass
