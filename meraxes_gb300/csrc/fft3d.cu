@@ -402,14 +402,15 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
 }
 
 // ------------------------------------------------------------------ x-pass
-// Grid: one block per (ky, tile of TXC kz columns, radius), the radius
-// fastest, so that the blocks of all radii of a tile run together and its
-// unfiltered columns are read from HBM once and from L2 by the others.  A
+// Grid: one block per (|ky| <= D/2, tile of TXC kz columns, radius), the
+// radius fastest, so that the blocks of all radii of a tile run together and
+// its unfiltered columns are read from HBM once and from L2 by the others.  A
 // block computes the filter weights of its tile for its radius (shared by all
-// fields), then for every field loads the unfiltered columns (rows of H),
-// scales by 1/N, multiplies by W(|k| R), inverse-DFTs along x and stores to
-// out[(r*G + g) * C + (x*D + ky)*HP + kz], all HP columns (those past H are
-// zero in, zero out).
+// fields and by the rows ky and D - ky, which have the same |k|), then for
+// each of the two rows and every field loads the unfiltered columns (rows of
+// H), scales by 1/N, multiplies by W(|k| R), inverse-DFTs along x and stores
+// to out[(r*G + g) * C + (x*D + ky)*HP + kz], all HP columns (those past H
+// are zero in, zero out).
 //
 // Per-radius weight tables built once per context (read instead of the
 // sincosf) measured slower: the table read before the block's barrier is a
@@ -428,16 +429,17 @@ __global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) 
   fill_twiddles<D>(tw);
   const int r = blockIdx.x % a.n;
   const int tile = blockIdx.x / a.n;
-  const int ky = tile / P::NT;
+  const int kyp = tile / P::NT;  // |ky|: the block transforms rows ky = kyp and D - kyp
   const int kz0 = (tile % P::NT) * TXC;
-  const float kyv = kcomp(ky, D, a.delta_k);
+  // the weights depend on ky only through kyv^2, the same for both rows
+  const float kyv = kcomp(kyp, D, a.delta_k);
   // this thread's column: kz = kz0 + t, the same in every step
   const int t0 = threadIdx.x % TXC;
   const bool live = kz0 + t0 < H;
   // the unfiltered points of step A, read into registers before the step
   using T = TileSteps<D, XTHREADS>;
   float2 pts[T::NPTS];
-  auto read_points = [&](int g) {
+  auto read_points = [&](int ky, int g) {
     const float2* __restrict__ src = a.in[g] + (long long)ky * H + kz0 + t0;
     T::for_each_input([&](int kx, int i) {
       pts[i] = live ? src[(long long)kx * (D * H)] : make_float2(0.f, 0.f);
@@ -452,38 +454,39 @@ __global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) 
     wsm[i] = a.apply[r] ? x_weight(kx, kyv, kz0 + t, D, a.delta_k, a.filter_type, a.R[r], a.sharpk_max, a.scale)
                         : a.scale;
   }
-  read_points(0);
-  __syncthreads();
   const float* wcol = wsm + t0;
-  // steps B and C of field g after its step A
-  auto finish = [&](int g) {
-    __syncthreads();
-    T::b(buf, tw);
-    __syncthreads();
-    float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C + (long long)ky * Pitch<D>::HP + kz0 + t0;
-    T::c(buf, [&](int x, int, float2 v) { dst[(long long)x * (D * Pitch<D>::HP)] = v; });
-    __syncthreads();
-  };
-  // field 0 from the points already read (outside the loop, so that they are
-  // dead after this step A), the others straight from memory
-  T::a(buf, tw, [&](int kx, int, int i) {
-    float2 x = pts[i];
-    const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
-    x.x *= wv;
-    x.y *= wv;
-    return x;
-  });
-  finish(0);
-  for (int g = 1; g < a.G; g++) {
-    read_points(g);
-    T::a(buf, tw, [&](int kx, int, int i) {
-      float2 x = pts[i];
-      const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
-      x.x *= wv;
-      x.y *= wv;
-      return x;
-    });
-    finish(g);
+  const int n_rows = (kyp == 0 || kyp == D / 2) ? 1 : 2;
+  for (int h = 0; h < n_rows; h++) {
+    const int ky = h == 0 ? kyp : D - kyp;
+    read_points(ky, 0);
+    if (h == 0)
+      __syncthreads();
+    // steps B and C of field g after its step A
+    auto finish = [&](int g) {
+      __syncthreads();
+      T::b(buf, tw);
+      __syncthreads();
+      float2* __restrict__ dst =
+        a.out + (long long)(r * a.G + g) * a.C + (long long)ky * Pitch<D>::HP + kz0 + t0;
+      T::c(buf, [&](int x, int, float2 v) { dst[(long long)x * (D * Pitch<D>::HP)] = v; });
+      __syncthreads();
+    };
+    auto step_a = [&]() {
+      T::a(buf, tw, [&](int kx, int, int i) {
+        float2 x = pts[i];
+        const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
+        x.x *= wv;
+        x.y *= wv;
+        return x;
+      });
+    };
+    step_a();
+    finish(0);
+    for (int g = 1; g < a.G; g++) {
+      read_points(ky, g);
+      step_a();
+      finish(g);
+    }
   }
 }
 
@@ -1050,7 +1053,7 @@ template <int D, int T>
 static void launch_x_t(const XPassArgs& a, cudaStream_t s)
 {
   cudaFuncSetAttribute(k_fft_x_filter<D, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x<D>());
-  const long long blocks = (long long)D * TilePlan<D>::NT * a.n;
+  const long long blocks = (long long)(D / 2 + 1) * TilePlan<D>::NT * a.n;
   k_fft_x_filter<D, T><<<(unsigned)blocks, T, smem_x<D>(), s>>>(a);
 }
 template <int D>
