@@ -44,6 +44,26 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned b
     : "memory");
 }
 
+// Opaque copy of a CUtensorMap (128 bytes, 64-byte aligned), so that kernel
+// headers need not include the driver API.  Passed to kernels as a
+// __grid_constant__ parameter.
+struct alignas(64) TensorMap
+{
+  unsigned long long v[16];
+};
+
+// One tiled tensor copy of the box at coordinates (x, y) of a 2-D tensor map
+// into shared memory (128-byte aligned), completing on `bar`.  x times the
+// element size is a multiple of 16 bytes.
+__device__ __forceinline__ void bulk_tensor_2d(void* dst, const TensorMap* map, int x, int y, uint64_t* bar)
+{
+  asm volatile(
+    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+      smem_addr(dst)),
+    "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+    : "memory");
+}
+
 // Arms the barrier for `bytes` and issues one bulk copy of that size.
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar)
 {

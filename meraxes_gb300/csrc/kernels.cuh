@@ -167,7 +167,11 @@ struct EvolveArgs
   unsigned int* err;      // error word: bit 1 iteration cap, bit 2 a shell-copy wait timed out
   int n_shells;           // S of *cst (sizes the shared-memory shell ring)
 };
-void launch_evolve(const EvolveArgs& a, const GridDims& gd, cudaStream_t s);
+// shell_map: 2-D tensor map of the shells (cells x shells, box EV_TILE x S;
+// ev_shell_map_ok() says when one applies), or nullptr for one bulk copy per
+// shell row
+bool ev_shell_map_ok(long long N, int S);
+void launch_evolve(const EvolveArgs& a, const GridDims& gd, const void* shell_map, cudaStream_t s);
 
 // Adjoint of the per-cell spin-temperature update and of the 21cm box.
 struct AdjointArgs
@@ -191,7 +195,7 @@ struct AdjointArgs
   unsigned int* err;
   int n_shells;
 };
-void launch_evolve_adjoint(const AdjointArgs& a, const GridDims& gd, cudaStream_t s);
+void launch_evolve_adjoint(const AdjointArgs& a, const GridDims& gd, const void* shell_map, cudaStream_t s);
 // grad (PADDED) += alpha * (v (PADDED) + u0 (REAL)) at the cells, alpha = a_first
 // on the first D*D*(D/2+1) floats of the padded array, a_second after
 void launch_adjoint_axpy(float* grad, const float* v, const float* u0, float a_first, float a_second,

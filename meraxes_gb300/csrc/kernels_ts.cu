@@ -9,6 +9,7 @@
 // reference's 1e-3 criterion (those cells are recomputed in FP64 so that they
 // stop after the same iteration as the reference).
 #include <cmath>
+#include <cstring>
 
 #include "bulk.cuh"
 #include "kernels.cuh"
@@ -236,31 +237,49 @@ __device__ bool get_Ts_f(const TsDevConst& c, float delta, float TK, float xe, f
 // into shared memory by bulk copies through a two-stage ring, so the shell
 // reads do not depend on how many loads each thread keeps in flight; the next
 // tile's copies run while the current tile is computed.
+// With a tensor map of the shells (cells x shells) a tile's S rows arrive
+// by one tiled tensor copy of the box (EV_TILE cells, S shells); the copy
+// engine's cost per copy made the S separate row copies the bound of the
+// ring.  The map applies when every tile is whole, the cell coordinate fits
+// a signed 32-bit index and S fits a box dimension.
 constexpr int EV_TILE = RED_THREADS;
 
-__device__ __forceinline__ void ev_issue(uint64_t* bars, float* stages, const float* shells, int S, long long N,
-                                         long long tile, int k)
+bool ev_shell_map_ok(long long N, int S) { return N % EV_TILE == 0 && N < (1LL << 31) && S >= 1 && S <= 256; }
+
+// shared-memory offset (floats) of the shell ring of k_evolve_f32: after the
+// tables, on a 128-byte boundary for the tensor copies
+__host__ __device__ constexpr int ev_ring_offset(int S) { return (ev_tables_floats(S) + 31) / 32 * 32; }
+
+__device__ __forceinline__ void ev_issue(uint64_t* bars, float* stages, const float* shells, const bulk::TensorMap* map,
+                                         int S, long long N, long long tile, int k)
 {
   const long long c0 = tile * EV_TILE;
-  const int n = (int)((N - c0) < EV_TILE ? (N - c0) : EV_TILE);
   float* st = stages + (size_t)(k & 1) * S * EV_TILE;
   uint64_t* bar = &bars[k & 1];
+  if (map) {
+    bulk::mbar_arm(bar, (unsigned)(sizeof(float) * EV_TILE * S));
+    bulk::bulk_tensor_2d(st, map, (int)c0, 0, bar);
+    return;
+  }
+  const int n = (int)((N - c0) < EV_TILE ? (N - c0) : EV_TILE);
   bulk::mbar_arm(bar, (unsigned)(sizeof(float) * n * S));
   for (int r = 0; r < S; r++)
     bulk::bulk_copy(st + r * EV_TILE, shells + (long long)r * N + c0, (unsigned)(sizeof(float) * n), bar);
 }
 
-__global__ void __launch_bounds__(RED_THREADS) k_evolve_f32(EvolveArgs a, int D, int H, long long N)
+__global__ void __launch_bounds__(RED_THREADS)
+  k_evolve_f32(EvolveArgs a, int D, int H, long long N, const __grid_constant__ bulk::TensorMap shell_map, int use_map)
 {
+  const bulk::TensorMap* map = use_map ? &shell_map : nullptr;
   const TsDevConst& c = *a.cst;
   const int S = c.S;
   // frequency tables times the shell coefficients, P[x][r] = (K_H tab_H,
   // K_I tab_I, K_L tab_L, K_S) at node x of the x_HII table, then the shell
   // ring.  The interpolation in x_HII is linear, so a cell's sums are
   // (1 - w) sum_r shell_r P[lo][r] + w sum_r shell_r P[hi][r].
-  extern __shared__ __align__(16) float sm[];
+  extern __shared__ __align__(128) float sm[];
   float4* s_P = reinterpret_cast<float4*>(sm);  // NXHII * S
-  float* stages = sm + ev_tables_floats(S);     // 2 * S * EV_TILE
+  float* stages = sm + ev_ring_offset(S);       // 2 * S * EV_TILE
   __shared__ uint64_t bars[2];
   for (int i = threadIdx.x; i < NXHII * S; i += blockDim.x) {
     const int x = i / S, r = i % S;
@@ -278,8 +297,20 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_f32(EvolveArgs a, int D,
   __syncthreads();
   if (threadIdx.x == 0 && light)
     for (int k = 0; k < 2 && k < my_tiles; k++)
-      ev_issue(bars, stages, a.shells, S, N, blockIdx.x + (long long)k * gridDim.x, k);
+      ev_issue(bars, stages, a.shells, map, S, N, blockIdx.x + (long long)k * gridDim.x, k);
   double acc[4] = { 0, 0, 0, 0 };
+  // the cell state of tile k + 1 is read while tile k is computed
+  float n_delta = 0.f, n_xe = 0.f, n_T = 1.f;
+  auto read_state = [&](int k) {
+    const long long ir = (blockIdx.x + (long long)k * gridDim.x) * EV_TILE + threadIdx.x;
+    if (k < my_tiles && ir < N) {
+      const long long ip = pad_index(ir, D, H);
+      n_delta = a.deltax[ip];
+      n_xe = a.x_e_prev[ip];
+      n_T = a.Tk[ir];
+    }
+  };
+  read_state(0);
   for (int k = 0; k < my_tiles; k++) {
     const long long tile = blockIdx.x + (long long)k * gridDim.x;
     const long long ir = tile * EV_TILE + threadIdx.x;
@@ -287,10 +318,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_f32(EvolveArgs a, int D,
     const long long ip = valid ? pad_index(ir, D, H) : 0;
     float delta = 0.f, xe = 0.f, T = 1.f;
     if (valid) {
-      delta = a.deltax[ip];
-      xe = a.x_e_prev[ip];
-      T = a.Tk[ir];
+      delta = n_delta;
+      xe = n_xe;
+      T = n_T;
     }
+    read_state(k + 1);
     // interpolation bracket in x_HII (ComputeTs.c:761-773)
     float xcall = xe;
     if (xcall > c.xhii[NXHII - 1] * 0.999f)
@@ -336,7 +368,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_f32(EvolveArgs a, int D,
       // every thread has read stage k & 1: refill it with tile k + 2
       __syncthreads();
       if (threadIdx.x == 0 && k + 2 < my_tiles)
-        ev_issue(bars, stages, a.shells, S, N, tile + 2LL * gridDim.x, k + 2);
+        ev_issue(bars, stages, a.shells, map, S, N, tile + 2LL * gridDim.x, k + 2);
     }
     if (!valid)
       continue;
@@ -375,11 +407,14 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_f32(EvolveArgs a, int D,
   block_sum_store<4>(acc, a.partials);
 }
 
-void launch_evolve(const EvolveArgs& a, const GridDims& gd, cudaStream_t s)
+void launch_evolve(const EvolveArgs& a, const GridDims& gd, const void* shell_map, cudaStream_t s)
 {
-  const size_t smem = sizeof(float) * (ev_tables_floats(a.n_shells) + 2 * (size_t)a.n_shells * EV_TILE);
+  const size_t smem = sizeof(float) * (ev_ring_offset(a.n_shells) + 2 * (size_t)a.n_shells * EV_TILE);
   cudaFuncSetAttribute(k_evolve_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_evolve_f32<<<RED_BLOCKS, RED_THREADS, smem, s>>>(a, gd.D, gd.H, gd.N);
+  bulk::TensorMap map{};
+  if (shell_map)
+    std::memcpy(&map, shell_map, sizeof(map));
+  k_evolve_f32<<<RED_BLOCKS, RED_THREADS, smem, s>>>(a, gd.D, gd.H, gd.N, map, shell_map ? 1 : 0);
   ts_launches++;
 }
 
@@ -517,14 +552,19 @@ __device__ TsGrad get_Ts_grad(const TsDevConst& c, float delta, float TK, float 
 // dL/d(shell), zero where the shell was clamped at 0.  Per block: sums of
 // heat_bar * heat + ion_bar * ion + lya_bar * lya (the L_X term) and of the
 // E0 term with the dP/dE0 tables.
-__global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, int D, int H, long long N)
+__global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, int D, int H, long long N,
+                                                                 const __grid_constant__ bulk::TensorMap shell_map,
+                                                                 int use_map)
 {
+  // the gradients of tile k are written in place while the tensor copies
+  // read tiles k + 1 and k + 2: different cells
+  const bulk::TensorMap* map = use_map ? &shell_map : nullptr;
   const TsDevConst& c = *a.cst;
   const int S = c.S;
-  extern __shared__ __align__(16) float sm[];
+  extern __shared__ __align__(128) float sm[];
   float4* s_P = reinterpret_cast<float4*>(sm);              // NXHII * S
   float4* s_dP = s_P + NXHII * S;                            // NXHII * S (d/dE0; w unused)
-  float* stages = sm + 2 * ev_tables_floats(S);              // 2 * S * EV_TILE
+  float* stages = sm + (2 * ev_tables_floats(S) + 31) / 32 * 32;  // 2 * S * EV_TILE, 128-byte aligned
   __shared__ uint64_t bars[2];
   for (int i = threadIdx.x; i < NXHII * S; i += blockDim.x) {
     const int x = i / S, r = i % S;
@@ -543,7 +583,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, i
   __syncthreads();
   if (threadIdx.x == 0 && light)
     for (int k = 0; k < 2 && k < my_tiles; k++)
-      ev_issue(bars, stages, a.shells, S, N, blockIdx.x + (long long)k * gridDim.x, k);
+      ev_issue(bars, stages, a.shells, map, S, N, blockIdx.x + (long long)k * gridDim.x, k);
   double acc[2] = { 0, 0 };
   for (int k = 0; k < my_tiles; k++) {
     const long long tile = blockIdx.x + (long long)k * gridDim.x;
@@ -679,7 +719,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, i
       }
       __syncthreads();
       if (threadIdx.x == 0 && k + 2 < my_tiles)
-        ev_issue(bars, stages, a.shells, S, N, tile + 2LL * gridDim.x, k + 2);
+        ev_issue(bars, stages, a.shells, map, S, N, tile + 2LL * gridDim.x, k + 2);
     }
     if (valid) {
       acc[0] += (double)heat_bar * heat + (double)ion_bar * ion + (double)lya_bar * lya;
@@ -689,11 +729,15 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, i
   block_sum_store<2>(acc, a.partials);
 }
 
-void launch_evolve_adjoint(const AdjointArgs& a, const GridDims& gd, cudaStream_t s)
+void launch_evolve_adjoint(const AdjointArgs& a, const GridDims& gd, const void* shell_map, cudaStream_t s)
 {
-  const size_t smem = sizeof(float) * (2 * ev_tables_floats(a.n_shells) + 2 * (size_t)a.n_shells * EV_TILE);
+  const size_t smem =
+    sizeof(float) * ((2 * ev_tables_floats(a.n_shells) + 31) / 32 * 32 + 2 * (size_t)a.n_shells * EV_TILE);
   cudaFuncSetAttribute(k_evolve_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_evolve_adjoint<<<RED_BLOCKS, RED_THREADS, smem, s>>>(a, gd.D, gd.H, gd.N);
+  bulk::TensorMap map{};
+  if (shell_map)
+    std::memcpy(&map, shell_map, sizeof(map));
+  k_evolve_adjoint<<<RED_BLOCKS, RED_THREADS, smem, s>>>(a, gd.D, gd.H, gd.N, map, shell_map ? 1 : 0);
   ts_launches++;
 }
 

@@ -1,6 +1,8 @@
 // C ABI of the GB300 reionization grid step (include/mx_reion.h):
 // context, device memory plan, cuFFT plans and the orchestration of
 // find_HII_bubbles, ComputeTs and the brightness-temperature box.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
 
@@ -22,6 +24,7 @@
 #include "pecvel.cuh"
 #include "ps.cuh"
 #include "host_physics.h"
+#include "bulk.cuh"
 #include "kernels.cuh"
 #include "mx_reion.h"
 
@@ -76,6 +79,10 @@ struct mx_ctx
   bool fused_fft = false;
   // threads per block of the fused x- and y-pass, chosen by tune_fft()
   int x_threads = 512, y_threads = 256;
+  // 2-D tensor map of d_shells (cells x shells) for the evolve kernel's tile
+  // copies (make_shell_map), when one applies
+  bulk::TensorMap shell_map{};
+  bool has_shell_map = false;
 
   RecombTable rr;
   HeatTables ht;
@@ -134,6 +141,7 @@ struct mx_ctx
 
   ~mx_ctx();
   void alloc_scratch();
+  void make_shell_map();
   cufftHandle c2r_plan(long long batch);
   void ensure_mirror();
 };
@@ -217,6 +225,38 @@ mx_ctx::~mx_ctx()
 
 static int n_fields(const mx_params& p) { return 3 + (p.flag_spin_temp ? 1 : 0) + (p.flag_recombinations ? 1 : 0); }
 
+// The evolve kernel's tensor map of the shells: a 2-D FP32 tensor of N cells
+// (inner) by S shells (rows N * 4 bytes apart), box EV_TILE x S.  Encoded
+// through the runtime's driver entry point, so the library does not link the
+// driver API.  Left out (per-row bulk copies instead) when it does not apply
+// or MX_SHELL_MAP=0.
+void mx_ctx::make_shell_map()
+{
+  has_shell_map = false;
+  const int S = p.ts_num_filter_steps;
+  const char* env = std::getenv("MX_SHELL_MAP");
+  if ((env && std::string(env) == "0") || !ev_shell_map_ok(gd.N, S))
+    return;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q{};
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return;
+  static_assert(sizeof(CUtensorMap) == sizeof(bulk::TensorMap), "tensor map size");
+  CUtensorMap m;
+  const cuuint64_t dims[2] = { (cuuint64_t)gd.N, (cuuint64_t)S };
+  const cuuint64_t strides[1] = { (cuuint64_t)gd.N * sizeof(float) };
+  const cuuint32_t box[2] = { (cuuint32_t)RED_THREADS, (cuuint32_t)S };
+  const cuuint32_t estr[2] = { 1, 1 };
+  const CUresult r = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn)(
+    &m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, d_shells, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return;
+  std::memcpy(&shell_map, &m, sizeof(m));
+  has_shell_map = true;
+}
+
 void mx_ctx::alloc_scratch()
 {
   const int G = n_fields(p);
@@ -255,6 +295,7 @@ void mx_ctx::alloc_scratch()
     MX_CUDA(cudaMalloc(&d_tsc, sizeof(TsDevConst)));
     MX_CUDA(cudaMallocHost(&h_tsc, sizeof(TsDevConst)));
     MX_CUDA(cudaMalloc(&d_shells, sizeof(float) * gd.N * (size_t)p.ts_num_filter_steps));
+    make_shell_map();
   }
   // forward transform: padded real input -> half spectrum (out of place)
   int n[3] = { gd.D, gd.D, gd.D };
@@ -883,7 +924,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     ea.n_shells = S;
     {
       Prof pr(c, "k_evolve", ((double)S + 6.0) * 4.0 * (double)gd.N, s);
-      launch_evolve(ea, gd, s);
+      launch_evolve(ea, gd, c->has_shell_map ? &c->shell_map : nullptr, s);
     }
     launch_finalize(c->d_partials, 4, c->d_sums + 8, s);
     MX_CUDA(cudaMemcpyAsync(c->h_sums + 8, c->d_sums + 8, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
@@ -1341,7 +1382,7 @@ static void run_adjoint(mx_ctx* c, int snapshot, const mx_grids* g, const float*
   MX_CUDA(cudaMemsetAsync(grad_stars, 0, sizeof(float) * gd.P, s));
   {
     Prof pr(c, "k_evolve_adjoint", ((double)S * 2 + 10.0) * 4.0 * (double)gd.N, s);
-    launch_evolve_adjoint(a, gd, s);
+    launch_evolve_adjoint(a, gd, c->has_shell_map ? &c->shell_map : nullptr, s);
   }
   launch_finalize(c->d_partials, 2, c->d_sums, s);
   // dL/d(shell) -> dL/d(sfr): each group of shells sharing a spectrum is a sum

@@ -127,6 +127,38 @@ def test_fft_block_sizes_give_identical_results(name, D, monkeypatch):
     tuned.close()
 
 
+# The evolve kernel takes each tile's shell rows by one tensor copy when the
+# context has a tensor map of the shells, else by one bulk copy per row
+# (MX_SHELL_MAP=0); the shared-memory tiles, hence the grids, are the same.
+@pytest.mark.parametrize("name,D", [("evolve16", 32), ("full24", 64)])
+def test_shell_map_gives_identical_results(name, D, monkeypatch):
+    from cases import initial
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+
+    c = CASES[name]
+    w = Case(name, c.base, D, c.overrides, c.fesc, c.snapshots).workload()
+    runs = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("MX_SHELL_MAP", flag)
+        step = ReionGridStep(w.params, w.redshifts)
+        gen = syn.FieldGenerator(w)
+        st = initial(w, step.n_sfr_histories)
+        glob = []
+        for s in w.snapshots:
+            st.update(gen.inputs(s, step.n_sfr_histories))
+            glob.append(step.step(s, st))
+        runs.append((st, glob))
+        step.close()
+    (sa, ga), (sb, gb) = runs
+    for k in OUTPUT_GRIDS:
+        if k in sa:
+            assert np.array_equal(sa[k], sb[k]), k
+    for a, b in zip(ga, gb):
+        for k in ("volume_weighted_global_xH", "volume_ave_TS", "volume_ave_Tb"):
+            assert a[k] == b[k], k
+
+
 def test_device_entry_points_match_host_entry_points():
     import torch
 
