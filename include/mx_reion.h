@@ -169,6 +169,40 @@ int mx_create(const mx_params* params, const char* tables_dir, mx_ctx** out);
  * the free device memory for it.  No reference counterpart. */
 int mx_create_limited(const mx_params* params, const char* tables_dir, size_t max_work_bytes, mx_ctx** out);
 void mx_destroy(mx_ctx* ctx);
+
+/* ---------------------------------------------------------------------------
+ * Batch of independent boxes (no reference counterpart: the reference runs one
+ * box per process).  Each item is one box's mx_step: its own configuration
+ * (grid size, physics, X-ray parameters), redshift list, snapshot and host
+ * grids (updated in place as by mx_step).
+ *
+ * mx_batch_run steps every item on up to max_workers host threads (0: one
+ * per item, at most 8).  Each worker owns its contexts (mx_create_limited
+ * with max_work_bytes; 0: 200 D^2 (D/2 + 16) bytes, about 25 spectra) and
+ * CUDA stream, so the boxes' kernels overlap on the GPU.  Items are taken in
+ * an order that keeps equal configurations together; a worker reuses its
+ * context for an item whose parameters differ only in lx_gal and
+ * nu_xray_gal_threshold, after clearing the per-box history (collapse
+ * fractions of earlier snapshots, light cone) and setting the item's
+ * redshifts and X-ray parameters.  An item's result does not depend on the
+ * packing.  Returns MX_OK when every item succeeded, else the code of the
+ * first failed item (in item order); items[i].status holds each item's code
+ * and mx_batch_last_error() the first failure's message.
+ * ------------------------------------------------------------------------- */
+typedef struct mx_batch_item
+{
+  const mx_params* params;
+  const double* redshifts; /* run_globals.ZZ of the box */
+  int32_t n_snaps;
+  int32_t snapshot;
+  const mx_grids* grids;   /* host pointers */
+  mx_globals* out;         /* may be NULL */
+  int32_t status;          /* written by mx_batch_run */
+} mx_batch_item;
+
+int mx_batch_run(mx_batch_item* items, int32_t n_items, const char* tables_dir, int32_t max_workers,
+                 size_t max_work_bytes);
+const char* mx_batch_last_error(void);
 const char* mx_last_error(const mx_ctx* ctx); /* ctx may be NULL: last mx_create error */
 
 /* run_globals.ZZ: redshift of every snapshot (descending).  Also computes the

@@ -27,8 +27,16 @@ EXPORTS = [
     "mx_lightcone_init", "mx_ConstructLightcone", "mx_ConstructLightcone_device",
     "mx_construct_baryon_grids", "mx_construct_baryon_grids_device", "mx_calculate_Mvir_crit",
     "mx_calculate_Mvir_crit_device", "mx_set_xray_params", "mx_ps_loss_device", "mx_adjoint_device",
-    "mx_create_limited", "mx_fft_block_sizes",
+    "mx_create_limited", "mx_fft_block_sizes", "mx_batch_run", "mx_batch_last_error",
 ]
+
+
+class MxBatchItem(ctypes.Structure):
+    """ctypes image of `mx_batch_item` (include/mx_reion.h)."""
+
+    _fields_ = [("params", ctypes.POINTER(MxParams)), ("redshifts", ctypes.POINTER(ctypes.c_double)),
+                ("n_snaps", ctypes.c_int32), ("snapshot", ctypes.c_int32), ("grids", ctypes.POINTER(MxGrids)),
+                ("out", ctypes.POINTER(MxGlobals)), ("status", ctypes.c_int32)]
 
 
 class MxKernelStat(ctypes.Structure):
@@ -117,6 +125,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mx_calculate_Mvir_crit_device.restype = ctypes.c_int
         L.mx_create_limited.argtypes = [ctypes.POINTER(MxParams), ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(P)]
         L.mx_create_limited.restype = ctypes.c_int
+        L.mx_batch_run.argtypes = [ctypes.POINTER(MxBatchItem), ctypes.c_int32, ctypes.c_char_p, ctypes.c_int32,
+                                   ctypes.c_size_t]
+        L.mx_batch_run.restype = ctypes.c_int
+        L.mx_batch_last_error.argtypes = []
+        L.mx_batch_last_error.restype = ctypes.c_char_p
         L.mx_set_xray_params.argtypes = [P, ctypes.c_double, ctypes.c_double]
         L.mx_set_xray_params.restype = ctypes.c_int
         L.mx_ps_loss_device.argtypes = [P, P, ctypes.c_int32, ctypes.POINTER(ctypes.c_float),

@@ -16,7 +16,8 @@
 namespace mx {
 
 namespace {
-int dep_launches = 0;
+// per host thread: a call counts its own launches when contexts run concurrently
+thread_local int dep_launches = 0;
 
 int key_bits(long long n_cells)
 {

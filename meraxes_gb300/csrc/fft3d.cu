@@ -55,7 +55,8 @@ constexpr int FFT_THREADS = 256;
 constexpr float REL_TOL_F = 1e-5f;
 constexpr float ABS_TOL_F = 1e-8f;
 constexpr double PI_D = 3.14159265358979323846;
-int fft_launches = 0;
+// per host thread: a call counts its own launches when contexts run concurrently
+thread_local int fft_launches = 0;
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {

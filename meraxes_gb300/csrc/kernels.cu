@@ -17,7 +17,8 @@
 namespace mx {
 
 namespace {
-int g_launches = 0;
+// per host thread: a call counts its own launches when contexts run concurrently
+thread_local int g_launches = 0;
 
 constexpr float REL_TOL = 1e-5f;
 constexpr float ABS_TOL = 1e-8f;

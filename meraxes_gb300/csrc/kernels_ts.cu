@@ -25,7 +25,8 @@ constexpr float MAX_TK = 5e4f;
 constexpr double FRACT_FLOAT_ERR = 1e-7;
 constexpr int TS_MAX_ITER = 10000;
 
-int ts_launches = 0;
+// per host thread: a call counts its own launches when contexts run concurrently
+thread_local int ts_launches = 0;
 
 template <int NV>
 __device__ void block_sum_store(double (&v)[NV], double* partials)

@@ -9,7 +9,8 @@
 namespace mx {
 
 namespace {
-int lc_launches = 0;
+// per host thread: a call counts its own launches when contexts run concurrently
+thread_local int lc_launches = 0;
 
 __global__ void k_lightcone(LightconeArgs a, int D)
 {

@@ -7,11 +7,13 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <future>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <new>
 #include <string>
@@ -2503,6 +2505,147 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
     if (out)
       out->gpu_launches = launches;
   });
+}
+
+}  // extern "C"
+
+// =================================================================== batch
+// mx_batch_run: independent boxes on a pool of host threads, each with its
+// own contexts and streams (include/mx_reion.h).
+namespace {
+std::mutex g_batch_mu;
+std::string g_batch_error;
+int g_batch_error_item = -1;
+
+void batch_fail(int item, const std::string& msg)
+{
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  if (g_batch_error_item < 0 || item < g_batch_error_item) {
+    g_batch_error_item = item;
+    g_batch_error = "item " + std::to_string(item) + ": " + msg;
+  }
+}
+
+// The configuration a context is built for: the item's parameters with
+// those a context takes per item (the X-ray parameters) cleared.
+mx_params batch_key(const mx_params& p)
+{
+  mx_params k;
+  std::memcpy(&k, &p, sizeof(k));
+  k.lx_gal = 0.0;
+  k.nu_xray_gal_threshold = 0.0;
+  return k;
+}
+
+struct BatchWorker
+{
+  mx_ctx* ctx = nullptr;
+  mx_params key{};
+};
+
+void batch_item(BatchWorker& w, mx_batch_item& it, int index, const char* tables_dir, size_t max_work_bytes)
+{
+  if (!it.params || !it.redshifts || !it.grids) {
+    it.status = MX_EINVAL;
+    batch_fail(index, "NULL params, redshifts or grids");
+    return;
+  }
+  const mx_params key = batch_key(*it.params);
+  if (w.ctx && std::memcmp(&key, &w.key, sizeof(key)) == 0) {
+    // same configuration: clear the previous box's history
+    std::memset(w.ctx->stored_fcoll, 0, sizeof(w.ctx->stored_fcoll));
+    w.ctx->lc_length = -1;
+    w.ctx->lc_pos = 0;
+    w.ctx->lc_end_snapshot = 0;
+    w.ctx->p.lx_gal = it.params->lx_gal;
+    w.ctx->p.nu_xray_gal_threshold = it.params->nu_xray_gal_threshold;
+  } else {
+    if (w.ctx) {
+      mx_destroy(w.ctx);
+      w.ctx = nullptr;
+    }
+    const double D = it.params->grid_dim;
+    const size_t cap = max_work_bytes ? max_work_bytes : (size_t)(200.0 * D * D * (D / 2 + 16));
+    const int rc = create_ctx(it.params, tables_dir, cap, &w.ctx);
+    if (rc != MX_OK) {
+      it.status = rc;
+      batch_fail(index, g_create_error);
+      w.ctx = nullptr;
+      return;
+    }
+    w.key = key;
+  }
+  int rc = mx_set_redshifts(w.ctx, it.redshifts, it.n_snaps);
+  mx_globals scratch{};
+  if (rc == MX_OK)
+    rc = mx_step(w.ctx, it.snapshot, it.grids, it.out ? it.out : &scratch);
+  it.status = rc;
+  if (rc != MX_OK)
+    batch_fail(index, w.ctx->err);
+}
+}  // namespace
+
+extern "C" {
+
+int mx_batch_run(mx_batch_item* items, int32_t n_items, const char* tables_dir, int32_t max_workers,
+                 size_t max_work_bytes)
+{
+  {
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    g_batch_error.clear();
+    g_batch_error_item = -1;
+  }
+  if (n_items < 0 || (n_items > 0 && !items)) {
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    g_batch_error = "mx_batch_run: bad item list";
+    return MX_EINVAL;
+  }
+  if (n_items == 0)
+    return MX_OK;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    g_batch_error = "mx_batch_run: no CUDA device";
+    return MX_ECUDA;
+  }
+  // equal configurations next to each other (ties in item order)
+  std::vector<int> order(n_items);
+  std::vector<mx_params> keys(n_items);
+  for (int i = 0; i < n_items; i++) {
+    order[i] = i;
+    if (items[i].params)
+      keys[i] = batch_key(*items[i].params);
+    else
+      std::memset(&keys[i], 0, sizeof(mx_params));
+  }
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return std::memcmp(&keys[a], &keys[b], sizeof(mx_params)) < 0; });
+  const int workers = max_workers > 0 ? std::min<int>(max_workers, n_items) : std::min<int>(n_items, 8);
+  std::atomic<int> next{ 0 };
+  auto work = [&]() {
+    cudaSetDevice(device);
+    BatchWorker w;
+    for (int j = next++; j < n_items; j = next++)
+      batch_item(w, items[order[j]], order[j], tables_dir, max_work_bytes);
+    if (w.ctx)
+      mx_destroy(w.ctx);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < workers; t++)
+    pool.emplace_back(work);
+  work();
+  for (std::thread& th : pool)
+    th.join();
+  for (int i = 0; i < n_items; i++)
+    if (items[i].status != MX_OK)
+      return items[i].status;
+  return MX_OK;
+}
+
+const char* mx_batch_last_error(void)
+{
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  return g_batch_error.c_str();
 }
 
 }  // extern "C"

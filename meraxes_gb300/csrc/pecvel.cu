@@ -20,7 +20,8 @@
 namespace mx {
 
 namespace {
-int pv_launches = 0;
+// per host thread: a call counts its own launches when contexts run concurrently
+thread_local int pv_launches = 0;
 constexpr double FRACT_FLOAT_ERR_D = 1e-7;
 constexpr double MPC_CM = 3.086e24;
 

@@ -19,7 +19,8 @@
 namespace mx {
 
 namespace {
-int ps_launches = 0;
+// per host thread: a call counts its own launches when contexts run concurrently
+thread_local int ps_launches = 0;
 
 __global__ void k_ps_sum(const float* __restrict__ dT, long long N, double* partials)
 {

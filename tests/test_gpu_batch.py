@@ -27,3 +27,65 @@ def test_batch_matches_single_box_runs():
         alone = BatchRunner([inst], max_workers_per_size=1).run()["results"][0]
         assert res == alone, (inst, res, alone)
         assert res["loss"] > 0 and res["dL_dLX"] != 0 and res["dL_dfesc"] != 0
+
+
+def _native_items(specs):
+    """Batch items for run_batch: (case name, grid size, L_X) -> params,
+    redshifts, first snapshot and host grids of that case."""
+    import dataclasses
+
+    from cases import CASES, Case, initial
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+
+    items = []
+    for name, D, lx in specs:
+        c = CASES[name]
+        w = Case(name, c.base, D, c.overrides, c.fesc, c.snapshots).workload()
+        p = w.params
+        if lx is not None:
+            p = dataclasses.replace(p, lx_gal=lx)
+        n_hist = ReionGridStep(p, w.redshifts).n_sfr_histories
+        st = initial(w, n_hist)
+        s = w.snapshots[0]
+        st.update(syn.FieldGenerator(w).inputs(s, n_hist))
+        items.append({"params": p, "redshifts": w.redshifts, "snapshot": s, "grids": st})
+    return items
+
+
+def test_native_batch_matches_single_box_runs():
+    """mx_batch_run: boxes of two sizes and two X-ray luminosities on 3
+    workers (contexts reused across the luminosities) give each box's grids
+    and globals bit for bit as ReionGridStep.step of that box alone."""
+    import numpy as np
+
+    from meraxes_gb300.api import ReionGridStep, run_batch
+
+    specs = [("full24", 32, 1e40), ("full24", 48, 1e40), ("full24", 32, 3e40), ("full24", 48, 3e40),
+             ("plain32_tophat", 64, None)]
+    items = _native_items(specs)
+    alone = []
+    for it in items:
+        g = {k: v.copy() for k, v in it["grids"].items()}
+        step = ReionGridStep(it["params"], it["redshifts"])
+        glob = step.step(it["snapshot"], g)
+        step.close()
+        alone.append((g, glob))
+    outs = run_batch(items, max_workers=3)
+    for it, out, (g, glob) in zip(items, outs, alone):
+        for k in g:
+            assert np.array_equal(it["grids"][k], g[k]), k
+        for k in ("volume_weighted_global_xH", "volume_ave_TS", "volume_ave_Tb"):
+            assert out[k] == glob[k], k
+
+
+def test_native_batch_reports_failed_items():
+    """A bad item fails alone: its status is reported, the others run."""
+    from meraxes_gb300 import _lib
+    from meraxes_gb300.api import run_batch
+
+    items = _native_items([("plain32_tophat", 32, None), ("plain32_tophat", 32, None)])
+    items[1]["snapshot"] = 999  # beyond the redshift list
+    with pytest.raises(_lib.MxError) as e:
+        run_batch(items, max_workers=2)
+    assert e.value.code == -1 and "item 1" in str(e.value)
