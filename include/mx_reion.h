@@ -176,18 +176,21 @@ void mx_destroy(mx_ctx* ctx);
  * (grid size, physics, X-ray parameters), redshift list, snapshot and host
  * grids (updated in place as by mx_step).
  *
- * mx_batch_run steps every item on up to max_workers host threads (0: one
- * per item, at most 8).  Each worker owns its contexts (mx_create_limited
- * with max_work_bytes; 0: 200 D^2 (D/2 + 16) bytes, about 25 spectra) and
- * CUDA stream, so the boxes' kernels overlap on the GPU.  Items are taken in
- * an order that keeps equal configurations together; a worker reuses its
- * context for an item whose parameters differ only in lx_gal and
- * nu_xray_gal_threshold, after clearing the per-box history (collapse
+ * A batch object owns up to max_workers workers (0: 8), each with its own
+ * contexts (mx_create_limited with max_work_bytes; 0: 200 D^2 (D/2 + 16)
+ * bytes, about 25 spectra) and CUDA stream.  mx_batch_run steps every item on
+ * concurrent host threads, so the boxes' kernels overlap on the GPU.  Items
+ * of one configuration (the parameters apart from lx_gal and
+ * nu_xray_gal_threshold) form a group; the workers are split over the groups
+ * in proportion to their items, and a group's items go to its workers in
+ * turn.  A worker keeps its context between items and between runs while the
+ * configuration stays the same, clearing the per-box history (collapse
  * fractions of earlier snapshots, light cone) and setting the item's
- * redshifts and X-ray parameters.  An item's result does not depend on the
- * packing.  Returns MX_OK when every item succeeded, else the code of the
- * first failed item (in item order); items[i].status holds each item's code
- * and mx_batch_last_error() the first failure's message.
+ * redshifts and X-ray parameters before each item.  An item's result does not
+ * depend on the packing.  mx_batch_run returns MX_OK when every item
+ * succeeded, else the code of the first failed item (in item order);
+ * items[i].status holds each item's code and mx_batch_last_error the first
+ * failure's message.  One mx_batch_run at a time per batch object.
  * ------------------------------------------------------------------------- */
 typedef struct mx_batch_item
 {
@@ -200,9 +203,11 @@ typedef struct mx_batch_item
   int32_t status;          /* written by mx_batch_run */
 } mx_batch_item;
 
-int mx_batch_run(mx_batch_item* items, int32_t n_items, const char* tables_dir, int32_t max_workers,
-                 size_t max_work_bytes);
-const char* mx_batch_last_error(void);
+typedef struct mx_batch mx_batch;
+int mx_batch_create(const char* tables_dir, int32_t max_workers, size_t max_work_bytes, mx_batch** out);
+int mx_batch_run(mx_batch* batch, mx_batch_item* items, int32_t n_items);
+void mx_batch_destroy(mx_batch* batch);
+const char* mx_batch_last_error(const mx_batch* batch);
 const char* mx_last_error(const mx_ctx* ctx); /* ctx may be NULL: last mx_create error */
 
 /* run_globals.ZZ: redshift of every snapshot (descending).  Also computes the

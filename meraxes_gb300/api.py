@@ -329,40 +329,70 @@ class ReionGridStep:
         return gs, gst, par[0], par[1]
 
 
+class Batch:
+    """Native executor of independent boxes (mx_batch_create / mx_batch_run,
+    include/mx_reion.h): worker threads with their own contexts and streams,
+    kept between runs while a worker's configuration stays the same."""
+
+    def __init__(self, tables_dir: str = TABLES_DIR, max_workers: int = 0, max_work_bytes: int = 0):
+        self.lib = _lib.load()
+        self.handle = ctypes.c_void_p()
+        rc = self.lib.mx_batch_create(tables_dir.encode(), int(max_workers), int(max_work_bytes),
+                                      ctypes.byref(self.handle))
+        if rc != 0:
+            raise _lib.MxError(rc, "mx_batch_create")
+
+    def run(self, items):
+        """items: dicts with "params" (ReionParams), "redshifts", "snapshot"
+        and "grids" (name -> C-contiguous float32 numpy array, updated in place
+        as by ReionGridStep.step).  Returns the globals of every item; raises
+        MxError if any item failed (the others still ran)."""
+        n = len(items)
+        arr = (_lib.MxBatchItem * n)()
+        keep = []  # ctypes objects that must outlive the call
+        outs = []
+        for i, it in enumerate(items):
+            pc = it["params"].to_ctypes()
+            zz = (ctypes.c_double * len(it["redshifts"]))(*[float(z) for z in it["redshifts"]])
+            g = MxGrids()
+            for name in GRID_NAMES:
+                a = it["grids"].get(name)
+                if a is None:
+                    continue
+                if not isinstance(a, np.ndarray) or a.dtype != np.float32 or not a.flags.c_contiguous:
+                    raise ValueError(f"item {i}, {name}: need C-contiguous float32 numpy array")
+                setattr(g, name, a.ctypes.data)
+            out = MxGlobals()
+            keep += [pc, zz, g]
+            outs.append(out)
+            arr[i].params = ctypes.pointer(pc)
+            arr[i].redshifts = zz
+            arr[i].n_snaps = len(it["redshifts"])
+            arr[i].snapshot = int(it["snapshot"])
+            arr[i].grids = ctypes.pointer(g)
+            arr[i].out = ctypes.pointer(out)
+            arr[i].status = -99
+        rc = self.lib.mx_batch_run(self.handle, arr, n)
+        if rc != 0:
+            raise _lib.MxError(rc, self.lib.mx_batch_last_error(self.handle).decode())
+        return [o.as_dict() for o in outs]
+
+    def close(self):
+        if self.handle:
+            self.lib.mx_batch_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def run_batch(items, tables_dir: str = TABLES_DIR, max_workers: int = 0, max_work_bytes: int = 0):
-    """Steps a batch of independent boxes through the native executor
-    mx_batch_run (include/mx_reion.h): each item is a dict with "params"
-    (ReionParams), "redshifts", "snapshot" and "grids" (name -> C-contiguous
-    float32 numpy array, updated in place as by ReionGridStep.step).  Returns
-    the globals of every item; raises MxError if any item failed (the others
-    still ran)."""
-    lib = _lib.load()
-    n = len(items)
-    arr = (_lib.MxBatchItem * n)()
-    keep = []  # ctypes objects that must outlive the call
-    outs = []
-    for i, it in enumerate(items):
-        pc = it["params"].to_ctypes()
-        zz = (ctypes.c_double * len(it["redshifts"]))(*[float(z) for z in it["redshifts"]])
-        g = MxGrids()
-        for name in GRID_NAMES:
-            a = it["grids"].get(name)
-            if a is None:
-                continue
-            if not isinstance(a, np.ndarray) or a.dtype != np.float32 or not a.flags.c_contiguous:
-                raise ValueError(f"item {i}, {name}: need C-contiguous float32 numpy array")
-            setattr(g, name, a.ctypes.data)
-        out = MxGlobals()
-        keep += [pc, zz, g]
-        outs.append(out)
-        arr[i].params = ctypes.pointer(pc)
-        arr[i].redshifts = zz
-        arr[i].n_snaps = len(it["redshifts"])
-        arr[i].snapshot = int(it["snapshot"])
-        arr[i].grids = ctypes.pointer(g)
-        arr[i].out = ctypes.pointer(out)
-        arr[i].status = -99
-    rc = lib.mx_batch_run(arr, n, tables_dir.encode(), int(max_workers), int(max_work_bytes))
-    if rc != 0:
-        raise _lib.MxError(rc, lib.mx_batch_last_error().decode())
-    return [o.as_dict() for o in outs]
+    """One-shot Batch(...).run(items)."""
+    b = Batch(tables_dir, max_workers, max_work_bytes)
+    try:
+        return b.run(items)
+    finally:
+        b.close()

@@ -2510,22 +2510,9 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
 }  // extern "C"
 
 // =================================================================== batch
-// mx_batch_run: independent boxes on a pool of host threads, each with its
-// own contexts and streams (include/mx_reion.h).
+// mx_batch_*: independent boxes on a pool of host threads, each with its own
+// contexts and streams (include/mx_reion.h).
 namespace {
-std::mutex g_batch_mu;
-std::string g_batch_error;
-int g_batch_error_item = -1;
-
-void batch_fail(int item, const std::string& msg)
-{
-  std::lock_guard<std::mutex> lk(g_batch_mu);
-  if (g_batch_error_item < 0 || item < g_batch_error_item) {
-    g_batch_error_item = item;
-    g_batch_error = "item " + std::to_string(item) + ": " + msg;
-  }
-}
-
 // The configuration a context is built for: the item's parameters with
 // those a context takes per item (the X-ray parameters) cleared.
 mx_params batch_key(const mx_params& p)
@@ -2542,110 +2529,199 @@ struct BatchWorker
   mx_ctx* ctx = nullptr;
   mx_params key{};
 };
-
-void batch_item(BatchWorker& w, mx_batch_item& it, int index, const char* tables_dir, size_t max_work_bytes)
-{
-  if (!it.params || !it.redshifts || !it.grids) {
-    it.status = MX_EINVAL;
-    batch_fail(index, "NULL params, redshifts or grids");
-    return;
-  }
-  const mx_params key = batch_key(*it.params);
-  if (w.ctx && std::memcmp(&key, &w.key, sizeof(key)) == 0) {
-    // same configuration: clear the previous box's history
-    std::memset(w.ctx->stored_fcoll, 0, sizeof(w.ctx->stored_fcoll));
-    w.ctx->lc_length = -1;
-    w.ctx->lc_pos = 0;
-    w.ctx->lc_end_snapshot = 0;
-    w.ctx->p.lx_gal = it.params->lx_gal;
-    w.ctx->p.nu_xray_gal_threshold = it.params->nu_xray_gal_threshold;
-  } else {
-    if (w.ctx) {
-      mx_destroy(w.ctx);
-      w.ctx = nullptr;
-    }
-    const double D = it.params->grid_dim;
-    const size_t cap = max_work_bytes ? max_work_bytes : (size_t)(200.0 * D * D * (D / 2 + 16));
-    const int rc = create_ctx(it.params, tables_dir, cap, &w.ctx);
-    if (rc != MX_OK) {
-      it.status = rc;
-      batch_fail(index, g_create_error);
-      w.ctx = nullptr;
-      return;
-    }
-    w.key = key;
-  }
-  int rc = mx_set_redshifts(w.ctx, it.redshifts, it.n_snaps);
-  mx_globals scratch{};
-  if (rc == MX_OK)
-    rc = mx_step(w.ctx, it.snapshot, it.grids, it.out ? it.out : &scratch);
-  it.status = rc;
-  if (rc != MX_OK)
-    batch_fail(index, w.ctx->err);
-}
 }  // namespace
+
+struct mx_batch
+{
+  std::string tables_dir;
+  size_t max_work_bytes = 0;
+  int device = 0;
+  std::vector<BatchWorker> workers;
+  std::mutex mu;
+  std::string err;
+  int err_item = -1;
+
+  void fail(int item, const std::string& msg)
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (err_item < 0 || item < err_item) {
+      err_item = item;
+      err = "item " + std::to_string(item) + ": " + msg;
+    }
+  }
+
+  void run_item(BatchWorker& w, mx_batch_item& it, int index)
+  {
+    const mx_params key = batch_key(*it.params);
+    if (w.ctx && std::memcmp(&key, &w.key, sizeof(key)) == 0) {
+      // same configuration: clear the previous box's history
+      std::memset(w.ctx->stored_fcoll, 0, sizeof(w.ctx->stored_fcoll));
+      w.ctx->lc_length = -1;
+      w.ctx->lc_pos = 0;
+      w.ctx->lc_end_snapshot = 0;
+      w.ctx->p.lx_gal = it.params->lx_gal;
+      w.ctx->p.nu_xray_gal_threshold = it.params->nu_xray_gal_threshold;
+    } else {
+      if (w.ctx) {
+        mx_destroy(w.ctx);
+        w.ctx = nullptr;
+      }
+      const double D = it.params->grid_dim;
+      const size_t cap = max_work_bytes ? max_work_bytes : (size_t)(200.0 * D * D * (D / 2 + 16));
+      const int rc = create_ctx(it.params, tables_dir.c_str(), cap, &w.ctx);
+      if (rc != MX_OK) {
+        it.status = rc;
+        fail(index, g_create_error);
+        w.ctx = nullptr;
+        return;
+      }
+      w.key = key;
+    }
+    int rc = mx_set_redshifts(w.ctx, it.redshifts, it.n_snaps);
+    mx_globals scratch{};
+    if (rc == MX_OK)
+      rc = mx_step(w.ctx, it.snapshot, it.grids, it.out ? it.out : &scratch);
+    it.status = rc;
+    if (rc != MX_OK)
+      fail(index, w.ctx->err);
+  }
+};
 
 extern "C" {
 
-int mx_batch_run(mx_batch_item* items, int32_t n_items, const char* tables_dir, int32_t max_workers,
-                 size_t max_work_bytes)
+int mx_batch_create(const char* tables_dir, int32_t max_workers, size_t max_work_bytes, mx_batch** out)
 {
-  {
-    std::lock_guard<std::mutex> lk(g_batch_mu);
-    g_batch_error.clear();
-    g_batch_error_item = -1;
-  }
-  if (n_items < 0 || (n_items > 0 && !items)) {
-    std::lock_guard<std::mutex> lk(g_batch_mu);
-    g_batch_error = "mx_batch_run: bad item list";
+  if (!out || max_workers < 0)
     return MX_EINVAL;
-  }
-  if (n_items == 0)
-    return MX_OK;
-  int device = 0;
-  if (cudaGetDevice(&device) != cudaSuccess) {
-    std::lock_guard<std::mutex> lk(g_batch_mu);
-    g_batch_error = "mx_batch_run: no CUDA device";
+  *out = nullptr;
+  std::unique_ptr<mx_batch> b(new (std::nothrow) mx_batch());
+  if (!b)
+    return MX_ENOMEM;
+  if (cudaGetDevice(&b->device) != cudaSuccess)
     return MX_ECUDA;
-  }
-  // equal configurations next to each other (ties in item order)
-  std::vector<int> order(n_items);
-  std::vector<mx_params> keys(n_items);
-  for (int i = 0; i < n_items; i++) {
-    order[i] = i;
-    if (items[i].params)
-      keys[i] = batch_key(*items[i].params);
-    else
-      std::memset(&keys[i], 0, sizeof(mx_params));
-  }
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int b) { return std::memcmp(&keys[a], &keys[b], sizeof(mx_params)) < 0; });
-  const int workers = max_workers > 0 ? std::min<int>(max_workers, n_items) : std::min<int>(n_items, 8);
-  std::atomic<int> next{ 0 };
-  auto work = [&]() {
-    cudaSetDevice(device);
-    BatchWorker w;
-    for (int j = next++; j < n_items; j = next++)
-      batch_item(w, items[order[j]], order[j], tables_dir, max_work_bytes);
+  b->tables_dir = tables_dir ? tables_dir : "";
+  b->max_work_bytes = max_work_bytes;
+  b->workers.resize(max_workers > 0 ? max_workers : 8);
+  *out = b.release();
+  return MX_OK;
+}
+
+void mx_batch_destroy(mx_batch* b)
+{
+  if (!b)
+    return;
+  cudaSetDevice(b->device);
+  for (BatchWorker& w : b->workers)
     if (w.ctx)
       mx_destroy(w.ctx);
+  delete b;
+}
+
+const char* mx_batch_last_error(const mx_batch* b) { return b ? b->err.c_str() : "mx_batch: NULL batch"; }
+
+int mx_batch_run(mx_batch* b, mx_batch_item* items, int32_t n_items)
+{
+  if (!b)
+    return MX_EINVAL;
+  b->err.clear();
+  b->err_item = -1;
+  if (n_items < 0 || (n_items > 0 && !items)) {
+    b->err = "mx_batch_run: bad item list";
+    return MX_EINVAL;
+  }
+  for (int i = 0; i < n_items; i++)
+    if (!items[i].params || !items[i].redshifts || !items[i].grids) {
+      b->err = "item " + std::to_string(i) + ": NULL params, redshifts or grids";
+      items[i].status = MX_EINVAL;
+      return MX_EINVAL;
+    }
+  if (n_items == 0)
+    return MX_OK;
+  // groups of equal configurations, in order of their first item
+  std::vector<mx_params> gkeys;
+  std::vector<std::vector<int>> groups;
+  for (int i = 0; i < n_items; i++) {
+    const mx_params k = batch_key(*items[i].params);
+    size_t g = 0;
+    while (g < gkeys.size() && std::memcmp(&gkeys[g], &k, sizeof(k)) != 0)
+      g++;
+    if (g == gkeys.size()) {
+      gkeys.push_back(k);
+      groups.emplace_back();
+    }
+    groups[g].push_back(i);
+  }
+  // workers per group in proportion to its items (at least one each, at
+  // most its items); a worker already holding a group's configuration stays
+  // with that group
+  const int W = (int)b->workers.size();
+  const int G = (int)groups.size();
+  std::vector<int> want(G);
+  for (int g = 0; g < G; g++)
+    want[g] = std::max(1, std::min((int)groups[g].size(), (int)((double)W * groups[g].size() / n_items)));
+  std::vector<std::vector<int>> gw(G);  // worker slots of each group
+  std::vector<bool> used(W, false);
+  for (int g = 0; g < G; g++)
+    for (int w = 0; w < W && (int)gw[g].size() < want[g]; w++)
+      if (!used[w] && b->workers[w].ctx && std::memcmp(&b->workers[w].key, &gkeys[g], sizeof(mx_params)) == 0) {
+        gw[g].push_back(w);
+        used[w] = true;
+      }
+  for (int g = 0; g < G; g++)
+    for (int w = 0; w < W && (int)gw[g].size() < want[g]; w++)
+      if (!used[w]) {
+        gw[g].push_back(w);
+        used[w] = true;
+      }
+  // workers left over go, one at a time, to the group with the most items
+  // per worker
+  for (int w = 0; w < W; w++) {
+    if (used[w])
+      continue;
+    int best = -1;
+    double most = 1.0;
+    for (int g = 0; g < G; g++) {
+      const double per = gw[g].empty() ? 1e30 : (double)groups[g].size() / gw[g].size();
+      if (per > most) {
+        most = per;
+        best = g;
+      }
+    }
+    if (best < 0)
+      break;
+    gw[best].push_back(w);
+    used[w] = true;
+  }
+  // more groups than workers: the groups without a worker go to the workers
+  // in turn (run after that worker's own group)
+  std::vector<std::vector<int>> queue(W);
+  std::vector<std::atomic<int>> next(G);
+  for (int g = 0; g < G; g++)
+    next[g] = 0;
+  std::vector<std::vector<int>> wgroups(W);  // groups a worker serves, in order
+  int spill = 0;
+  for (int g = 0; g < G; g++) {
+    if (gw[g].empty())
+      gw[g].push_back(spill++ % W);
+    for (int w : gw[g])
+      wgroups[w].push_back(g);
+  }
+  auto work = [&](int w) {
+    cudaSetDevice(b->device);
+    for (int g : wgroups[w])
+      for (int j = next[g]++; j < (int)groups[g].size(); j = next[g]++)
+        b->run_item(b->workers[w], items[groups[g][j]], groups[g][j]);
   };
   std::vector<std::thread> pool;
-  for (int t = 1; t < workers; t++)
-    pool.emplace_back(work);
-  work();
+  for (int w = 0; w < W; w++)
+    if (!wgroups[w].empty())
+      pool.emplace_back(work, w);
   for (std::thread& th : pool)
     th.join();
   for (int i = 0; i < n_items; i++)
     if (items[i].status != MX_OK)
       return items[i].status;
   return MX_OK;
-}
-
-const char* mx_batch_last_error(void)
-{
-  std::lock_guard<std::mutex> lk(g_batch_mu);
-  return g_batch_error.c_str();
 }
 
 }  // extern "C"

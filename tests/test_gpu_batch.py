@@ -89,3 +89,25 @@ def test_native_batch_reports_failed_items():
     with pytest.raises(_lib.MxError) as e:
         run_batch(items, max_workers=2)
     assert e.value.code == -1 and "item 1" in str(e.value)
+
+
+def test_native_batch_object_reuses_contexts_across_runs():
+    """A Batch object keeps its workers' contexts between runs: a second run
+    on fresh copies of the inputs gives the same grids as the first."""
+    import numpy as np
+
+    from meraxes_gb300.api import Batch
+
+    items = _native_items([("full24", 32, 1e40), ("full24", 32, 2e40), ("plain32_tophat", 48, None)])
+    fresh = [{k: v.copy() for k, v in it["grids"].items()} for it in items]
+    b = Batch(max_workers=2)
+    first = b.run(items)
+    grids_first = [{k: v.copy() for k, v in it["grids"].items()} for it in items]
+    for it, f in zip(items, fresh):
+        it["grids"] = {k: v.copy() for k, v in f.items()}
+    second = b.run(items)
+    b.close()
+    assert first == second
+    for it, g in zip(items, grids_first):
+        for k in g:
+            assert np.array_equal(it["grids"][k], g[k]), k
