@@ -74,6 +74,10 @@ struct mx_ctx
   cudaStream_t stream = nullptr;
   cudaStream_t copy_stream = nullptr;  // host-pointer mx_step: copies that overlap the compute
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+  // host-pointer mx_step: ComputeTs inputs arriving on the copy stream
+  // (TsUploads)
+  cudaEvent_t ev_ts_first = nullptr, ev_ts_sfr = nullptr, ev_ts_tk = nullptr;
+  std::vector<cudaEvent_t> ev_slices;
   int device = 0;
   int nthreads = 4;
   // inverse transforms: fused three-pass kernels for power-of-two grids
@@ -219,6 +223,11 @@ mx_ctx::~mx_ctx()
     cudaEventDestroy(ev_a);
   if (ev_b)
     cudaEventDestroy(ev_b);
+  for (cudaEvent_t e : { ev_ts_first, ev_ts_sfr, ev_ts_tk })
+    if (e)
+      cudaEventDestroy(e);
+  for (cudaEvent_t e : ev_slices)
+    cudaEventDestroy(e);
   if (copy_stream)
     cudaStreamDestroy(copy_stream);
   if (stream)
@@ -720,12 +729,26 @@ static void fill_ts_constants(mx_ctx* c, TsDevConst* t, const ShellPlan& sp, con
   fill_fast_evolve(c, t, sp, ft, zp);
 }
 
+// ComputeTs inputs that a host-pointer call uploads on the copy stream while
+// the compute stream works: `first` (stars, deltax, x_e_box_prev: the
+// collapse fraction and <x_e>), `sfr`, each history slice (slices[j]), and
+// `tk` (Tk_box, read by the per-cell update).  The compute stream waits for
+// each right before its first use.  nullptr: every input is already there.
+struct TsUploads
+{
+  cudaEvent_t first, sfr, tk;
+  const std::vector<cudaEvent_t>* slices;
+};
+
 // Shells of ComputeTs (ComputeTs.c:276-503) into c->d_shells: apply the
 // SFR-history operations to `sfr` (in place, like the reference), forward
 // transform when the grid changed, then filter + inverse transform in
 // batches of shells sharing a spectrum.
-static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sfr_histories, cudaStream_t s)
+static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sfr_histories, cudaStream_t s,
+                           const TsUploads* up = nullptr)
 {
+  if (up)
+    MX_CUDA(cudaStreamWaitEvent(s, up->sfr, 0));
   const mx_params& p = c->p;
   const GridDims& gd = c->gd;
   const int S = p.ts_num_filter_steps;
@@ -734,6 +757,8 @@ static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sf
   int r = 0;
   while (r < S) {
     for (const SfrOp& op : sp.ops[r]) {
+      if (up && op.kind >= SfrOp::LOAD)
+        MX_CUDA(cudaStreamWaitEvent(s, (*up->slices)[op.slice], 0));
       Prof pr(c, "k_sfr_history", op.kind <= SfrOp::ZERO_HALF ? 8.0 * (double)nhalf : 12.0 * (double)gd.N, s);
       if (op.kind == SfrOp::SCALE_HALF)
         launch_sfr_scale_half(sfr, nhalf, op.dweight, s);
@@ -823,7 +848,8 @@ static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sf
   }
 }
 
-static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s)
+static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s,
+                          const TsUploads* up = nullptr)
 {
   const mx_params& p = c->p;
   const GridDims& gd = c->gd;
@@ -849,6 +875,13 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
   const double RtoM_h2 = RtoM(p, c->d, R0) * p.hubble_h * p.hubble_h;
   double collapse_fraction = 0.0, x_e_ave = 0.0;
 
+  if (up) {
+    MX_CUDA(cudaStreamWaitEvent(s, up->first, 0));
+    if (sp.homogeneous) {
+      MX_CUDA(cudaStreamWaitEvent(s, up->sfr, 0));
+      MX_CUDA(cudaStreamWaitEvent(s, up->tk, 0));
+    }
+  }
   if (sp.homogeneous) {
     // ComputeTs.c:189-262
     MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
@@ -905,7 +938,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     // transform when the grid changed, then filter + inverse transform in
     // batches of shells sharing a spectrum.
     try {
-      compute_shells(c, sp, g->sfr, g->sfr_histories, s);
+      compute_shells(c, sp, g->sfr, g->sfr_histories, s, up);
     } catch (...) {
       tables.wait();
       throw;
@@ -924,6 +957,8 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     ea.partials = c->d_partials;
     ea.err = c->d_err;
     ea.n_shells = S;
+    if (up)
+      MX_CUDA(cudaStreamWaitEvent(s, up->tk, 0));
     {
       Prof pr(c, "k_evolve", ((double)S + 6.0) * 4.0 * (double)gd.N, s);
       launch_evolve(ea, gd, c->has_shell_map ? &c->shell_map : nullptr, s);
@@ -2118,6 +2153,9 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
     MX_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     MX_CUDA(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
     MX_CUDA(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
+    MX_CUDA(cudaEventCreateWithFlags(&c->ev_ts_first, cudaEventDisableTiming));
+    MX_CUDA(cudaEventCreateWithFlags(&c->ev_ts_sfr, cudaEventDisableTiming));
+    MX_CUDA(cudaEventCreateWithFlags(&c->ev_ts_tk, cudaEventDisableTiming));
     if (p.filter_type != 0 && p.filter_type != 1 && p.filter_type != 2)
       throw CudaError{ MX_EINVAL, "invalid filter type" };
     if (p.flag_spin_temp) {
@@ -2475,18 +2513,53 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
       late_out.push_back({ &mx_grids::vel, true, OUT });
       late_out.push_back({ &mx_grids::delta_T, false, OUT });
     }
-    // the copy stream starts after the compute stream's earlier work
+    // The copy stream starts after the compute stream's earlier work and
+    // carries every input: first what ComputeTs reads first (stars, deltax,
+    // x_e_box_prev), then sfr, the SFR-history slices in the order the shell
+    // operations first read them (slices no operation reads are not needed),
+    // Tk_box, and the find_HII_bubbles inputs.  The compute stream waits for
+    // each right before its first use (TsUploads), so most of the upload runs
+    // under the shell transforms.
     MX_CUDA(cudaEventRecord(ctx->ev_a, s));
     MX_CUDA(cudaStreamWaitEvent(cs, ctx->ev_a, 0));
-    copy_fields(ctx, host, ts_in, IN, s);
-    if (spin)
-      copy_histories(ctx, host, s);
+    TsUploads up{};
+    if (spin) {
+      auto upload = [&](float* mx_grids::*member, bool padded) {
+        copy_fields(ctx, host, { { member, padded, IN } }, IN, cs);
+      };
+      upload(&mx_grids::stars, true);
+      upload(&mx_grids::deltax, true);
+      upload(&mx_grids::x_e_box_prev, true);
+      MX_CUDA(cudaEventRecord(ctx->ev_ts_first, cs));
+      upload(&mx_grids::sfr, true);
+      MX_CUDA(cudaEventRecord(ctx->ev_ts_sfr, cs));
+      while ((int)ctx->ev_slices.size() < ctx->n_hist) {
+        cudaEvent_t e = nullptr;
+        MX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->ev_slices.push_back(e);
+      }
+      const ShellPlan sp = plan_shells(ctx->p, ctx->zz, snapshot);
+      std::vector<char> sent(ctx->n_hist, 0);
+      if (!sp.homogeneous && host->sfr_histories)
+        for (const std::vector<SfrOp>& ops : sp.ops)
+          for (const SfrOp& op : ops)
+            if (op.kind >= SfrOp::LOAD && op.slice >= 0 && op.slice < ctx->n_hist && !sent[op.slice]) {
+              const size_t P = (size_t)ctx->gd.P;
+              MX_CUDA(cudaMemcpyAsync(ctx->mirror.sfr_histories + P * op.slice, host->sfr_histories + P * op.slice,
+                                      sizeof(float) * P, cudaMemcpyHostToDevice, cs));
+              MX_CUDA(cudaEventRecord(ctx->ev_slices[op.slice], cs));
+              sent[op.slice] = 1;
+            }
+      upload(&mx_grids::Tk_box, false);
+      MX_CUDA(cudaEventRecord(ctx->ev_ts_tk, cs));
+      up = { ctx->ev_ts_first, ctx->ev_ts_sfr, ctx->ev_ts_tk, &ctx->ev_slices };
+    }
     copy_fields(ctx, host, fhb_in, IN, cs);
     MX_CUDA(cudaEventRecord(ctx->ev_b, cs));
     mx_grids m = mirror_for(ctx, host);
     int launches = 0;
     if (spin) {
-      run_ComputeTs(ctx, snapshot, &m, out, s);
+      run_ComputeTs(ctx, snapshot, &m, out, s, &up);
       launches += out ? out->gpu_launches : 0;
       MX_CUDA(cudaEventRecord(ctx->ev_a, s));
       MX_CUDA(cudaStreamWaitEvent(cs, ctx->ev_a, 0));

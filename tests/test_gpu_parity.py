@@ -159,6 +159,43 @@ def test_shell_map_gives_identical_results(name, D, monkeypatch):
             assert a[k] == b[k], k
 
 
+# Radii (and ComputeTs shells) go through the transforms in batches sized by
+# the work buffer; at 512^3 find_HII_bubbles takes two.  Small batches
+# (MX_MAX_BATCH_SPECTRA) must give the same grids as one batch, bit for bit.
+@pytest.mark.parametrize("transform", ["fused", "cufft"])
+@pytest.mark.parametrize("name,D,spectra", [("full24", 64, 15), ("plain32_tophat", 64, 6), ("evolve16", 32, 10)])
+def test_radius_batches_give_identical_results(name, D, spectra, transform, monkeypatch):
+    from cases import initial
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+
+    monkeypatch.setenv("MX_TRANSFORM", transform)
+    c = CASES[name]
+    w = Case(name, c.base, D, c.overrides, c.fesc, c.snapshots).workload()
+    runs = []
+    for cap in (None, str(spectra)):
+        if cap is None:
+            monkeypatch.delenv("MX_MAX_BATCH_SPECTRA", raising=False)
+        else:
+            monkeypatch.setenv("MX_MAX_BATCH_SPECTRA", cap)
+        step = ReionGridStep(w.params, w.redshifts)
+        gen = syn.FieldGenerator(w)
+        st = initial(w, step.n_sfr_histories)
+        glob = []
+        for s in w.snapshots:
+            st.update(gen.inputs(s, step.n_sfr_histories))
+            glob.append(step.step(s, st))
+        runs.append((st, glob))
+        step.close()
+    (sa, ga), (sb, gb) = runs
+    for k in OUTPUT_GRIDS:
+        if k in sa:
+            assert np.array_equal(sa[k], sb[k]), k
+    for a, b in zip(ga, gb):
+        for k in ("volume_weighted_global_xH", "volume_ave_TS", "volume_ave_Tb"):
+            assert a[k] == b[k], k
+
+
 def test_device_entry_points_match_host_entry_points():
     import torch
 
