@@ -846,7 +846,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
   constexpr int IXE = 3, INR = SPIN ? 4 : 3;
   extern __shared__ __align__(128) unsigned char zsmem[];
   char* smem = reinterpret_cast<char*>(zsmem);
-  const long long row0 = (long long)blockIdx.x * P::TZ;
+  const long long row0 = ((long long)blockIdx.x + a.group0) * P::TZ;
   const int n_items = a.n_f * G;
   z_setup<D>(smem, a.spectra, a.C, row0, n_items);
   ZTw<D> w;
@@ -1085,7 +1085,8 @@ static void launch_zt_cfg(const ZThresholdArgs& a, cudaStream_t s)
 {
   const size_t bytes = ZPlan<D>::BYTES;
   cudaFuncSetAttribute(k_fft_z_threshold<D, SPIN, RECOMB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  k_fft_z_threshold<D, SPIN, RECOMB><<<D * D / ZPlan<D>::TZ, FFT_THREADS, bytes, s>>>(a);
+  const int groups = a.n_groups > 0 ? a.n_groups : D * D / ZPlan<D>::TZ;
+  k_fft_z_threshold<D, SPIN, RECOMB><<<groups, FFT_THREADS, bytes, s>>>(a);
 }
 template <int D>
 static void launch_zt(const ZThresholdArgs& a, cudaStream_t s)
@@ -1156,8 +1157,14 @@ bool launch_fft_y(int D, float2* data, long long C, int n_spectra, int threads, 
   return true;
 }
 
+int fft_z_rows_per_group(int D) { return 2048 / D; }
+int fft_z_row_groups(int D) { return D * D / fft_z_rows_per_group(D); }
+
 bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s)
 {
+  if (a.n_groups < 0 || a.group0 < 0 || (a.n_groups == 0 && a.group0 != 0) ||
+      (long long)a.group0 + a.n_groups > fft_z_row_groups(D))
+    return false;
   // the kernel's fixed field order
   if (a.G != 3 + (a.spin ? 1 : 0) + (a.recomb ? 1 : 0) || a.idx_xe != (a.spin ? 3 : -1) ||
       a.idx_nr != (a.recomb ? (a.spin ? 4 : 3) : -1))

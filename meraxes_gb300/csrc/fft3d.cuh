@@ -44,6 +44,9 @@ struct ZThresholdArgs
   float gamma_halo_bias;
   int uvb, recomb, spin;
   unsigned* err;  // bit 2: a pipeline wait timed out
+  // row groups [group0, group0 + n_groups) of fft_z_row_groups(D) (n_groups
+  // 0: all), so that a launch can cover a slab of rows
+  int group0 = 0, n_groups = 0;
 };
 
 bool fft3d_supported(int D);
@@ -60,6 +63,9 @@ bool launch_fft_y(int D, float2* data, long long C, int n_spectra, int threads, 
 bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s);
 bool launch_fft_z_store(int D, const float2* spectra, long long C, int n, int r0, float* shells, long long N,
                         unsigned* err, cudaStream_t s);
+// row groups of the threshold z-pass and rows (x * D + y) per group
+int fft_z_row_groups(int D);
+int fft_z_rows_per_group(int D);
 int fft_kernel_launches();
 
 }  // namespace mx

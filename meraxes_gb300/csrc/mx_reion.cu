@@ -358,7 +358,26 @@ void mx_ctx::ensure_mirror()
 // ======================================================================
 // find_HII_bubbles (src/core/find_HII_bubbles.c:47-495)
 // ======================================================================
-static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s)
+// Outputs of find_HII_bubbles that a host-pointer call copies back slab by
+// slab: the last radius batch's threshold z-pass runs as `slabs` launches
+// over row slabs, and after each one the copy stream (which waits on `ev`)
+// copies that slab's rows of xH, z_at_ionization, r_bubble, J_21,
+// J_21_at_ionization and Gamma12 into `host`, while the next slab computes.
+// `done` is set when that happened (fused transforms only).
+struct FhbDownloads
+{
+  cudaStream_t cs;
+  cudaEvent_t ev;
+  const mx_grids* host;
+  int slabs;
+  bool done;
+};
+
+float* mx_grids::* const SLAB_OUTPUTS[] = { &mx_grids::xH,   &mx_grids::z_at_ionization,    &mx_grids::r_bubble,
+                                             &mx_grids::J_21, &mx_grids::J_21_at_ionization, &mx_grids::Gamma12 };
+
+static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s,
+                                 FhbDownloads* dl = nullptr)
 {
   const mx_params& p = c->p;
   const GridDims& gd = c->gd;
@@ -439,10 +458,12 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
   }
   MX_CUDA(cudaMemcpyAsync(c->d_rp, rps.data(), sizeof(RadiusParams) * nR, cudaMemcpyHostToDevice, s));
 
-  // batched filter -> C2R -> threshold over chunks of radii, largest first
+  // batched filter -> C2R -> threshold over chunks of radii, largest first;
+  // the first batch takes the remainder, so that the last (whose threshold
+  // pass a host call overlaps with the output copies) is a full one
   const int per_batch = (int)std::max<long long>(1, c->work_fields / G);
-  for (int r0 = 0; r0 < nR; r0 += per_batch) {
-    const int nb = std::min(per_batch, nR - r0);
+  const int n_batches = (nR + per_batch - 1) / per_batch;
+  for (int r0 = 0, nb = nR - (n_batches - 1) * per_batch; r0 < nR; r0 += nb, nb = per_batch) {
     // the last, unfiltered step is read from the input grids (identity transform)
     const int nf = (r0 + nb == nR) ? nb - 1 : nb;
     const int nstate = 3 + (uvb ? 2 : 0) + (recomb ? 1 : 0);
@@ -500,8 +521,30 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
       // J_21_at_ionization, Gamma12 written) counted with the first batch
       Prof pr(c, "fft_z_threshold",
               (double)G * nf * B8C + (double)(nb - nf) * G * B4N + (r0 == 0 ? 8.0 * B4N : 0.0), s);
-      if (!launch_fft_z_threshold(gd.D, za, s))
-        throw CudaError{ MX_ECUDA, "find_HII_bubbles: field layout does not match the fused z-pass" };
+      if (!dl || r0 + nb < nR) {
+        if (!launch_fft_z_threshold(gd.D, za, s))
+          throw CudaError{ MX_ECUDA, "find_HII_bubbles: field layout does not match the fused z-pass" };
+        continue;
+      }
+      // last batch of a host call: row slabs, each slab's outputs copied
+      // back while the next computes
+      const int groups = fft_z_row_groups(gd.D);
+      const int K = std::max(1, std::min(dl->slabs, groups));
+      const long long cells_per_group = (long long)fft_z_rows_per_group(gd.D) * gd.D;
+      for (int k = 0; k < K; k++) {
+        za.group0 = (int)((long long)groups * k / K);
+        za.n_groups = (int)((long long)groups * (k + 1) / K) - za.group0;
+        if (!launch_fft_z_threshold(gd.D, za, s))
+          throw CudaError{ MX_ECUDA, "find_HII_bubbles: field layout does not match the fused z-pass" };
+        MX_CUDA(cudaEventRecord(dl->ev, s));
+        MX_CUDA(cudaStreamWaitEvent(dl->cs, dl->ev, 0));
+        const long long cell0 = za.group0 * cells_per_group, cells = za.n_groups * cells_per_group;
+        for (float* mx_grids::*m : SLAB_OUTPUTS)
+          if (dl->host->*m && g->*m)
+            MX_CUDA(cudaMemcpyAsync(dl->host->*m + cell0, g->*m + cell0, sizeof(float) * cells,
+                                    cudaMemcpyDeviceToHost, dl->cs));
+      }
+      dl->done = true;
       continue;
     }
     FilterBatch fb;
@@ -2566,11 +2609,19 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
       copy_fields(ctx, host, ts_out, OUT, cs);
     }
     MX_CUDA(cudaStreamWaitEvent(s, ctx->ev_b, 0));
-    run_find_HII_bubbles(ctx, snapshot, &m, out, s);
+    FhbDownloads dl{ cs, ctx->ev_a, host, 4, false };
+    run_find_HII_bubbles(ctx, snapshot, &m, out, s, &dl);
     launches += out ? out->gpu_launches : 0;
     if (b21) {
       run_delta_T(ctx, snapshot, &m, out, s);
       launches += out ? out->gpu_launches : 0;
+    }
+    if (dl.done) {
+      std::vector<FieldIO> rest;
+      for (const FieldIO& f : late_out)
+        if (std::find(std::begin(SLAB_OUTPUTS), std::end(SLAB_OUTPUTS), f.member) == std::end(SLAB_OUTPUTS))
+          rest.push_back(f);
+      late_out.swap(rest);
     }
     copy_fields(ctx, host, late_out, OUT, s);
     MX_CUDA(cudaStreamSynchronize(cs));
