@@ -77,6 +77,7 @@ struct mx_ctx
   // host-pointer mx_step: ComputeTs inputs arriving on the copy stream
   // (TsUploads)
   cudaEvent_t ev_ts_first = nullptr, ev_ts_sfr = nullptr, ev_ts_tk = nullptr;
+  cudaEvent_t ev_state = nullptr;  // find_HII_bubbles state grids uploaded
   std::vector<cudaEvent_t> ev_slices;
   int device = 0;
   int nthreads = 4;
@@ -223,7 +224,7 @@ mx_ctx::~mx_ctx()
     cudaEventDestroy(ev_a);
   if (ev_b)
     cudaEventDestroy(ev_b);
-  for (cudaEvent_t e : { ev_ts_first, ev_ts_sfr, ev_ts_tk })
+  for (cudaEvent_t e : { ev_ts_first, ev_ts_sfr, ev_ts_tk, ev_state })
     if (e)
       cudaEventDestroy(e);
   for (cudaEvent_t e : ev_slices)
@@ -364,6 +365,9 @@ void mx_ctx::ensure_mirror()
 // copies that slab's rows of xH, z_at_ionization, r_bubble, J_21,
 // J_21_at_ionization and Gamma12 into `host`, while the next slab computes.
 // `done` is set when that happened (fused transforms only).
+// `state_in` (if set): the event after which the state grids the threshold
+// reads first (z_at_ionization, J_21_at_ionization, Gamma12) are on the
+// device; the first threshold launch waits for it.
 struct FhbDownloads
 {
   cudaStream_t cs;
@@ -371,6 +375,7 @@ struct FhbDownloads
   const mx_grids* host;
   int slabs;
   bool done;
+  cudaEvent_t state_in;
 };
 
 float* mx_grids::* const SLAB_OUTPUTS[] = { &mx_grids::xH,   &mx_grids::z_at_ionization,    &mx_grids::r_bubble,
@@ -491,6 +496,8 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
         Prof pr(c, "fft_y", 2.0 * G * nf * B8C, s);
         launch_fft_y(gd.D, c->d_work, c->work_C, nf * G, c->y_threads, s);
       }
+      if (dl && dl->state_in && r0 == 0)
+        MX_CUDA(cudaStreamWaitEvent(s, dl->state_in, 0));
       ZThresholdArgs za;
       za.spectra = c->d_work;
       za.C = c->work_C;
@@ -568,6 +575,8 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
       Prof pr(c, "cufft_c2r", (double)G * (B8C + B4N), s);
       MX_CUFFT(cufftExecC2R(plan, w, (cufftReal*)w));
     }
+    if (dl && dl->state_in && r0 == 0)
+      MX_CUDA(cudaStreamWaitEvent(s, dl->state_in, 0));
     ThresholdArgs ta;
     ta.fields = (const float*)c->d_work;
     ta.P = gd.P;
@@ -2199,6 +2208,7 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
     MX_CUDA(cudaEventCreateWithFlags(&c->ev_ts_first, cudaEventDisableTiming));
     MX_CUDA(cudaEventCreateWithFlags(&c->ev_ts_sfr, cudaEventDisableTiming));
     MX_CUDA(cudaEventCreateWithFlags(&c->ev_ts_tk, cudaEventDisableTiming));
+    MX_CUDA(cudaEventCreateWithFlags(&c->ev_state, cudaEventDisableTiming));
     if (p.filter_type != 0 && p.filter_type != 1 && p.filter_type != 2)
       throw CudaError{ MX_EINVAL, "invalid filter type" };
     if (p.flag_spin_temp) {
@@ -2597,8 +2607,19 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
       MX_CUDA(cudaEventRecord(ctx->ev_ts_tk, cs));
       up = { ctx->ev_ts_first, ctx->ev_ts_sfr, ctx->ev_ts_tk, &ctx->ev_slices };
     }
-    copy_fields(ctx, host, fhb_in, IN, cs);
+    // find_HII_bubbles: the grids its forward transforms read (ev_b), then
+    // the state grids its first threshold pass reads (ev_state)
+    std::vector<FieldIO> fhb_early, fhb_state;
+    for (const FieldIO& f : fhb_in)
+      (f.member == &mx_grids::z_at_ionization || f.member == &mx_grids::J_21_at_ionization ||
+           f.member == &mx_grids::Gamma12
+         ? fhb_state
+         : fhb_early)
+        .push_back(f);
+    copy_fields(ctx, host, fhb_early, IN, cs);
     MX_CUDA(cudaEventRecord(ctx->ev_b, cs));
+    copy_fields(ctx, host, fhb_state, IN, cs);
+    MX_CUDA(cudaEventRecord(ctx->ev_state, cs));
     mx_grids m = mirror_for(ctx, host);
     int launches = 0;
     if (spin) {
@@ -2609,7 +2630,7 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
       copy_fields(ctx, host, ts_out, OUT, cs);
     }
     MX_CUDA(cudaStreamWaitEvent(s, ctx->ev_b, 0));
-    FhbDownloads dl{ cs, ctx->ev_a, host, 4, false };
+    FhbDownloads dl{ cs, ctx->ev_a, host, 4, false, ctx->ev_state };
     run_find_HII_bubbles(ctx, snapshot, &m, out, s, &dl);
     launches += out ? out->gpu_launches : 0;
     if (b21) {
