@@ -374,21 +374,21 @@ void launch_fhb_reduce(const FhbReduceArgs& a, const GridDims& gd, cudaStream_t 
   g_launches++;
 }
 
-__global__ void k_finalize(const double* __restrict__ partials, int nvals, double* __restrict__ out)
+__global__ void k_finalize(const double* __restrict__ partials, int nvals, int nblocks, double* __restrict__ out)
 {
   // one thread per value, fixed summation order over blocks
   const int v = threadIdx.x;
   if (v < nvals) {
     double s = 0.0;
-    for (int b = 0; b < RED_BLOCKS; b++)
+    for (int b = 0; b < nblocks; b++)
       s += partials[(long long)b * nvals + v];
     out[v] = s;
   }
 }
 
-void launch_finalize(const double* partials, int nvals, double* out, cudaStream_t s)
+void launch_finalize(const double* partials, int nvals, double* out, cudaStream_t s, int nblocks)
 {
-  k_finalize<<<1, 32, 0, s>>>(partials, nvals, out);
+  k_finalize<<<1, 32, 0, s>>>(partials, nvals, nblocks, out);
   g_launches++;
 }
 

@@ -88,7 +88,8 @@ struct FhbReduceArgs
 };
 void launch_fhb_reduce(const FhbReduceArgs& a, const GridDims& gd, cudaStream_t s);
 // Sums `nvals` columns of a RED_BLOCKS x nvals partials array in fixed order.
-void launch_finalize(const double* partials, int nvals, double* out, cudaStream_t s);
+// out[v] = sum over the first nblocks blocks' partials (fixed order)
+void launch_finalize(const double* partials, int nvals, double* out, cudaStream_t s, int nblocks = RED_BLOCKS);
 
 // ------------------------------------------------------------ grid helpers
 void launch_fill(float* p, long long n, float v, cudaStream_t s);
@@ -171,7 +172,8 @@ struct EvolveArgs
 // ev_shell_map_ok() says when one applies), or nullptr for one bulk copy per
 // shell row
 bool ev_shell_map_ok(long long N, int S);
-void launch_evolve(const EvolveArgs& a, const GridDims& gd, const void* shell_map, cudaStream_t s);
+// returns the number of blocks (of partial sums) launched
+int launch_evolve(const EvolveArgs& a, const GridDims& gd, const void* shell_map, cudaStream_t s);
 
 // Adjoint of the per-cell spin-temperature update and of the 21cm box.
 struct AdjointArgs

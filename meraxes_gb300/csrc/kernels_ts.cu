@@ -8,7 +8,9 @@
 // of the rare cells whose FP32 stopping test lands within 1e-5 of the
 // reference's 1e-3 criterion (those cells are recomputed in FP64 so that they
 // stop after the same iteration as the reference).
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "bulk.cuh"
@@ -251,12 +253,13 @@ bool ev_shell_map_ok(long long N, int S) { return N % EV_TILE == 0 && N < (1LL <
 // tables, on a 128-byte boundary for the tensor copies
 __host__ __device__ constexpr int ev_ring_offset(int S) { return (ev_tables_floats(S) + 31) / 32 * 32; }
 
+template <int STAGES = 2>
 __device__ __forceinline__ void ev_issue(uint64_t* bars, float* stages, const float* shells, const bulk::TensorMap* map,
                                          int S, long long N, long long tile, int k)
 {
   const long long c0 = tile * EV_TILE;
-  float* st = stages + (size_t)(k & 1) * S * EV_TILE;
-  uint64_t* bar = &bars[k & 1];
+  float* st = stages + (size_t)(k % STAGES) * S * EV_TILE;
+  uint64_t* bar = &bars[k % STAGES];
   if (map) {
     bulk::mbar_arm(bar, (unsigned)(sizeof(float) * EV_TILE * S));
     bulk::bulk_tensor_2d(st, map, (int)c0, 0, bar);
@@ -268,7 +271,11 @@ __device__ __forceinline__ void ev_issue(uint64_t* bars, float* stages, const fl
     bulk::bulk_copy(st + r * EV_TILE, shells + (long long)r * N + c0, (unsigned)(sizeof(float) * n), bar);
 }
 
-__global__ void __launch_bounds__(RED_THREADS)
+// STAGES shell-ring stages (2: a tile in flight while one is summed).  One
+// stage (half the shared memory, three blocks per SM at 80 registers with
+// spills) measured slower: 11.9 against 11.2 ms at 512^3.
+template <int STAGES>
+__global__ void __launch_bounds__(RED_THREADS, 2)
   k_evolve_f32(EvolveArgs a, int D, int H, long long N, const __grid_constant__ bulk::TensorMap shell_map, int use_map)
 {
   const bulk::TensorMap* map = use_map ? &shell_map : nullptr;
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(RED_THREADS)
   extern __shared__ __align__(128) float sm[];
   float4* s_P = reinterpret_cast<float4*>(sm);  // NXHII * S
   float* stages = sm + ev_ring_offset(S);       // 2 * S * EV_TILE
-  __shared__ uint64_t bars[2];
+  __shared__ uint64_t bars[STAGES];
   for (int i = threadIdx.x; i < NXHII * S; i += blockDim.x) {
     const int x = i / S, r = i % S;
     s_P[i] = make_float4(c.fKH[r] * c.ftab[0][x][r], c.fKI[r] * c.ftab[1][x][r], c.fKL[r] * c.ftab[2][x][r],
@@ -291,14 +298,14 @@ __global__ void __launch_bounds__(RED_THREADS)
   const int my_tiles = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
   const bool light = !c.no_light;
   if (threadIdx.x == 0 && light) {
-    bulk::mbar_init(&bars[0], 1);
-    bulk::mbar_init(&bars[1], 1);
+    for (int b = 0; b < STAGES; b++)
+      bulk::mbar_init(&bars[b], 1);
     bulk::mbar_init_fence();
   }
   __syncthreads();
   if (threadIdx.x == 0 && light)
-    for (int k = 0; k < 2 && k < my_tiles; k++)
-      ev_issue(bars, stages, a.shells, map, S, N, blockIdx.x + (long long)k * gridDim.x, k);
+    for (int k = 0; k < STAGES && k < my_tiles; k++)
+      ev_issue<STAGES>(bars, stages, a.shells, map, S, N, blockIdx.x + (long long)k * gridDim.x, k);
   double acc[4] = { 0, 0, 0, 0 };
   // the cell state of tile k + 1 is read while tile k is computed
   float n_delta = 0.f, n_xe = 0.f, n_T = 1.f;
@@ -337,17 +344,17 @@ __global__ void __launch_bounds__(RED_THREADS)
     const float w = (xcall - c.xhii[lo]) / (c.xhii[hi] - c.xhii[lo]);
     float heat = 0.f, ion = 0.f, lya = 0.f, star = 0.f;
     if (light) {
-      const bool arrived = bulk::mbar_wait(&bars[k & 1], (unsigned)(k >> 1) & 1u);
+      const bool arrived = bulk::mbar_wait(&bars[k % STAGES], (unsigned)(k / STAGES) & 1u);
       if (__syncthreads_or(!arrived)) {
         if (threadIdx.x == 0) {
           atomicOr(a.err, bulk::ERR_PIPELINE_TIMEOUT);
           // copies of tiles k and k + 1 may still be in flight
-          for (int j = k; j < my_tiles && j < k + 2; j++)
-            bulk::mbar_wait(&bars[j & 1], (unsigned)(j >> 1) & 1u);
+          for (int j = k; j < my_tiles && j < k + STAGES; j++)
+            bulk::mbar_wait(&bars[j % STAGES], (unsigned)(j / STAGES) & 1u);
         }
         return;
       }
-      const float* st = stages + (size_t)(k & 1) * S * EV_TILE + threadIdx.x;
+      const float* st = stages + (size_t)(k % STAGES) * S * EV_TILE + threadIdx.x;
       const float4* Plo = s_P + lo * S;
       const float4* Phi = s_P + hi * S;
       float hl = 0.f, il = 0.f, ll = 0.f, hh = 0.f, ih = 0.f, lh = 0.f;
@@ -366,10 +373,10 @@ __global__ void __launch_bounds__(RED_THREADS)
       heat = fmaf(w, hh - hl, hl);
       ion = fmaf(w, ih - il, il);
       lya = fmaf(w, lh - ll, ll);
-      // every thread has read stage k & 1: refill it with tile k + 2
+      // every thread has read this tile's stage: refill it with tile k + STAGES
       __syncthreads();
-      if (threadIdx.x == 0 && k + 2 < my_tiles)
-        ev_issue(bars, stages, a.shells, map, S, N, tile + 2LL * gridDim.x, k + 2);
+      if (threadIdx.x == 0 && k + STAGES < my_tiles)
+        ev_issue<STAGES>(bars, stages, a.shells, map, S, N, tile + (long long)STAGES * gridDim.x, k + STAGES);
     }
     if (!valid)
       continue;
@@ -408,15 +415,31 @@ __global__ void __launch_bounds__(RED_THREADS)
   block_sum_store<4>(acc, a.partials);
 }
 
-void launch_evolve(const EvolveArgs& a, const GridDims& gd, const void* shell_map, cudaStream_t s)
+// Grid: every SM's resident blocks once (the blocks loop over their tiles),
+// at most RED_BLOCKS (the partial-sum slots).
+template <int STAGES>
+static int launch_evolve_t(const EvolveArgs& a, const GridDims& gd, const bulk::TensorMap& map, int use_map,
+                           cudaStream_t s)
 {
-  const size_t smem = sizeof(float) * (ev_ring_offset(a.n_shells) + 2 * (size_t)a.n_shells * EV_TILE);
-  cudaFuncSetAttribute(k_evolve_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const size_t smem = sizeof(float) * (ev_ring_offset(a.n_shells) + STAGES * (size_t)a.n_shells * EV_TILE);
+  cudaFuncSetAttribute(k_evolve_f32<STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int dev = 0, sms = 152, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_evolve_f32<STAGES>, RED_THREADS, smem);
+  const int blocks = std::max(1, std::min(RED_BLOCKS, std::max(1, per_sm) * sms));
+  k_evolve_f32<STAGES><<<blocks, RED_THREADS, smem, s>>>(a, gd.D, gd.H, gd.N, map, use_map);
+  return blocks;
+}
+
+int launch_evolve(const EvolveArgs& a, const GridDims& gd, const void* shell_map, cudaStream_t s)
+{
   bulk::TensorMap map{};
   if (shell_map)
     std::memcpy(&map, shell_map, sizeof(map));
-  k_evolve_f32<<<RED_BLOCKS, RED_THREADS, smem, s>>>(a, gd.D, gd.H, gd.N, map, shell_map ? 1 : 0);
+  const int blocks = launch_evolve_t<2>(a, gd, map, shell_map ? 1 : 0, s);
   ts_launches++;
+  return blocks;
 }
 
 // ======================================================================

@@ -1011,11 +1011,12 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     ea.n_shells = S;
     if (up)
       MX_CUDA(cudaStreamWaitEvent(s, up->tk, 0));
+    int ev_blocks = RED_BLOCKS;
     {
       Prof pr(c, "k_evolve", ((double)S + 6.0) * 4.0 * (double)gd.N, s);
-      launch_evolve(ea, gd, c->has_shell_map ? &c->shell_map : nullptr, s);
+      ev_blocks = launch_evolve(ea, gd, c->has_shell_map ? &c->shell_map : nullptr, s);
     }
-    launch_finalize(c->d_partials, 4, c->d_sums + 8, s);
+    launch_finalize(c->d_partials, 4, c->d_sums + 8, s, ev_blocks);
     MX_CUDA(cudaMemcpyAsync(c->h_sums + 8, c->d_sums + 8, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
   }
 
