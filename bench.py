@@ -331,6 +331,14 @@ def run_gb300(args, rank, world, local):
     # whole-step algorithmic bandwidth
     total_bytes = sum(v[2] for v in kstats.values())
     step_gbs = (total_bytes / args.steps / 1e9) / (value * world / 1e3)
+    # the algorithmic model of a snapshot (every grid read and written once per
+    # logical pass, every 3-D FFT one ideal read + write): find_HII_bubbles
+    # N (8G + 12 G n_R + 32), ComputeTs N (8 + 12 S + 24), delta_T 16 N
+    G = 3 + (1 if p.flag_recombinations else 0) + (1 if p.flag_spin_temp else 0)
+    n_R = len(p.filter_radii())
+    S = p.ts_num_filter_steps if p.flag_spin_temp else 0
+    model_bytes = float(D) ** 3 * ((8 * G + 12 * G * n_R + 32) + ((8 + 12 * S + 24) if S else 0) + 16)
+    model_gbs = (model_bytes / 1e9) / (value * world / 1e3)
 
     # ------------------------------------------------------------------ e2e
     e2e = None
@@ -349,7 +357,9 @@ def run_gb300(args, rank, world, local):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (each grid 0.54 GB at 512^3)",
                    "fft_block_sizes": list(step.fft_block_sizes())},
-        "gpu_launches": launches, "clocks": clk, "roofline": roofline, "step_algorithmic_gbs": round(step_gbs, 1),
+        "gpu_launches": launches, "clocks": clk, "roofline": roofline,
+        "step_model_gbs": round(model_gbs, 1), "step_model_frac": round(model_gbs / hbm_peak, 4),
+        "step_model_bytes": model_bytes, "step_pass_gbs": round(step_gbs, 1),
         "kernels": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
                     for k, v in kernels.items()},
         "last_globals": {k: glob[k] for k in ("volume_weighted_global_xH", "volume_ave_TS", "volume_ave_Tb")},
