@@ -713,14 +713,26 @@ struct ZTw
   }
 };
 
+// Spectrum of ring item `it` when a radius has G fields (spectrum r*G + g):
+// the items of a radius take field 2 (weighted_sfr, which the threshold
+// reads only for its J_21 / Gamma12 bookkeeping) last.
+__device__ __forceinline__ int z_item_spectrum(int it, int G)
+{
+  if (G <= 3)
+    return it;
+  const int j = it % G;
+  return it - j + (j < 2 ? j : (j < G - 1 ? j + 1 : 2));
+}
+
 // Producer side of the ring: thread 0 issues item `it` into stage it % ZSTAGES.
 template <int D>
-__device__ __forceinline__ void z_issue(char* smem, const float2* spectra, long long C, long long row0, int it)
+__device__ __forceinline__ void z_issue(char* smem, const float2* spectra, long long C, long long row0, int it,
+                                        int G = 1)
 {
   using P = ZPlan<D>;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   float2* st = reinterpret_cast<float2*>(smem + P::OFF_STAGE) + (size_t)(it % ZSTAGES) * P::STAGE;
-  bulk_load(st, spectra + (long long)it * C + row0 * P::HP, (unsigned)(sizeof(float2) * P::STAGE),
+  bulk_load(st, spectra + (long long)z_item_spectrum(it, G) * C + row0 * P::HP, (unsigned)(sizeof(float2) * P::STAGE),
             &bars[it % ZSTAGES]);
 }
 
@@ -731,7 +743,7 @@ __device__ __forceinline__ void z_issue(char* smem, const float2* spectra, long 
 // arrive.  One block barrier per call: the transpose buffer alternates.
 template <int D, bool XS>
 __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const float2* spectra, long long C,
-                                      long long row0, const ZTw<D>& w, float2 (&z)[4])
+                                      long long row0, const ZTw<D>& w, float2 (&z)[4], int G = 1)
 {
   using P = ZPlan<D>;
   constexpr int H = P::H, DH = P::DH, P1 = P::P1, P2 = P::P2, L1 = P::L1, L2 = P::L2;
@@ -775,7 +787,7 @@ __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const flo
   if (__syncthreads_or(!arrived))
     return false;
   if (threadIdx.x == 0 && it + ZSTAGES < n_items)
-    z_issue<D>(smem, spectra, C, row0, it + ZSTAGES);
+    z_issue<D>(smem, spectra, C, row0, it + ZSTAGES, G);
   {
     // step B: row t, k1, lane-part l of the P2-point DFT over n2
     const int l = threadIdx.x % L2, k1 = (threadIdx.x / L2) % P1, t = threadIdx.x / (L2 * P1);
@@ -787,9 +799,27 @@ __device__ __forceinline__ bool z_c2r(char* smem, int it, int n_items, const flo
   return true;
 }
 
+// Consumes ring item `it` without transforming it: waits for its copy, then
+// (after a block barrier, which also keeps the transpose buffers'
+// alternation safe) refills its stage.  Returns false if the copy did not
+// arrive.
+template <int D>
+__device__ __forceinline__ bool z_skip(char* smem, int it, int n_items, const float2* spectra, long long C,
+                                       long long row0, int G)
+{
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  const bool arrived = mbar_wait(&bars[it % ZSTAGES], (unsigned)(it / ZSTAGES) & 1u);
+  if (__syncthreads_or(!arrived))
+    return false;
+  if (threadIdx.x == 0 && it + ZSTAGES < n_items)
+    z_issue<D>(smem, spectra, C, row0, it + ZSTAGES, G);
+  return true;
+}
+
 // Ring setup: barriers, the first ZSTAGES copies.
 template <int D>
-__device__ __forceinline__ void z_setup(char* smem, const float2* spectra, long long C, long long row0, int n_items)
+__device__ __forceinline__ void z_setup(char* smem, const float2* spectra, long long C, long long row0, int n_items,
+                                        int G = 1)
 {
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   if (threadIdx.x == 0) {
@@ -800,7 +830,7 @@ __device__ __forceinline__ void z_setup(char* smem, const float2* spectra, long 
   __syncthreads();
   if (threadIdx.x == 0)
     for (int it = 0; it < ZSTAGES && it < n_items; it++)
-      z_issue<D>(smem, spectra, C, row0, it);
+      z_issue<D>(smem, spectra, C, row0, it, G);
 }
 
 // After a timed-out wait: record the error and wait (bounded) for the copies
@@ -848,7 +878,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
   char* smem = reinterpret_cast<char*>(zsmem);
   const long long row0 = ((long long)blockIdx.x + a.group0) * P::TZ;
   const int n_items = a.n_f * G;
-  z_setup<D>(smem, a.spectra, a.C, row0, n_items);
+  z_setup<D>(smem, a.spectra, a.C, row0, n_items, G);
   ZTw<D> w;
   w.init();
   // this thread's cells: row t, z = 2 m_e + {0, 1}
@@ -867,6 +897,11 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
     st[2 * e] = (x0.x > REL_TOL_F ? ST_XHIGH : 0u) | (x0.x < REL_TOL_F ? ST_XLOW : 0u) | (z0.x < 0 ? ST_ZUNSET : 0u);
     st[2 * e + 1] = (x0.y > REL_TOL_F ? ST_XHIGH : 0u) | (x0.y < REL_TOL_F ? ST_XLOW : 0u) | (z0.y < 0 ? ST_ZUNSET : 0u);
   }
+  // weighted_sfr (field 2) enters only the J_21 / Gamma12 values of a cell
+  // ionised for the first time at this radius and J_21_at_ionization where
+  // z_at_ionization is first set; its transform is skipped for a block with
+  // no such cell (its ring item is still consumed)
+  const bool need_ws = a.uvb || RECOMB;
   int it = 0;
   for (int r = 0; r < a.n_r; r++) {
     const RadiusParams rp = a.rp[r];
@@ -874,8 +909,9 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
     float2 f[G][4];
     if (!direct) {
 #pragma unroll
-      for (int g = 0; g < G; g++) {
-        if (!z_c2r<D, true>(smem, it, n_items, a.spectra, a.C, row0, w, f[g])) {
+      for (int j = 0; j < G - 1; j++) {
+        const int g = j < 2 ? j : j + 1;
+        if (!z_c2r<D, true>(smem, it, n_items, a.spectra, a.C, row0, w, f[g], G)) {
           z_abort<D>(smem, it, n_items, a.err);
           return;
         }
@@ -888,30 +924,28 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
         for (int e = 0; e < 4; e++)
           f[g][e] = *reinterpret_cast<const float2*>(a.direct[g] + rowc * 2LL * P::H + zc[e]);
     }
+    // the test and the state update; bit c of first_ion / first_z marks a
+    // cell whose J_21 / Gamma12 resp. J_21_at_ionization is written below
+    unsigned first_ion = 0, first_z = 0;
 #pragma unroll
     for (int c = 0; c < 8; c++) {
       const int e = c >> 1;
       const bool hi = c & 1;
-      float fv[G];
-#pragma unroll
-      for (int g = 0; g < G; g++)
-        fv[g] = hi ? f[g][e].y : f[g][e].x;
-      const float dx = fmaxf(fv[0], -1 + REL_TOL_F);
-      float stv = fmaxf(fv[1], 0.0f);
+      const float v0 = hi ? f[0][e].y : f[0][e].x;
+      const float v1 = hi ? f[1][e].y : f[1][e].x;
+      const float dx = fmaxf(v0, -1 + REL_TOL_F);
+      float stv = fmaxf(v1, 0.0f);
       if (stv < ABS_TOL_F)
         stv = 0;
-      float ws = fmaxf(fv[2], 0.0f);
-      if (ws < ABS_TOL_F)
-        ws = 0;
       float nr = 0.0f, xe = 0.0f;
       if constexpr (RECOMB) {
-        nr = fv[INR];
+        nr = hi ? f[INR][e].y : f[INR][e].x;
         nr = fmaxf(nr, 0.0f);
         if (nr < ABS_TOL_F)
           nr = 0;
       }
       if constexpr (SPIN) {
-        xe = fv[IXE];
+        xe = hi ? f[IXE][e].y : f[IXE][e].x;
         xe = fmaxf(xe, 0.0f);
         if (xe < ABS_TOL_F)
           xe = 0;
@@ -940,14 +974,9 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
       unsigned s = st[c];
       const bool xr_high = !(s & ST_ION) && (s & ST_XHIGH);  // running xH > REL_TOL
       bool xr_low = (s & ST_ION) || (s & ST_XLOW);            // running xH < REL_TOL
-      const float J21_aux = a.uvb ? ws * rp.kj : 0.0f;
       if (ionised) {
-        if (xr_high) {
-          if (a.uvb)
-            a.J21[ir] = J21_aux;
-          if (RECOMB)
-            a.Gamma12[ir] = ws * rp.kg;
-        }
+        if (xr_high)
+          first_ion |= 1u << c;
         s = (s & ((1u << ST_RB_SHIFT) - 1)) | ST_ION | ((unsigned)r << ST_RB_SHIFT);
         xr_low = true;
       } else if (rp.last && xr_high) {
@@ -957,11 +986,45 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
       }
       if (xr_low && (s & ST_ZUNSET)) {
         a.z_at_ion[ir] = (float)a.redshift;
-        if (a.uvb)
-          a.J21_at_ion[ir] = J21_aux * a.gamma_halo_bias;
+        first_z |= 1u << c;
         s &= ~ST_ZUNSET;
       }
       st[c] = s;
+    }
+    if (!need_ws)
+      first_ion = first_z = 0;
+    if (!a.uvb)
+      first_z = 0;
+    if (!direct) {
+      // field 2 of this radius: transformed if a cell of the block needs it
+      const bool any = __syncthreads_or((first_ion | first_z) != 0);
+      const bool ok = any ? z_c2r<D, true>(smem, it, n_items, a.spectra, a.C, row0, w, f[2], G)
+                          : z_skip<D>(smem, it, n_items, a.spectra, a.C, row0, G);
+      if (!ok) {
+        z_abort<D>(smem, it, n_items, a.err);
+        return;
+      }
+      it++;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      if (!((first_ion | first_z) >> c & 1u))
+        continue;
+      const int e = c >> 1;
+      const bool hi = c & 1;
+      const long long ir = rowc * D + zc[e] + (hi ? 1 : 0);
+      float ws = fmaxf(hi ? f[2][e].y : f[2][e].x, 0.0f);
+      if (ws < ABS_TOL_F)
+        ws = 0;
+      const float J21_aux = a.uvb ? ws * rp.kj : 0.0f;
+      if (first_ion >> c & 1u) {
+        if (a.uvb)
+          a.J21[ir] = J21_aux;
+        if (RECOMB)
+          a.Gamma12[ir] = ws * rp.kg;
+      }
+      if (first_z >> c & 1u)
+        a.J21_at_ion[ir] = J21_aux * a.gamma_halo_bias;
     }
   }
 #pragma unroll
