@@ -463,12 +463,16 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
   }
   MX_CUDA(cudaMemcpyAsync(c->d_rp, rps.data(), sizeof(RadiusParams) * nR, cudaMemcpyHostToDevice, s));
 
-  // batched filter -> C2R -> threshold over chunks of radii, largest first;
-  // the first batch takes the remainder, so that the last (whose threshold
-  // pass a host call overlaps with the output copies) is a full one
+  // batched filter -> C2R -> threshold over chunks of radii, largest first.
+  // A host call (whose output copies overlap the last batch's threshold
+  // pass) puts the remainder first, so that the last batch is a full one;
+  // otherwise the remainder goes last, where a remainder of only the
+  // unfiltered step needs no transforms.  The grids do not depend on it.
   const int per_batch = (int)std::max<long long>(1, c->work_fields / G);
   const int n_batches = (nR + per_batch - 1) / per_batch;
-  for (int r0 = 0, nb = nR - (n_batches - 1) * per_batch; r0 < nR; r0 += nb, nb = per_batch) {
+  const int rem = nR - (n_batches - 1) * per_batch;
+  auto batch_size = [&](int i) { return dl ? (i == 0 ? rem : per_batch) : (i == n_batches - 1 ? rem : per_batch); };
+  for (int bi = 0, r0 = 0, nb = batch_size(0); r0 < nR; r0 += nb, nb = batch_size(++bi)) {
     // the last, unfiltered step is read from the input grids (identity transform)
     const int nf = (r0 + nb == nR) ? nb - 1 : nb;
     const int nstate = 3 + (uvb ? 2 : 0) + (recomb ? 1 : 0);
