@@ -65,7 +65,7 @@ __device__ void block_reduce_store(double (&v)[NV], double* partials)
 
 __device__ __forceinline__ long long pad_of(long long ir, int D, int H)
 {
-  const long long row = ir / D;
+  const long long row = row_of(ir, D);
   return ir - row * D + row * 2LL * H;
 }
 
@@ -78,7 +78,7 @@ __global__ void k_adjoint_axpy(float* __restrict__ grad, const float* __restrict
                                float a_first, float a_second, int D, int H, long long N, long long C)
 {
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long row = ir / D;
+    const long long row = row_of(ir, D);
     const long long ip = row * 2LL * H + (ir - row * D);
     float x = 0.0f;
     if (v)
@@ -303,7 +303,7 @@ void launch_threshold(const ThresholdArgs& a, const GridDims& gd, cudaStream_t s
 // recombination update (recombinations.c:30-52 lookup).
 __global__ void k_fhb_reduce(FhbReduceArgs a, int D, int H, long long N)
 {
-  double acc[4] = { 0, 0, 0, 0 };
+  CSum sum[4];
   // RR_DEL_LNG * RR_LNG_NPTS is a float product in recombinations.c:46
   const double lng_top = RR_LNG_MIN + (double)(RR_DEL_LNG * (float)RR_LNG_NPTS);
   const float dNfac = a.fabs_dtdz * a.zstep;
@@ -311,13 +311,12 @@ __global__ void k_fhb_reduce(FhbReduceArgs a, int D, int H, long long N)
     const long long ip = pad_of(ir, D, H);
     const float xHf = a.xH[ir];
     const float dxf = a.deltax[ip];
-    const double cell_xH = (double)xHf;
-    acc[0] += cell_xH;
+    sum[0].add(xHf);
     if (a.uvb)
-      acc[1] += (double)a.J21[ir];
-    const double dom = 1.0 + (double)dxf;
-    acc[2] += cell_xH * dom;
-    acc[3] += dom;
+      sum[1].add(a.J21[ir]);
+    const float domf = 1.0f + dxf;
+    sum[2].add(xHf * domf);
+    sum[3].add(domf);
     const float g12 = a.recomb ? a.Gamma12[ir] : 0.0f;
     // dNrec is exactly zero for neutral cells and for Gamma12 = 0 (log -> -inf)
     if (a.recomb && xHf < 1.0f && g12 > 0.0f) {
@@ -330,7 +329,7 @@ __global__ void k_fhb_reduce(FhbReduceArgs a, int D, int H, long long N)
       if (fabsf(qf - rintf(qf)) > 2e-4f) {
         z_ct = (int)qf;
       } else {
-        const float z_eff = (float)__dsub_rn(__dmul_rn(1. + a.redshift, pow(dom, 1.0 / 3.0)), 1.0);
+        const float z_eff = (float)__dsub_rn(__dmul_rn(1. + a.redshift, pow(1.0 + (double)dxf, 1.0 / 3.0)), 1.0);
         z_ct = (int)((double)z_eff / (double)RR_DEL_Z + 0.5);
       }
       z_ct = z_ct < 0 ? 0 : (z_ct >= RR_Z_NPTS ? RR_Z_NPTS - 1 : z_ct);
@@ -365,6 +364,7 @@ __global__ void k_fhb_reduce(FhbReduceArgs a, int D, int H, long long N)
       }
     }
   }
+  double acc[4] = { sum[0].value(), sum[1].value(), sum[2].value(), sum[3].value() };
   block_reduce_store<4>(acc, a.partials);
 }
 
@@ -468,15 +468,16 @@ void launch_shell_extract(const float* filtered, long long P, int n, int r0, flo
 // ComputeTs.c:438-475
 __global__ void k_cf_xe(CfArgs a, int D, int H, long long N)
 {
-  double acc[2] = { 0, 0 };
-  // per-cell collapse fraction in FP32, volume sums in FP64
+  CSum sum[2];
+  // per-cell collapse fraction in FP32, volume sums compensated (CSum)
   const float kcf = (float)((4.0 / 3.0) * PI_D * a.R3 / a.pixel_volume / a.RtoM_h2);
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
     const long long ip = pad_of(ir, D, H);
     const float cf = fminf(a.stars[ip] * kcf / (1.0f + a.deltax[ip]), 1.0f);
-    acc[0] += (double)cf;
-    acc[1] += (double)a.x_e_prev[ip];
+    sum[0].add(cf);
+    sum[1].add(a.x_e_prev[ip]);
   }
+  double acc[2] = { sum[0].value(), sum[1].value() };
   block_reduce_store<2>(acc, a.partials);
 }
 void launch_cf_xe(const CfArgs& a, const GridDims& gd, cudaStream_t s)
@@ -487,11 +488,12 @@ void launch_cf_xe(const CfArgs& a, const GridDims& gd, cudaStream_t s)
 
 __global__ void k_ts_means(const float* TS, const float* Tk, double* partials, long long N)
 {
-  double acc[2] = { 0, 0 };
+  CSum sum[2];
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    acc[0] += (double)TS[ir];
-    acc[1] += (double)Tk[ir];
+    sum[0].add(TS[ir]);
+    sum[1].add(Tk[ir]);
   }
+  double acc[2] = { sum[0].value(), sum[1].value() };
   block_reduce_store<2>(acc, partials);
 }
 void launch_ts_means(const float* TS, const float* Tk, double* partials, const GridDims& gd, cudaStream_t s)
@@ -504,7 +506,7 @@ void launch_ts_means(const float* TS, const float* Tk, double* partials, const G
 // BrightnessTemperature.c:84-124 and the mean at :512-535
 __global__ void k_delta_T(DeltaTArgs a, int D, int H, long long N)
 {
-  double acc[1] = { 0 };
+  CSum sum;
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
     const long long ip = pad_of(ir, D, H);
     float dT = a.const_factor * a.xH[ir] * (1.0f + a.deltax[ip]);
@@ -516,8 +518,9 @@ __global__ void k_delta_T(DeltaTArgs a, int D, int H, long long N)
         dT = dT * (1.0f - a.T_rad_f / ts);
     }
     a.delta_T[ir] = dT;
-    acc[0] += (double)dT;
+    sum.add(dT);
   }
+  double acc[1] = { sum.value() };
   block_reduce_store<1>(acc, a.partials);
 }
 void launch_delta_T(const DeltaTArgs& a, const GridDims& gd, cudaStream_t s)

@@ -9,6 +9,31 @@ namespace mx {
 // Reduction blocks used by every deterministic two-stage FP64 reduction.
 constexpr int RED_BLOCKS = 608;  // 4 x 152 SMs
 constexpr int RED_THREADS = 256;
+
+// ir / D for a non-negative cell index: a 32-bit division while the index
+// fits in 32 bits (every grid up to 1625^3), which costs a fraction of the
+// emulated 64-bit one
+__device__ __forceinline__ long long row_of(long long ir, int D)
+{
+  return ir < 4294967296LL ? (long long)((unsigned)ir / (unsigned)D) : ir / D;
+}
+
+// A thread's running sum of float terms as an unevaluated pair hi + lo
+// (Neumaier's compensated summation, error O(n eps^2) of the sum of |terms|):
+// as accurate as an FP64 running sum at these lengths, on the FP32 pipe
+// (GB300 issues FP64 at a small fraction of the FP32 rate).  value() is the
+// FP64 sum that the block and grid reductions (FP64) take.
+struct CSum
+{
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x)
+  {
+    const float t = hi + x;
+    lo += fabsf(hi) >= fabsf(x) ? (hi - t) + x : (x - t) + hi;
+    hi = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 constexpr int MAX_FIELDS = 5;
 constexpr int MAX_SHELLS = 64;
 constexpr int MAX_RADII = 256;

@@ -59,7 +59,7 @@ __host__ __device__ constexpr int ev_tables_floats(int S) { return 4 * NXHII * S
 
 __device__ __forceinline__ long long pad_index(long long ir, int D, int H)
 {
-  const long long row = ir / D;
+  const long long row = row_of(ir, D);
   return ir - row * D + row * 2LL * H;
 }
 
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(RED_THREADS, 2)
   if (threadIdx.x == 0 && light)
     for (int k = 0; k < STAGES && k < my_tiles; k++)
       ev_issue<STAGES>(bars, stages, a.shells, map, S, N, blockIdx.x + (long long)k * gridDim.x, k);
-  double acc[4] = { 0, 0, 0, 0 };
+  CSum sum[4];
   // the cell state of tile k + 1 is read while tile k is computed
   float n_delta = 0.f, n_xe = 0.f, n_T = 1.f;
   auto read_state = [&](int k) {
@@ -407,11 +407,12 @@ __global__ void __launch_bounds__(RED_THREADS, 2)
     a.x_e_prev[ip] = xe;
     a.Tk[ir] = T;
     a.TS[ir] = TS;
-    acc[0] += (double)Jalpha;
-    acc[1] += (double)xalpha;
-    acc[2] += (double)dxheat_dzp;
-    acc[3] += (double)ion;
+    sum[0].add(Jalpha);
+    sum[1].add(xalpha);
+    sum[2].add(dxheat_dzp);
+    sum[3].add(ion);
   }
+  double acc[4] = { sum[0].value(), sum[1].value(), sum[2].value(), sum[3].value() };
   block_sum_store<4>(acc, a.partials);
 }
 

@@ -28,7 +28,7 @@ constexpr double MPC_CM = 3.086e24;
 __global__ void k_vel_convert(float* vel, int trees_id, float redshift, int D, int H, long long N)
 {
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long row = ir / D;
+    const long long row = row_of(ir, D);
     const long long ip = row * 2LL * H + (ir - row * D);
     float v = vel[ip];
     if (trees_id == 1)
@@ -63,7 +63,7 @@ __global__ void k_vel_grad_k(float2* spec, int H, long long C, double n_cells, d
 __global__ void k_pecvel_cells(PecvelArgs a, int D, int H, long long N)
 {
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long row = ir / D;
+    const long long row = row_of(ir, D);
     const long long ip = row * 2LL * H + (ir - row * D);
     const double g = (double)a.grad[ip];
     if (a.mode == 1) {

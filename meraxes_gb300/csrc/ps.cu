@@ -59,7 +59,7 @@ __global__ void k_ps_field(const float* __restrict__ dT, const double* __restric
 {
   const double ave = sum[0] / n_cells;
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long row = ir / D;
+    const long long row = row_of(ir, D);
     const long long ip = row * 2LL * H + (ir - row * D);
     float v = (float)(((double)dT[ir] / ave - 1) * (double)volume / (double)n_cells_f);
     v = (float)((double)v * ave);
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_ps_bin(PsArgs a)
 __global__ void k_ps_scale(const float* __restrict__ dT, float scale, int D, int H, long long N, float* __restrict__ out)
 {
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long row = ir / D;
+    const long long row = row_of(ir, D);
     out[row * 2LL * H + (ir - row * D)] = dT[ir] * scale;
   }
 }
@@ -191,7 +191,7 @@ __global__ void k_padded_to_real(const float* __restrict__ in, float scale, int 
                                  float* __restrict__ out)
 {
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long row = ir / D;
+    const long long row = row_of(ir, D);
     out[ir] = in[row * 2LL * H + (ir - row * D)] * scale;
   }
 }
