@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, i
   if (threadIdx.x == 0 && light)
     for (int k = 0; k < 2 && k < my_tiles; k++)
       ev_issue(bars, stages, a.shells, map, S, N, blockIdx.x + (long long)k * gridDim.x, k);
-  double acc[2] = { 0, 0 };
+  CSum sum[2];
   for (int k = 0; k < my_tiles; k++) {
     const long long tile = blockIdx.x + (long long)k * gridDim.x;
     const long long ir = tile * EV_TILE + threadIdx.x;
@@ -747,10 +747,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, i
         ev_issue(bars, stages, a.shells, map, S, N, tile + 2LL * gridDim.x, k + 2);
     }
     if (valid) {
-      acc[0] += (double)heat_bar * heat + (double)ion_bar * ion + (double)lya_bar * lya;
-      acc[1] += (double)heat_bar * dheat + (double)ion_bar * dion + (double)lya_bar * dlya;
+      sum[0].add(fmaf(heat_bar, heat, fmaf(ion_bar, ion, lya_bar * lya)));
+      sum[1].add(fmaf(heat_bar, dheat, fmaf(ion_bar, dion, lya_bar * dlya)));
     }
   }
+  double acc[2] = { sum[0].value(), sum[1].value() };
   block_sum_store<2>(acc, a.partials);
 }
 
@@ -773,7 +774,7 @@ int ts_kernel_launches() { return ts_launches; }
 __global__ void k_homog_f32(HomogArgs a, int D, int H, long long N)
 {
   const TsDevConst& c = *a.cst;
-  double acc[1] = { 0 };
+  CSum sum;
   const float kcf = (float)((4.0 / 3.0) * 3.14159265358979323846 * a.R3 / a.pixel_volume / a.RtoM_h2);
   for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
     const long long ip = pad_index(ir, D, H);
@@ -785,8 +786,9 @@ __global__ void k_homog_f32(HomogArgs a, int D, int H, long long N)
       TS = get_Ts_d(c, c.zp, delta, a.tk0, a.xe0, 0.0f, &xa, a.err);
     a.TS[ir] = TS;
     const float cf = fminf(a.stars[ip] * kcf / (1.0f + delta), 1.0f);
-    acc[0] += (double)cf;
+    sum.add(cf);
   }
+  double acc[1] = { sum.value() };
   block_sum_store<1>(acc, a.partials);
 }
 

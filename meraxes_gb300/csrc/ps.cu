@@ -25,9 +25,10 @@ thread_local int ps_launches = 0;
 __global__ void k_ps_sum(const float* __restrict__ dT, long long N, double* partials)
 {
   __shared__ double sh[RED_THREADS / 32];
-  double acc = 0.0;
+  CSum sum;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
-    acc += (double)dT[i];
+    sum.add(dT[i]);
+  double acc = sum.value();
   for (int o = 16; o > 0; o >>= 1)
     acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0)
