@@ -847,6 +847,23 @@ __device__ void z_abort(char* smem, int it, int n_items, unsigned* err)
     mbar_wait(&bars[j % ZSTAGES], (unsigned)(j / ZSTAGES) & 1u);
 }
 
+// The FP64 decision of the threshold for a cell whose FP32 sides lie within
+// 4e-6 of each other, as the reference writes it (find_HII_bubbles.c:348-
+// 428): returns whether the cell is ionised and sets the partial xH.  Out of
+// line, so that the rare FP64 path does not weigh on the registers and the
+// schedule of the per-cell loop.
+__device__ __noinline__ bool threshold_fp64(float dx, float stv, float nr, float xe, bool recomb, bool spin,
+                                            double M_mean, double R_cubed, double pixel_volume, double eff,
+                                            float* xpart)
+{
+  const double dom = 1.0 + (double)dx;
+  const double rec = recomb ? (double)nr / dom : 0.0;
+  const double nf = spin ? 1.0 - (double)xe : 1.0;
+  const double f_coll = (double)stv / (M_mean * dom) * (4.0 / 3.0) * PI_D * R_cubed / pixel_volume;
+  *xpart = (float)__dsub_rn(nf, __dmul_rn(f_coll, eff));
+  return f_coll * eff > nf * (1. + rec);
+}
+
 // cell state bits of the threshold z-pass
 constexpr unsigned ST_ION = 1u;      // ionised at some radius of this launch
 constexpr unsigned ST_XHIGH = 2u;    // xH at launch start > REL_TOL
@@ -963,12 +980,7 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdAr
         ionised = lhs_f > rhs_f;
         xpart = nf_f - lhs_f;
       } else {
-        const double dom = 1.0 + (double)dx;
-        const double rec = RECOMB ? (double)nr / dom : 0.0;
-        const double nf = SPIN ? 1.0 - (double)xe : 1.0;
-        const double f_coll = (double)stv / (rp.M_mean * dom) * (4.0 / 3.0) * PI_D * rp.R_cubed / a.pixel_volume;
-        ionised = f_coll * a.eff > nf * (1. + rec);
-        xpart = (float)__dsub_rn(nf, __dmul_rn(f_coll, a.eff));
+        ionised = threshold_fp64(dx, stv, nr, xe, RECOMB, SPIN, rp.M_mean, rp.R_cubed, a.pixel_volume, a.eff, &xpart);
       }
       const long long ir = rowc * D + zc[e] + (hi ? 1 : 0);
       unsigned s = st[c];
