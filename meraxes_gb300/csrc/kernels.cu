@@ -63,6 +63,9 @@ __device__ void block_reduce_store(double (&v)[NV], double* partials)
   }
 }
 
+// cells whose loads a grid-stride loop issues together
+constexpr int CELL_BATCH = 4;
+
 __device__ __forceinline__ long long pad_of(long long ir, int D, int H)
 {
   const long long row = row_of(ir, D);
@@ -311,13 +314,14 @@ __global__ void k_fhb_reduce(FhbReduceArgs a, int D, int H, long long N)
     const long long ip = pad_of(ir, D, H);
     const float xHf = a.xH[ir];
     const float dxf = a.deltax[ip];
+    const float j21 = a.uvb ? a.J21[ir] : 0.0f;
+    const float g12 = a.recomb ? a.Gamma12[ir] : 0.0f;
     sum[0].add(xHf);
     if (a.uvb)
-      sum[1].add(a.J21[ir]);
+      sum[1].add(j21);
     const float domf = 1.0f + dxf;
     sum[2].add(xHf * domf);
     sum[3].add(domf);
-    const float g12 = a.recomb ? a.Gamma12[ir] : 0.0f;
     // dNrec is exactly zero for neutral cells and for Gamma12 = 0 (log -> -inf)
     if (a.recomb && xHf < 1.0f && g12 > 0.0f) {
       // FP32 lookup of splined_recombination_rate (recombinations.c:30-52);
@@ -469,13 +473,29 @@ void launch_shell_extract(const float* filtered, long long P, int n, int r0, flo
 __global__ void k_cf_xe(CfArgs a, int D, int H, long long N)
 {
   CSum sum[2];
-  // per-cell collapse fraction in FP32, volume sums compensated (CSum)
+  // per-cell collapse fraction in FP32, volume sums compensated (CSum); the
+  // loads of CELL_BATCH cells of a thread's stride are issued together
   const float kcf = (float)((4.0 / 3.0) * PI_D * a.R3 / a.pixel_volume / a.RtoM_h2);
-  for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long ip = pad_of(ir, D, H);
-    const float cf = fminf(a.stars[ip] * kcf / (1.0f + a.deltax[ip]), 1.0f);
-    sum[0].add(cf);
-    sum[1].add(a.x_e_prev[ip]);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long ir0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir0 < N; ir0 += CELL_BATCH * stride) {
+    float st[CELL_BATCH], dx[CELL_BATCH], xe[CELL_BATCH];
+#pragma unroll
+    for (int u = 0; u < CELL_BATCH; u++) {
+      const long long ir = ir0 + u * stride;
+      if (ir < N) {
+        const long long ip = pad_of(ir, D, H);
+        st[u] = a.stars[ip];
+        dx[u] = a.deltax[ip];
+        xe[u] = a.x_e_prev[ip];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < CELL_BATCH; u++) {
+      if (ir0 + u * stride < N) {
+        sum[0].add(fminf(st[u] * kcf / (1.0f + dx[u]), 1.0f));
+        sum[1].add(xe[u]);
+      }
+    }
   }
   double acc[2] = { sum[0].value(), sum[1].value() };
   block_reduce_store<2>(acc, a.partials);
@@ -507,18 +527,34 @@ void launch_ts_means(const float* TS, const float* Tk, double* partials, const G
 __global__ void k_delta_T(DeltaTArgs a, int D, int H, long long N)
 {
   CSum sum;
-  for (long long ir = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir < N; ir += (long long)gridDim.x * blockDim.x) {
-    const long long ip = pad_of(ir, D, H);
-    float dT = a.const_factor * a.xH[ir] * (1.0f + a.deltax[ip]);
-    if (a.spin) {
-      const float ts = a.TS[ir];
-      if (a.pecvel > 1)
-        dT = dT * ((1.0f + a.redshift) / (1000.0f * ts));
-      else
-        dT = dT * (1.0f - a.T_rad_f / ts);
+  // the loads of CELL_BATCH cells of a thread's stride are issued together
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long ir0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; ir0 < N; ir0 += CELL_BATCH * stride) {
+    float xh[CELL_BATCH], dx[CELL_BATCH], ts[CELL_BATCH];
+#pragma unroll
+    for (int u = 0; u < CELL_BATCH; u++) {
+      const long long ir = ir0 + u * stride;
+      if (ir < N) {
+        xh[u] = a.xH[ir];
+        dx[u] = a.deltax[pad_of(ir, D, H)];
+        ts[u] = a.spin ? a.TS[ir] : 1.0f;
+      }
     }
-    a.delta_T[ir] = dT;
-    sum.add(dT);
+#pragma unroll
+    for (int u = 0; u < CELL_BATCH; u++) {
+      const long long ir = ir0 + u * stride;
+      if (ir < N) {
+        float dT = a.const_factor * xh[u] * (1.0f + dx[u]);
+        if (a.spin) {
+          if (a.pecvel > 1)
+            dT = dT * ((1.0f + a.redshift) / (1000.0f * ts[u]));
+          else
+            dT = dT * (1.0f - a.T_rad_f / ts[u]);
+        }
+        a.delta_T[ir] = dT;
+        sum.add(dT);
+      }
+    }
   }
   double acc[1] = { sum.value() };
   block_reduce_store<1>(acc, a.partials);
