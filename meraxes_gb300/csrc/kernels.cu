@@ -307,6 +307,11 @@ void launch_threshold(const ThresholdArgs& a, const GridDims& gd, cudaStream_t s
 __global__ void k_fhb_reduce(FhbReduceArgs a, int D, int H, long long N)
 {
   CSum sum[4];
+  // the lnGamma nodes of the recombination table, searched per cell
+  __shared__ float rr_x[RR_LNG_NPTS];
+  for (int i = threadIdx.x; i < RR_LNG_NPTS; i += blockDim.x)
+    rr_x[i] = a.recomb ? a.rr_xf[i] : 0.0f;
+  __syncthreads();
   // RR_DEL_LNG * RR_LNG_NPTS is a float product in recombinations.c:46
   const double lng_top = RR_LNG_MIN + (double)(RR_DEL_LNG * (float)RR_LNG_NPTS);
   const float dNfac = a.fabs_dtdz * a.zstep;
@@ -344,7 +349,7 @@ __global__ void k_fhb_reduce(FhbReduceArgs a, int D, int H, long long N)
       if (!below) {
         if ((double)lnG >= lng_top)
           lnG = (float)(lng_top - FRACT_FLOAT_ERR);
-        const float* x = a.rr_xf;
+        const float* x = rr_x;
         const float* y = a.rr_yf + (long long)z_ct * RR_LNG_NPTS;
         const float* c = a.rr_cf + (long long)z_ct * RR_LNG_NPTS;
         float rr;
