@@ -48,10 +48,12 @@ FESC = 0.01
 # 256^3, 272 for 257 at 512^3): PAD_512_OVER_256 rescales that share.
 _C256, _N256 = 256 * 256 * 129, 256 ** 3
 PAD_512_OVER_256 = (272 / 257) / (144 / 129)
+_C512 = 512 * 512 * 257
 DRAM_PER_ALGORITHMIC = {
     # find_HII_bubbles launch: 5 fields x 2 radii (5 unfiltered spectra read, 10 written)
-    "fft_x_filter": 1040.55e6 / (8 * _C256 * 5 * (1 + 2)) * PAD_512_OVER_256,
-    "fft_y": 1447.70e6 / (16 * _C256 * 10) * PAD_512_OVER_256,                     # 10 spectra
+    # measured at 512^3 (profiles/dram_traffic_evolve512.md): the 5-field, 40-radius launches
+    "fft_x_filter": (2.93e9 + 114.88e9) / (8 * _C512 * 5 * (1 + 40)),
+    "fft_y": (114.10e9 + 114.02e9) / (16 * _C512 * 200),
     "fft_z_threshold": 892.79e6 / (8 * _C256 * 10 + 2 * 4 * _N256) * PAD_512_OVER_256,  # 10 spectra + xH, z_at_ion
     "fft_z_store": 1236.80e6 / ((8 * _C256 + 4 * _N256) * 9),                       # 9 shells
     "k_evolve": 3084.0e6 / (46 * 4 * _N256),
