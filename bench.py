@@ -37,21 +37,22 @@ METRIC = "ms/snapshot at 512^3 (ComputeTs + find_HII_bubbles + 21cm box)"
 UNIT = "ms/snapshot"
 REION_EFF = 1.0 / 0.15714 * 4000.0 / (1.0 - 0.75 * 0.24)
 FESC = 0.01
-# DRAM bytes (read + write) per algorithmic byte of each kernel, from one ncu
-# capture of the same workload at 256^3 (profiles/*_256.md):
-# `ncu --set full -k regex:"k_fft_x_filter|k_fft_y|k_fft_z_threshold|k_fft_z_store|k_evolve_f32" -s 10 -c 7`
-# on `python bench.py --grid 256 --steps 1 --warmup 1 --no-cpu --no-e2e` with
-# MX_MAX_BATCH_SPECTRA=10.  Each kernel's DRAM traffic grows in proportion to
-# the spectra (or cells) it processes, so traffic per launch at 512^3 is this
-# ratio times the launch's algorithmic bytes.  The transforms also move the
-# row padding of the batch spectra (rows of 144 complex values for 129 at
-# 256^3, 272 for 257 at 512^3): PAD_512_OVER_256 rescales that share.
+# DRAM bytes (read + write) per algorithmic byte of each kernel.  The x- and
+# y-pass ratios come from a single-pass ncu capture (dram__bytes_read/write)
+# of this workload at 512^3; the others from an `ncu --set full` capture of
+# the same kernels at 256^3 (`python bench.py --grid 256 --steps 1 --warmup 1
+# --no-cpu --no-e2e` with MX_MAX_BATCH_SPECTRA=10).  Each kernel's DRAM
+# traffic grows in proportion to the spectra (or cells) it processes, so
+# traffic per launch at 512^3 is this ratio times the launch's algorithmic
+# bytes.  The transforms also move the row padding of the batch spectra (rows
+# of 144 complex values for 129 at 256^3, 272 for 257 at 512^3):
+# PAD_512_OVER_256 rescales that share of the 256^3 ratios.
 _C256, _N256 = 256 * 256 * 129, 256 ** 3
 PAD_512_OVER_256 = (272 / 257) / (144 / 129)
 _C512 = 512 * 512 * 257
 DRAM_PER_ALGORITHMIC = {
     # find_HII_bubbles launch: 5 fields x 2 radii (5 unfiltered spectra read, 10 written)
-    # measured at 512^3 (profiles/dram_traffic_evolve512.md): the 5-field, 40-radius launches
+    # measured at 512^3 on the 5-field, 40-radius launches
     "fft_x_filter": (2.93e9 + 114.88e9) / (8 * _C512 * 5 * (1 + 40)),
     "fft_y": (114.10e9 + 114.02e9) / (16 * _C512 * 200),
     "fft_z_threshold": 892.79e6 / (8 * _C256 * 10 + 2 * 4 * _N256) * PAD_512_OVER_256,  # 10 spectra + xH, z_at_ion
