@@ -64,16 +64,16 @@ DRAM_PER_ALGORITHMIC = {
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--grid", type=int, default=512)
     ap.add_argument("--e2e-steps", type=int, default=4)
-    ap.add_argument("--cpu-sample-grid", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--adjoint-grid", type=int, default=256)
     return ap.parse_args(argv)
 
@@ -253,6 +253,89 @@ def state_grids(p, z_prev, device):
 
 
 # -------------------------------------------------------------------- arms
+def time_evolution(step, w, fields, hist, smax, warm, timed, device, world, local, profile=False):
+    """Runs the warm-up snapshots, resets the state, then times the
+    snapshots `timed` of one evolution from the initial state (CUDA events
+    on the default stream, barrier + synchronize on both sides).  Where the
+    timed list wraps past the last snapshot, the state is reset to the
+    initial state (a device copy inside the timed region) so that every
+    snapshot runs on the state of its own evolution."""
+    import torch
+
+    n_hist = step.n_sfr_histories
+    state0 = state_grids(w.params, w.redshifts[0], device)
+    state = {k: v.clone() for k, v in state0.items()}
+
+    def grids_for(s):
+        g = dict(state)
+        g.update(fields[s])
+        g["sfr_histories"] = hist[smax - s: smax - s + n_hist]
+        return g
+
+    def reset():
+        for k, v in state0.items():
+            state[k].copy_(v)
+
+    for s in warm:
+        if s == 0:
+            reset()
+        step.step(s, grids_for(s))
+    reset()
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if profile:
+        step.profile(True)
+    launches = 0
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0.record()
+    glob = None
+    for i, s in enumerate(timed):
+        if s == 0 and i > 0:
+            reset()
+        glob = step.step(s, grids_for(s))
+        launches += step.last_launches
+    t1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = t0.elapsed_time(t1)
+    clk = clocks.stop()
+    kstats = None
+    if profile:
+        kstats = step.profile_read()
+        step.profile(False)
+    return ms, launches, glob, clk, kstats
+
+
+def run_plain_gpu(args, w, fields, hist, smax, warm, timed, device, world, local):
+    """The "plain GPU" comparator: the same evolution through the same entry
+    points with the transforms of a plain GPU port (MX_TRANSFORM=cufft: one
+    cuFFT R2C per field, then per radius and field a filter kernel, a cuFFT
+    C2R and separate clamp/threshold kernels, the loop structure of the
+    reference)."""
+    from meraxes_gb300.api import ReionGridStep
+
+    old = os.environ.get("MX_TRANSFORM")
+    os.environ["MX_TRANSFORM"] = "cufft"
+    try:
+        step = ReionGridStep(w.params, w.redshifts)
+    finally:
+        if old is None:
+            os.environ.pop("MX_TRANSFORM", None)
+        else:
+            os.environ["MX_TRANSFORM"] = old
+    ms, launches, glob, clk, _ = time_evolution(step, w, fields, hist, smax, warm, timed, device, world, local)
+    step.close()
+    return {"value": round(replica_value(ms, len(timed), world, device), 3), "unit": UNIT,
+            "transform": "cuFFT R2C/C2R + per-radius filter and threshold kernels (MX_TRANSFORM=cufft)",
+            "steps": len(timed), "gpu_launches": launches, "clocks": clk,
+            "last_volume_weighted_global_xH": glob["volume_weighted_global_xH"]}
+
+
 def run_gb300(args, rank, world, local):
     import torch
 
@@ -265,48 +348,16 @@ def run_gb300(args, rank, world, local):
     p = w.params
     D = p.grid_dim
     n_snap = len(w.redshifts)
-    total = args.warmup + args.steps
-    order = [i % n_snap for i in range(total)]
-    used = sorted(set(order))
+    warm = [i % n_snap for i in range(args.warmup)]
+    timed = [i % n_snap for i in range(args.steps)]
+    used = sorted(set(warm) | set(timed))
     fields = make_device_fields(w, used, device)
-    from meraxes_gb300.params import ReionParams  # noqa: F401
 
     step = ReionGridStep(p, w.redshifts)
     n_hist = step.n_sfr_histories
     hist, smax = history_buffer(fields, used, n_hist, D, device)
-    state = state_grids(p, w.redshifts[0], device)
-
-    def grids_for(s):
-        g = dict(state)
-        g.update(fields[s])
-        g["sfr_histories"] = hist[smax - s: smax - s + n_hist]
-        return g
-
-    # warm-up (also the first snapshots of the evolution)
-    for i in range(args.warmup):
-        step.step(order[i], grids_for(order[i]))
-    torch.cuda.synchronize()
-    barrier(world)
-    clocks = ClockSampler(local)
-    clocks.start()
-    step.profile(True)
-    launches = 0
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    barrier(world)
-    t0.record()
-    glob = None
-    for i in range(args.warmup, total):
-        glob = step.step(order[i], grids_for(order[i]))
-        launches += step.last_launches
-    t1.record()
-    torch.cuda.synchronize()
-    barrier(world)
-    ms = t0.elapsed_time(t1)
-    clk = clocks.stop()
-    kstats = step.profile_read()
-    step.profile(False)
+    ms, launches, glob, clk, kstats = time_evolution(step, w, fields, hist, smax, warm, timed, device, world, local,
+                                                     profile=True)
     value = replica_value(ms, args.steps, world, device)
 
     # per-kernel achieved bandwidth (algorithmic bytes / event time)
@@ -347,8 +398,13 @@ def run_gb300(args, rank, world, local):
     e2e = None
     if not args.no_e2e and args.e2e_steps > 0:
         e2e = run_e2e(args, step, w, fields, used, n_hist, device, world)
+    block_sizes = list(step.fft_block_sizes())
+    step.close()
+    plain = None
+    if not args.no_plain:
+        plain = run_plain_gpu(args, w, fields, hist, smax, warm, timed, device, world, local)
 
-    del fields, hist, state
+    del fields, hist
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(value * world, 3), "higher_is_better": False,
@@ -356,10 +412,12 @@ def run_gb300(args, rank, world, local):
         "data": "synthetic (seeded Gaussian density, stellar and SFR grids)",
         "config": {"workload": f"evolve_512: {D}^3, L={p.box_size} Mpc/h, 20 snapshots z=15..6, "
                                "ComputeTs 40 shells + find_HII_bubbles 41 radii x 5 fields + 21cm box",
-                   "grid": D, "snapshots_timed": [order[i] for i in range(args.warmup, total)],
+                   "grid": D, "snapshots_warmup": warm, "snapshots_timed": timed,
+                   "state": "the timed snapshots are one evolution from the initial state (reset after the "
+                            "warm-up)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (each grid 0.54 GB at 512^3)",
-                   "fft_block_sizes": list(step.fft_block_sizes())},
+                   "fft_block_sizes": block_sizes},
         "gpu_launches": launches, "clocks": clk, "roofline": roofline,
         "step_model_gbs": round(model_gbs, 1), "step_model_frac": round(model_gbs / hbm_peak, 4),
         "step_model_bytes": model_bytes, "step_pass_gbs": round(step_gbs, 1),
@@ -369,6 +427,9 @@ def run_gb300(args, rank, world, local):
     }
     if e2e:
         out["e2e"] = e2e
+    if plain:
+        plain["ratio_to_value"] = round(plain["value"] / value, 3)
+        out["plain_gpu"] = plain
     if not args.no_adjoint and args.adjoint_grid > 0:
         out["adjoint"] = run_adjoint_ratio(args)
     if not args.no_batch and world == 1:
@@ -534,99 +595,150 @@ def run_e2e(args, step, w, fields, used, n_hist, device, world):
         t0 = time.perf_counter()
         step.step(s, host)
         t += time.perf_counter() - t0
-    return {"value": round(replica_value(t * 1e3, args.e2e_steps, world, device), 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps, "entry_point": "mx_step (host pointers)"}
+    # the drop-in adapter's path: the reference's three entry points called
+    # one after another (ComputeTs, find_HII_bubbles, the 21cm box), each
+    # copying the grids it reads to the device and the grids it writes back
+    step.ComputeTs(s, host)
+    torch.cuda.synchronize()
+    t3 = 0.0
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        step.ComputeTs(s, host)
+        step.find_HII_bubbles(s, host)
+        step.ComputeBrightnessTemperatureBox(s, host)
+        t3 += time.perf_counter() - t0
+    return {"value": round(replica_value(t * 1e3, args.e2e_steps, world, device), 3), "unit": UNIT,
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+            "entry_point": "mx_step (host pointers)",
+            "three_calls": {"value": round(replica_value(t3 * 1e3, args.e2e_steps, world, device), 3), "unit": UNIT,
+                            "entry_points": "mx_ComputeTs, mx_find_HII_bubbles, "
+                                            "mx_ComputeBrightnessTemperatureBox (host pointers, as the C "
+                                            "adapter calls them)"}}
 
 
-def cpu_sample(grid_s: int, threads: int):
-    """One full snapshot of the oracle at grid_s^3 with the evolve_512 cell size
-    (and its filter radii, shells and physics), timed on the host cores."""
-    from cases import initial
+# CPU timing.  The reference runs this step on CPU cores (FFTW float
+# transforms, per-cell C loops); its CPU path is timed here as the oracle
+# port built with single-precision transforms (oracle/_build/
+# libmxoracle_f32.so: batched Stockham FFTs and per-cell loops on all host
+# threads) at the benchmark's own grid size.  A full 512^3 snapshot takes
+# minutes, so a timed snapshot is a bounded sample of itself: the first
+# `radii` radii of find_HII_bubbles, the first `shells` ComputeTs shells and
+# 1/`cell_div` of the per-cell spin-temperature work are run and timed, and
+# the per-radius, per-shell and per-cell times are scaled to the workload's 41
+# radii, 40 shells and all cells.  Everything else (the forward transforms,
+# the collapse fraction, the frequency-integral tables, the global means,
+# N_rec, delta_T) runs in full.  The oracle keeps its grid buffers across
+# calls, as the reference allocates its grids once, so the first snapshot of
+# a process also pays the first touch of those buffers and is not timed.
+CPU_SAMPLE = {"radii": 3, "shells": 3, "cell_div": 16}
+
+
+def cpu_run(grid: int, threads: int, radii: int, shells: int, cell_div: int, runs: int) -> dict:
+    """Runs `runs` sampled snapshots (snapshot 10 of evolve_512 at grid^3) of
+    the oracle port in this process; returns each run's estimated full
+    snapshot time (s) with its measured parts."""
     from meraxes_gb300 import synthetic as syn
     from oracle import OracleBackend
 
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    w = workload_for(grid_s)
-    orc = OracleBackend(w.params, w.redshifts, syn.TABLES_DIR)
+    w = workload_for(grid)
+    n_R = len(w.params.filter_radii())
+    S = w.params.ts_num_filter_steps
+    orc = OracleBackend(w.params, w.redshifts, syn.TABLES_DIR, timing=True)
+    orc.set_timing_sample(radii, shells, cell_div)
     gen = syn.FieldGenerator(w)
     s = 10
-    st = syn.initial_state(w.params, w.redshifts[s - 1])
-    st.update(gen.inputs(s, orc.n_sfr_histories))
-    t0 = time.perf_counter()
-    orc.step(s, st)
-    return time.perf_counter() - t0
-
-
-def cpu_extrapolate(samples, grid: int):
-    """Fits t(D) = a + b * D^3 log2(D^3) to timed samples (fixed per-snapshot
-    table work + grid work) and evaluates it at `grid`."""
-    xs = np.array([d ** 3 * np.log2(d ** 3) for d, _ in samples], dtype=np.float64)
-    ts = np.array([t for _, t in samples], dtype=np.float64)
-    if len(samples) >= 2:
-        b = (ts[-1] - ts[0]) / (xs[-1] - xs[0])
-        b = max(b, ts[-1] / xs[-1] * 0.5)
-        a = max(ts[-1] - b * xs[-1], 0.0)
-    else:
-        a, b = 0.0, ts[0] / xs[0]
-    x = grid ** 3 * np.log2(grid ** 3)
-    return a + b * x, a, b
-
-
-def cpu_samples(grid_s: int, threads: int):
-    code = (f"import sys; sys.path.insert(0, {ROOT!r}); sys.path.insert(0, {os.path.join(ROOT, 'tests')!r});"
-            "import bench; print(bench.cpu_sample(%d, %d))")
-    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    st0 = syn.initial_state(w.params, w.redshifts[s - 1])
+    st0.update(gen.inputs(s, orc.n_sfr_histories))
     out = []
-    for d in (grid_s // 2, grid_s):
-        r = subprocess.run([sys.executable, "-c", code % (d, threads)], capture_output=True, text=True, env=env,
-                           timeout=1800)
-        if r.returncode != 0:
-            raise RuntimeError(r.stderr[-500:])
-        out.append((d, float(r.stdout.strip().split()[-1])))
-    return out
+    for _ in range(runs):
+        st = {k: v.copy() for k, v in st0.items()}
+        t0 = time.perf_counter()
+        orc.ComputeTs(s, st)
+        t1 = time.perf_counter()
+        ts = orc.phase_times()
+        orc.find_HII_bubbles(s, st)
+        t2 = time.perf_counter()
+        fh = orc.phase_times()
+        orc.delta_T(s, st)
+        t3 = time.perf_counter()
+        per_radius = fh["radii"] / max(fh["n_radii"], 1)
+        per_shell = ts["shells"] / max(ts["n_shells"], 1)
+        est_ts = (t1 - t0) - ts["shell_copies"] + per_shell * (S - ts["n_shells_run"]) \
+            + ts["evolve"] * (1.0 / ts["evolve_frac"] - 1.0)
+        est_fhb = (t2 - t1) + per_radius * (n_R - fh["n_radii_run"])
+        out.append({"estimate_s": est_ts + est_fhb + (t3 - t2), "sampled_s": t3 - t0, "ComputeTs_s": est_ts,
+                    "find_HII_bubbles_s": est_fhb, "delta_T_s": t3 - t2, "per_radius_s": per_radius,
+                    "per_shell_s": per_shell, "evolve_s": ts["evolve"] / ts["evolve_frac"],
+                    "forward_s": fh["forward"], "tables_s": ts["tables"]})
+    orc.close()
+    return {"grid": grid, "threads": threads, "n_radii": n_R, "n_shells": S, "runs": out}
+
+
+def cpu_runs(grid: int, threads: int, runs: int, sample=None, timeout: float = 3000) -> dict:
+    """cpu_run in a child process with OMP_NUM_THREADS = threads (the child
+    keeps the oracle's OpenMP pool away from this process's CUDA context)."""
+    smp = dict(CPU_SAMPLE if sample is None else sample)
+    code = (f"import sys, json; sys.path.insert(0, {ROOT!r}); sys.path.insert(0, {os.path.join(ROOT, 'tests')!r});"
+            f"import bench; print(json.dumps(bench.cpu_run({grid}, {threads}, {smp['radii']}, {smp['shells']}, "
+            f"{smp['cell_div']}, {runs})))")
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_PROC_BIND="false")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr[-500:])
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    res["sample"] = smp
+    return res
+
+
+def cpu_sample_text(res: dict, timed: list) -> str:
+    smp = res["sample"]
+    r = timed[-1]
+    return (f"oracle port with single-precision transforms (oracle/_build/libmxoracle_f32.so), {res['threads']} "
+            f"host threads, snapshot 10 of evolve_512 at {res['grid']}^3; each timed snapshot runs the forward "
+            f"transforms, tables, means, N_rec and delta_T in full and {smp['radii']} of {res['n_radii']} radii, "
+            f"{smp['shells']} of {res['n_shells']} shells and 1/{smp['cell_div']} of the per-cell spin-temperature "
+            f"work, timed and scaled to the full counts (measured at {res['grid']}^3: {r['per_radius_s']:.2f} s per "
+            f"radius, {r['per_shell_s']:.2f} s per shell, {r['evolve_s']:.1f} s per-cell evolution, "
+            f"{r['forward_s']:.2f} s forward transforms; {r['sampled_s']:.1f} s of CPU work per timed snapshot); "
+            f"one untimed snapshot first")
 
 
 def cpu_baseline(args):
     threads = os.cpu_count() or 1
     try:
-        samples = cpu_samples(args.cpu_sample_grid, threads)
+        res = cpu_runs(args.grid, threads, 2)
     except Exception as e:  # noqa: BLE001
         return {"value": None, "unit": UNIT, "error": str(e)[-300:]}
-    t, a, b = cpu_extrapolate(samples, args.grid)
-    desc = ", ".join(f"{d}^3: {ts:.2f} s" for d, ts in samples)
-    return {"value": round(t * 1e3, 1), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"oracle (C restatement, OpenMP on all host threads) full step of snapshot 10 of evolve_512 "
-                      f"with its cell size at {desc}; extrapolated to {args.grid}^3 by t = a + b N log2 N "
-                      f"(a = {a:.2f} s per-snapshot tables, b fitted)"}
+    timed = res["runs"][1:]
+    est = timed[-1]["estimate_s"]
+    return {"value": round(est * 1e3, 1), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": cpu_sample_text(res, timed),
+            "parts_s": {k: round(v, 3) for k, v in timed[-1].items()}}
 
 
 def run_reference(args, rank, world):
-    """The CPU implementation of the path (the oracle port: the reference's
-    own build needs FFTW/GSL/MPI/HDF5 and the reference tree, absent on the
-    GPU host) on all host threads, on bounded samples of the workload."""
+    """The CPU implementation of the path on all host threads: the oracle
+    port (the reference's own build needs FFTW/GSL/MPI/HDF5 and the reference
+    tree, absent on the GPU host), each step one sampled snapshot at the
+    benchmark's grid size (CPU_SAMPLE), after W warm-up snapshots."""
     if rank != 0:
         return None, rank
     threads = os.cpu_count() or 1
-    vals = []
-    samples = None
-    for i in range(args.warmup + args.steps):
-        try:
-            samples = cpu_samples(args.cpu_sample_grid, threads)
-        except Exception as e:  # noqa: BLE001
-            return {"impl": "reference", "unavailable": "oracle port failed: " + str(e)[-300:]}, rank
-        if i >= args.warmup:
-            vals.append(cpu_extrapolate(samples, args.grid)[0])
-    value = statistics.mean(vals) * 1e3
-    desc = ", ".join(f"{d}^3: {ts:.2f} s" for d, ts in samples)
-    sample = (f"per step: oracle port full step of snapshot 10 of evolve_512 (its cell size) at {desc}; "
-              f"extrapolated to {args.grid}^3 by t = a + b N log2 N")
+    try:
+        res = cpu_runs(args.grid, threads, max(args.warmup, 1) + args.steps)
+    except Exception as e:  # noqa: BLE001
+        return {"impl": "reference", "unavailable": "oracle port failed: " + str(e)[-300:]}, rank
+    timed = res["runs"][max(args.warmup, 1):]
+    value = statistics.mean(r["estimate_s"] for r in timed) * 1e3
+    sample = cpu_sample_text(res, timed)
     return {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 1), "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 grids, f64 FFT internals and physics",
-            "data": "synthetic", "config": {"workload": f"evolve_512 at {args.grid}^3 (sampled)"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 grids and transforms, f64 physics",
+            "data": "synthetic", "config": {"workload": f"evolve_512 at {args.grid}^3 (sampled snapshots)"},
             "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
-            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}, rank
+            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "steps_s": [round(r["estimate_s"], 2) for r in timed]}, rank
 
 
 def main():

@@ -427,13 +427,18 @@ int mx_adjoint_device(mx_ctx* ctx,
                       double* grad_params,
                       void* stream);
 
-/* Build information: returns a static string. *//* Build information: returns a static string. */
+/* Build information: returns a static string. */
 const char* mx_build_info(void);
 
 /* Brightness-temperature box without any device allocation.  No counterpart
  * in the reference: it is the computation of
- * ComputeBrightnessTemperatureBox (BrightnessTemperature.c:495-545) for
- * callers that cannot allocate device memory.  A host that keeps all its
+ * ComputeBrightnessTemperatureBox without peculiar velocities (constants
+ * BrightnessTemperature.c:48-53, cell formula :82-124, volume average
+ * :530-545) for callers that cannot allocate device memory.  The cell formula
+ * runs in float (the reference rounds const_factor * xH * (1 + deltax) from
+ * double once): a few ulp, inside the 1e-4 relative tolerance of delta_T.
+ * Spin temperature together with flag_pecvel > 0 returns MX_ENOTSUP (the
+ * peculiar-velocity modes need the context's transforms).  A host that keeps all its
  * grids resident has often given the rest of the GPU to its own pool.  A
  * thread that must not stall cannot call cudaMalloc/cudaFree, which may
  * synchronise the device.  No context is needed.  All pointers are device
@@ -448,9 +453,11 @@ const char* mx_build_info(void);
  * MX_NOALLOC_MAX_CELLS cells (512^3) are rejected with MX_EINVAL.  Calls that
  * overlap in time on one device (different streams or threads, not ordered
  * by the caller) race on that scratch and give wrong means: serialise them.
- * The first call on each device looks up the scratch address for that device
- * (with it current).  Make that first call before starting any stream
- * capture.  On error the message goes to errbuf (may be NULL). */
+ * Each call outside stream capture looks up the scratch address on the
+ * current device; a call on a capturing stream uses the address of the last
+ * call outside capture on that device (MX_ESTATE if there was none), so make
+ * the first call on a device, and the first after a cudaDeviceReset, before
+ * any stream capture.  On error the message goes to errbuf (may be NULL). */
 #define MX_NOALLOC_MAX_CELLS 134217728
 #define MX_NOALLOC_SCRATCH_BYTES 65792
 int mx_brightness_temperature_noalloc(const mx_params* params,

@@ -46,10 +46,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     def compile_one(src: str) -> str:
         obj = os.path.join(OUT_DIR, "obj", os.path.splitext(src)[0] + ".o")
         cmd = [cc, "-c", os.path.join(CSRC, src), "-o", obj] + common
-        if src.endswith(".cu"):
-            cmd += ["-Xptxas", "-v"] if verbose else []
-        else:
-            cmd += ["-x", "cu"] if False else []
+        if src.endswith(".cu") and verbose:
+            cmd += ["-Xptxas", "-v"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

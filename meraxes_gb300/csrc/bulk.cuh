@@ -91,19 +91,44 @@ __device__ __forceinline__ unsigned long long global_ns()
   return t;
 }
 
-// Waits for phase `parity` of the barrier; false after about WAIT_LIMIT_NS.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
+// Polls a consumer's wait may take before it gives up (at most
+// WAIT_LIMIT_ITERS, and never longer than WAIT_LIMIT_NS).  One copy per
+// translation unit; set_consumer_wait_polls() sets this unit's copy.  A
+// context sets it when it is created: the default, or a lower value that a
+// test of the give-up path asks for (MX_WAIT_POLL_LIMIT).
+static __device__ long long consumer_wait_polls = WAIT_LIMIT_ITERS;
+
+static inline cudaError_t set_consumer_wait_polls(long long polls)
+{
+  return cudaMemcpyToSymbol(consumer_wait_polls, &polls, sizeof(polls));
+}
+
+__device__ __forceinline__ bool mbar_wait_polls(uint64_t* bar, unsigned parity, long long polls)
 {
   if (mbar_test(bar, parity))
     return true;
   const unsigned long long t0 = global_ns();
-  for (long long it = 1; it < WAIT_LIMIT_ITERS; it++) {
+  for (long long it = 1; it < polls; it++) {
     if (mbar_test(bar, parity))
       return true;
     if ((it & 255) == 0 && global_ns() - t0 > WAIT_LIMIT_NS)
       return false;
   }
   return false;
+}
+
+// A consumer's wait for phase `parity` of the barrier; false when it gives
+// up (consumer_wait_polls polls, or about WAIT_LIMIT_NS).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity)
+{
+  return mbar_wait_polls(bar, parity, consumer_wait_polls);
+}
+
+// The wait of a block that gave up, for its own copies still in flight
+// before it exits: always the full limit, whatever the consumers' limit.
+__device__ __forceinline__ bool mbar_drain(uint64_t* bar, unsigned parity)
+{
+  return mbar_wait_polls(bar, parity, WAIT_LIMIT_ITERS);
 }
 
 }  // namespace bulk

@@ -210,6 +210,8 @@ __device__ __forceinline__ float x_weight(int kx, float kyv, int kz, int D, floa
 
 int fft_kernel_launches() { return fft_launches; }
 
+cudaError_t fft_set_wait_polls(long long polls) { return set_consumer_wait_polls(polls); }
+
 // ---------------------------------------------------- column-tile engine
 // The x- and y-passes transform TXC adjacent columns (kz) of D points along
 // a slow axis.  D = R1 * R2 * R3; with n = n' + M n1 (M = R2 R3) and
@@ -844,7 +846,7 @@ __device__ void z_abort(char* smem, int it, int n_items, unsigned* err)
   atomicOr(err, ERR_PIPELINE_TIMEOUT);
   // items it .. min(it + ZSTAGES, n_items) - 1 may have been issued
   for (int j = it; j < n_items && j < it + ZSTAGES; j++)
-    mbar_wait(&bars[j % ZSTAGES], (unsigned)(j / ZSTAGES) & 1u);
+    mbar_drain(&bars[j % ZSTAGES], (unsigned)(j / ZSTAGES) & 1u);
 }
 
 // The FP64 decision of the threshold for a cell whose FP32 sides lie within

@@ -67,5 +67,7 @@ bool launch_fft_z_store(int D, const float2* spectra, long long C, int n, int r0
 int fft_z_row_groups(int D);
 int fft_z_rows_per_group(int D);
 int fft_kernel_launches();
+// Sets the poll limit of this unit's pipeline waits (bulk.cuh).
+cudaError_t fft_set_wait_polls(long long polls);
 
 }  // namespace mx

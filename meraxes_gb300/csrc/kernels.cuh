@@ -265,5 +265,7 @@ void launch_delta_T(const DeltaTArgs& a, const GridDims& gd, cudaStream_t s);
 int kernel_launch_count();
 void reset_kernel_launch_count();
 int ts_kernel_launches();
+// Sets the poll limit of the evolve kernels' pipeline waits (bulk.cuh).
+cudaError_t ts_set_wait_polls(long long polls);
 
 }  // namespace mx

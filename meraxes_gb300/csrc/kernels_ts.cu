@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(RED_THREADS, 2)
           atomicOr(a.err, bulk::ERR_PIPELINE_TIMEOUT);
           // copies of tiles k and k + 1 may still be in flight
           for (int j = k; j < my_tiles && j < k + STAGES; j++)
-            bulk::mbar_wait(&bars[j % STAGES], (unsigned)(j / STAGES) & 1u);
+            bulk::mbar_drain(&bars[j % STAGES], (unsigned)(j / STAGES) & 1u);
         }
         return;
       }
@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, i
         if (threadIdx.x == 0) {
           atomicOr(a.err, bulk::ERR_PIPELINE_TIMEOUT);
           for (int j = k; j < my_tiles && j < k + 2; j++)
-            bulk::mbar_wait(&bars[j & 1], (unsigned)(j >> 1) & 1u);
+            bulk::mbar_drain(&bars[j & 1], (unsigned)(j >> 1) & 1u);
         }
         return;
       }
@@ -768,6 +768,8 @@ void launch_evolve_adjoint(const AdjointArgs& a, const GridDims& gd, const void*
 }
 
 int ts_kernel_launches() { return ts_launches; }
+
+cudaError_t ts_set_wait_polls(long long polls) { return bulk::set_consumer_wait_polls(polls); }
 
 // Homogeneous branch, ComputeTs.c:189-262: x_e and T_K from RECFAST, T_S with
 // J_alpha = 0 (no iteration), and the collapse fraction.

@@ -20,6 +20,7 @@
 #include <thread>
 #include <vector>
 
+#include "bulk.cuh"
 #include "deposit.cuh"
 #include "fft3d.cuh"
 #include "lightcone.cuh"
@@ -2206,6 +2207,15 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
   try {
     if (cudaGetDevice(&c->device) != cudaSuccess)
       throw CudaError{ MX_ECUDA, "no CUDA device" };
+    // poll limit of the pipeline waits (process-wide on this device): the
+    // default, or a lower one that a test of the give-up path asks for
+    {
+      long long polls = bulk::WAIT_LIMIT_ITERS;
+      if (const char* env = std::getenv("MX_WAIT_POLL_LIMIT"))
+        polls = std::max(1LL, std::min(polls, std::atoll(env)));
+      MX_CUDA(fft_set_wait_polls(polls));
+      MX_CUDA(ts_set_wait_polls(polls));
+    }
     MX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     MX_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     MX_CUDA(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));

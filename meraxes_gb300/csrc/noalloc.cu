@@ -9,8 +9,12 @@
 // It takes the caller's device grids, and its only scratch is a file-scope
 // __device__ array of fixed size.
 //
-// Per-cell arithmetic: BrightnessTemperature.c:495-545 (the same float
-// operations as k_delta_T in kernels.cu).  The volume sum is deterministic.
+// Per-cell arithmetic: BrightnessTemperature.c:48-53 (constants) and :82-124
+// (the cell formula without peculiar velocities), in float: the reference
+// forms const_factor * xH * (1.0 + deltax) in double and rounds once, this
+// kernel rounds after each float product (a few ulp, well inside the 1e-4
+// relative tolerance of delta_T); the same float operations as k_delta_T in
+// kernels.cu.  The volume sum (:530-545) is deterministic.
 // Block b reduces cells [b * CELLS_PER_BLOCK, (b+1) * CELLS_PER_BLOCK) in a
 // fixed order and stores its partial.  The block that finishes last (by an
 // atomic ticket) sums the partials in index order and writes the mean.
@@ -105,6 +109,8 @@ __global__ void __launch_bounds__(NA_THREADS) k_delta_T_noalloc(NaArgs a)
     *a.mean = red[0] * a.inv_N;
 }
 
+// The scratch address per device, as last looked up outside stream capture
+// (calls made while their stream is capturing use it).
 std::mutex g_mu;
 void* g_scratch_addr[256] = {};
 
@@ -161,17 +167,31 @@ extern "C" int mx_brightness_temperature_noalloc(const mx_params* params,
     set_error(errbuf, errlen, "no current CUDA device");
     return MX_ECUDA;
   }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &capture) != cudaSuccess) {
+    set_error(errbuf, errlen, "invalid stream");
+    return MX_ECUDA;
+  }
   void* scratch = nullptr;
   {
-    // one symbol lookup per device, made with that device current
+    // The array's device address, looked up with the device current.  A call
+    // outside stream capture looks it up again, so that a context created
+    // anew on the device (after cudaDeviceReset) gets its own address; a
+    // call on a capturing stream uses the address of the last call outside
+    // capture.
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[dev]) {
-      const cudaError_t e = cudaGetSymbolAddress(&g_scratch_addr[dev], g_noalloc_scratch);
+    if (capture == cudaStreamCaptureStatusNone) {
+      void* addr = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
       if (e != cudaSuccess) {
-        g_scratch_addr[dev] = nullptr;
         set_error(errbuf, errlen, cudaGetErrorString(e));
         return MX_ECUDA;
       }
+      g_scratch_addr[dev] = addr;
+    } else if (!g_scratch_addr[dev]) {
+      set_error(errbuf, errlen, "the first call on a device must come before any stream capture");
+      return MX_ESTATE;
     }
     scratch = g_scratch_addr[dev];
   }
@@ -195,7 +215,6 @@ extern "C" int mx_brightness_temperature_noalloc(const mx_params* params,
   a.inv_N = 1.0 / (double)N;
   a.scratch = static_cast<unsigned char*>(scratch);
   a.mean = volume_ave_Tb;
-  cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned int), s);
   if (e == cudaSuccess) {
     const unsigned blocks = (unsigned)((N + NA_CELLS_PER_BLOCK - 1) / NA_CELLS_PER_BLOCK);

@@ -138,12 +138,166 @@ void mxo_fft_1d(double* data, int n, int sign)
   free(tmp);
 }
 
-/* Complex transforms of the half spectrum w ([D][D][H], double interleaved)
- * along x (axis 0) or y (axis 1).  Lines are independent, so they are
- * distributed over OpenMP threads; each line's arithmetic does not depend on
- * the thread count. */
-static void transform_axis(double* w, int D, int H, int axis, int sign)
+/* ------------------------------------------- 3-D transforms (FFTW layout)
+ *
+ * The work array of a 3-D transform holds the half spectrum [D][D][H]
+ * (H = D/2 + 1) as interleaved complex values of type fft_real: double by
+ * default, float when the library is compiled with MXO_FFT_SINGLE (the
+ * precision of the reference's fftwf calls; that build only serves CPU
+ * timing).
+ *
+ * Power-of-two lengths run a batched Stockham autosort FFT (radix-4 stages,
+ * one radix-2 stage when log2 n is odd): up to FFT_BATCH lines at a time are
+ * gathered into a buffer [n][B] whose batch index is fastest, so every
+ * butterfly is a short unit-stride loop over the batch.  Stockham's
+ * decimation in frequency, for a stage of length L and stride s (L s = n),
+ * maps x[q + s (p + r L/4)], r = 0..3, to y[q + s (4p + t)] with the
+ * twiddle w_L^{p t}; the next stage has length L/4 and stride 4s.  Other
+ * lengths use mxo_fft_1d line by line.  Lines are independent and spread
+ * over OpenMP threads; no line's arithmetic depends on the thread count. */
+#ifdef MXO_FFT_SINGLE
+typedef float fft_real;
+#else
+typedef double fft_real;
+#endif
+
+#define FFT_BATCH 16
+
+typedef struct p2_plan
 {
+  int n;
+  fft_real* tw; /* tw[2j], tw[2j+1] = cos, sin of 2 pi j / n */
+} p2_plan;
+
+static p2_plan g_p2[MXO_MAX_PLANS];
+static int g_np2 = 0;
+
+static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+/* Not thread-safe: called before the parallel regions. */
+static const p2_plan* get_p2(int n)
+{
+  for (int i = 0; i < g_np2; i++)
+    if (g_p2[i].n == n)
+      return &g_p2[i];
+  p2_plan* p;
+  if (g_np2 < MXO_MAX_PLANS) {
+    p = &g_p2[g_np2++];
+  } else {
+    p = &g_p2[0];
+    free(p->tw);
+  }
+  p->n = n;
+  p->tw = (fft_real*)malloc(sizeof(fft_real) * 2 * (size_t)n);
+  for (int j = 0; j < n; j++) {
+    const double ang = 2.0 * M_PI * (double)j / (double)n;
+    p->tw[2 * j] = (fft_real)cos(ang);
+    p->tw[2 * j + 1] = (fft_real)sin(ang);
+  }
+  return p;
+}
+
+/* B transforms of length n = P->n held in x as [n][B] (element (i, b) at
+ * x[2 (i B + b)]); y is scratch of the same size.  The result is left in x.
+ * sign = -1 forward, +1 backward; unnormalised. */
+static void p2_fft_batch(fft_real* x, fft_real* y, int B, int sign, const p2_plan* P)
+{
+  const int n = P->n;
+  const fft_real sg = (fft_real)sign;
+  fft_real* src = x;
+  fft_real* dst = y;
+  int s = 1;
+  for (int len = n; len > 1; len /= (len % 4 == 0 ? 4 : 2)) {
+    const int step = n / len; /* w_len^p = tw[p * step] */
+    if (len % 4 == 0) {
+      const int m = len / 4;
+      for (int p = 0; p < m; p++) {
+        const fft_real* t1 = P->tw + 2 * (size_t)p * step;
+        const fft_real* t2 = P->tw + 4 * (size_t)p * step;
+        const fft_real* t3 = P->tw + 6 * (size_t)p * step;
+        const fft_real w1r = t1[0], w1i = sg * t1[1];
+        const fft_real w2r = t2[0], w2i = sg * t2[1];
+        const fft_real w3r = t3[0], w3i = sg * t3[1];
+        for (int q = 0; q < s; q++) {
+          const fft_real* a = src + 2 * (size_t)(q + s * p) * B;
+          const fft_real* b = src + 2 * (size_t)(q + s * (p + m)) * B;
+          const fft_real* c = src + 2 * (size_t)(q + s * (p + 2 * m)) * B;
+          const fft_real* d = src + 2 * (size_t)(q + s * (p + 3 * m)) * B;
+          fft_real* o0 = dst + 2 * (size_t)(q + s * (4 * p)) * B;
+          fft_real* o1 = o0 + 2 * (size_t)s * B;
+          fft_real* o2 = o1 + 2 * (size_t)s * B;
+          fft_real* o3 = o2 + 2 * (size_t)s * B;
+          for (int j = 0; j < B; j++) {
+            const fft_real apcr = a[2 * j] + c[2 * j], apci = a[2 * j + 1] + c[2 * j + 1];
+            const fft_real amcr = a[2 * j] - c[2 * j], amci = a[2 * j + 1] - c[2 * j + 1];
+            const fft_real bpdr = b[2 * j] + d[2 * j], bpdi = b[2 * j + 1] + d[2 * j + 1];
+            /* sign * i * (b - d) */
+            const fft_real jr = -sg * (b[2 * j + 1] - d[2 * j + 1]), ji = sg * (b[2 * j] - d[2 * j]);
+            o0[2 * j] = apcr + bpdr;
+            o0[2 * j + 1] = apci + bpdi;
+            const fft_real y1r = amcr + jr, y1i = amci + ji;
+            const fft_real y2r = apcr - bpdr, y2i = apci - bpdi;
+            const fft_real y3r = amcr - jr, y3i = amci - ji;
+            o1[2 * j] = y1r * w1r - y1i * w1i;
+            o1[2 * j + 1] = y1r * w1i + y1i * w1r;
+            o2[2 * j] = y2r * w2r - y2i * w2i;
+            o2[2 * j + 1] = y2r * w2i + y2i * w2r;
+            o3[2 * j] = y3r * w3r - y3i * w3i;
+            o3[2 * j + 1] = y3r * w3i + y3i * w3r;
+          }
+        }
+      }
+      s *= 4;
+    } else { /* len == 2 */
+      for (int q = 0; q < s; q++) {
+        const fft_real* a = src + 2 * (size_t)q * B;
+        const fft_real* b = src + 2 * (size_t)(q + s) * B;
+        fft_real* o0 = dst + 2 * (size_t)q * B;
+        fft_real* o1 = dst + 2 * (size_t)(q + s) * B;
+        for (int j = 0; j < 2 * B; j++) {
+          const fft_real u = a[j], v = b[j];
+          o0[j] = u + v;
+          o1[j] = u - v;
+        }
+      }
+      s *= 2;
+    }
+    fft_real* t = src;
+    src = dst;
+    dst = t;
+  }
+  if (src != x)
+    memcpy(x, src, sizeof(fft_real) * 2 * (size_t)n * B);
+}
+
+/* Complex transforms of the half spectrum w along x (axis 0) or y (axis 1). */
+static void transform_axis(fft_real* w, int D, int H, int axis, int sign)
+{
+  if (is_pow2(D)) {
+    const p2_plan* P = get_p2(D);
+    const int nkb = (H + FFT_BATCH - 1) / FFT_BATCH;
+#pragma omp parallel
+    {
+      fft_real* buf = (fft_real*)malloc(sizeof(fft_real) * 4 * (size_t)D * FFT_BATCH);
+      fft_real* tmp = buf + 2 * (size_t)D * FFT_BATCH;
+#pragma omp for schedule(static)
+      for (long q = 0; q < (long)D * nkb; q++) {
+        const int a = (int)(q / nkb), kz0 = (int)(q % nkb) * FFT_BATCH;
+        const int B = H - kz0 < FFT_BATCH ? H - kz0 : FFT_BATCH;
+        for (int t = 0; t < D; t++) {
+          const size_t i = (axis == 0 ? ((size_t)t * D + a) : ((size_t)a * D + t)) * H + kz0;
+          memcpy(buf + 2 * (size_t)t * B, w + 2 * i, sizeof(fft_real) * 2 * (size_t)B);
+        }
+        p2_fft_batch(buf, tmp, B, sign, P);
+        for (int t = 0; t < D; t++) {
+          const size_t i = (axis == 0 ? ((size_t)t * D + a) : ((size_t)a * D + t)) * H + kz0;
+          memcpy(w + 2 * i, buf + 2 * (size_t)t * B, sizeof(fft_real) * 2 * (size_t)B);
+        }
+      }
+      free(buf);
+    }
+    return;
+  }
   (void)get_plan(D); /* create the shared plan before the parallel region */
 #pragma omp parallel
   {
@@ -159,62 +313,117 @@ static void transform_axis(double* w, int D, int H, int axis, int sign)
       mxo_fft_1d(line, D, sign);
       for (int t = 0; t < D; t++) {
         const size_t i = (axis == 0 ? ((size_t)t * D + a) : ((size_t)a * D + t)) * H + kz;
-        w[2 * i] = line[2 * t];
-        w[2 * i + 1] = line[2 * t + 1];
+        w[2 * i] = (fft_real)line[2 * t];
+        w[2 * i + 1] = (fft_real)line[2 * t + 1];
       }
     }
     free(line);
   }
 }
 
-void mxo_r2c_3d(int D, const float* in, int in_padded, float* out)
+/* z: rows of D real values (row q at in + q * rstride) -> the first H
+ * values of each row's forward DFT, into w */
+static void r2c_rows(int D, const float* in, int rstride, fft_real* w)
 {
   const int H = D / 2 + 1;
-  const size_t nc = (size_t)D * D * H;
-  const int rstride = in_padded ? 2 * H : D;
-  double* w = (double*)malloc(sizeof(double) * 2 * nc);
+  const long rows = (long)D * D;
+  if (is_pow2(D)) {
+    const p2_plan* P = get_p2(D);
+#pragma omp parallel
+    {
+      fft_real* buf = (fft_real*)malloc(sizeof(fft_real) * 4 * (size_t)D * FFT_BATCH);
+      fft_real* tmp = buf + 2 * (size_t)D * FFT_BATCH;
+#pragma omp for schedule(static)
+      for (long q0 = 0; q0 < rows; q0 += FFT_BATCH) {
+        const int B = rows - q0 < FFT_BATCH ? (int)(rows - q0) : FFT_BATCH;
+        for (int b = 0; b < B; b++) {
+          const float* src = in + (size_t)(q0 + b) * rstride;
+          for (int z = 0; z < D; z++) {
+            buf[2 * ((size_t)z * B + b)] = (fft_real)src[z];
+            buf[2 * ((size_t)z * B + b) + 1] = 0;
+          }
+        }
+        p2_fft_batch(buf, tmp, B, -1, P);
+        for (int b = 0; b < B; b++) {
+          fft_real* dst = w + 2 * (size_t)(q0 + b) * H;
+          for (int k = 0; k < H; k++) {
+            dst[2 * k] = buf[2 * ((size_t)k * B + b)];
+            dst[2 * k + 1] = buf[2 * ((size_t)k * B + b) + 1];
+          }
+        }
+      }
+      free(buf);
+    }
+    return;
+  }
   (void)get_plan(D);
-
-  /* z: real -> half complex */
 #pragma omp parallel
   {
     double* line = (double*)malloc(sizeof(double) * 2 * (size_t)D);
 #pragma omp for schedule(static)
-    for (long q = 0; q < (long)D * D; q++) {
+    for (long q = 0; q < rows; q++) {
       const float* src = in + (size_t)q * rstride;
       for (int z = 0; z < D; z++) {
         line[2 * z] = (double)src[z];
         line[2 * z + 1] = 0.0;
       }
       mxo_fft_1d(line, D, -1);
-      memcpy(w + 2 * (size_t)q * H, line, sizeof(double) * 2 * (size_t)H);
+      for (int k = 0; k < 2 * H; k++)
+        w[2 * (size_t)q * H + k] = (fft_real)line[k];
     }
     free(line);
   }
-  transform_axis(w, D, H, 1, -1); /* y */
-  transform_axis(w, D, H, 0, -1); /* x */
-  for (size_t i = 0; i < 2 * nc; i++)
-    out[i] = (float)w[i];
-  free(w);
 }
 
-void mxo_c2r_3d(int D, const float* in, float* out)
+/* z: half-complex rows of w -> real rows of out (padded, pitch 2H), with
+ * the Hermitian extension and the imaginary parts of kz = 0 and kz = D/2
+ * ignored (FFTW c2r semantics) */
+static void c2r_rows(int D, const fft_real* w, float* out)
 {
   const int H = D / 2 + 1;
-  const size_t nc = (size_t)D * D * H;
-  double* w = (double*)malloc(sizeof(double) * 2 * nc);
-  for (size_t i = 0; i < 2 * nc; i++)
-    w[i] = (double)in[i];
-
-  transform_axis(w, D, H, 0, +1); /* x */
-  transform_axis(w, D, H, 1, +1); /* y */
-  /* z: half complex -> real, Hermitian extension */
+  const long rows = (long)D * D;
+  if (is_pow2(D)) {
+    const p2_plan* P = get_p2(D);
+#pragma omp parallel
+    {
+      fft_real* buf = (fft_real*)malloc(sizeof(fft_real) * 4 * (size_t)D * FFT_BATCH);
+      fft_real* tmp = buf + 2 * (size_t)D * FFT_BATCH;
+#pragma omp for schedule(static)
+      for (long q0 = 0; q0 < rows; q0 += FFT_BATCH) {
+        const int B = rows - q0 < FFT_BATCH ? (int)(rows - q0) : FFT_BATCH;
+        for (int b = 0; b < B; b++) {
+          const fft_real* src = w + 2 * (size_t)(q0 + b) * H;
+          for (int k = 0; k < H; k++) {
+            buf[2 * ((size_t)k * B + b)] = src[2 * k];
+            buf[2 * ((size_t)k * B + b) + 1] = src[2 * k + 1];
+          }
+          buf[2 * (size_t)b + 1] = 0;
+          buf[2 * ((size_t)(D / 2) * B + b) + 1] = 0;
+          for (int k = H; k < D; k++) {
+            buf[2 * ((size_t)k * B + b)] = src[2 * (D - k)];
+            buf[2 * ((size_t)k * B + b) + 1] = -src[2 * (D - k) + 1];
+          }
+        }
+        p2_fft_batch(buf, tmp, B, +1, P);
+        for (int b = 0; b < B; b++) {
+          float* dst = out + (size_t)(q0 + b) * 2 * H;
+          for (int z = 0; z < D; z++)
+            dst[z] = (float)buf[2 * ((size_t)z * B + b)];
+          for (int z = D; z < 2 * H; z++)
+            dst[z] = 0.0f;
+        }
+      }
+      free(buf);
+    }
+    return;
+  }
+  (void)get_plan(D);
 #pragma omp parallel
   {
     double* line = (double*)malloc(sizeof(double) * 2 * (size_t)D);
 #pragma omp for schedule(static)
-    for (long q = 0; q < (long)D * D; q++) {
-      const double* src = w + 2 * (size_t)q * H;
+    for (long q = 0; q < rows; q++) {
+      const fft_real* src = w + 2 * (size_t)q * H;
       for (int k = 0; k < H; k++) {
         line[2 * k] = src[2 * k];
         line[2 * k + 1] = src[2 * k + 1];
@@ -235,6 +444,33 @@ void mxo_c2r_3d(int D, const float* in, float* out)
     }
     free(line);
   }
+}
+
+void mxo_r2c_3d(int D, const float* in, int in_padded, float* out)
+{
+  const int H = D / 2 + 1;
+  const size_t nc = (size_t)D * D * H;
+  fft_real* w = (fft_real*)malloc(sizeof(fft_real) * 2 * nc);
+  r2c_rows(D, in, in_padded ? 2 * H : D, w); /* z */
+  transform_axis(w, D, H, 1, -1);            /* y */
+  transform_axis(w, D, H, 0, -1);            /* x */
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)(2 * nc); i++)
+    out[i] = (float)w[i];
+  free(w);
+}
+
+void mxo_c2r_3d(int D, const float* in, float* out)
+{
+  const int H = D / 2 + 1;
+  const size_t nc = (size_t)D * D * H;
+  fft_real* w = (fft_real*)malloc(sizeof(fft_real) * 2 * nc);
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)(2 * nc); i++)
+    w[i] = (fft_real)in[i];
+  transform_axis(w, D, H, 0, +1); /* x */
+  transform_axis(w, D, H, 1, +1); /* y */
+  c2r_rows(D, w, out);            /* z */
   free(w);
 }
 

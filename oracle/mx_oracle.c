@@ -11,6 +11,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <omp.h>
+
 #include "mx_numerics.h"
 
 #ifndef M_PI
@@ -101,6 +103,16 @@ struct mxo_ctx
   double growth_zp, dgrowth_dzp, dt_dzp, const_zp_prefactor;
   double* freq_tables; /* [3][14][S] */
   float* margin;
+  /* grid buffers kept across calls, as the reference allocates its grids
+   * once (reionization.c malloc_reionization_grids) */
+  float* fhb_buf[10]; /* unfiltered and filtered spectra of the 5 fields */
+  float* ts_buf[2];
+  double* smoothed;
+  double* contrib;
+  int ts_shells;
+  /* CPU-timing sample (mxo_set_timing_sample) and phase times */
+  int sample_radii, sample_shells, sample_cell_div;
+  double phase[MXO_N_PHASES];
 };
 
 /* ======================================================= cosmology helpers */
@@ -165,6 +177,7 @@ static void c_filter(const mxo_ctx* c, float* box, int D, float R, int filter_ty
   const int H = D / 2 + 1;
   const float box_size = (float)c->p.box_size;
   const float delta_k = (float)(2.0 * M_PI / box_size);
+#pragma omp parallel for schedule(static)
   for (int n_x = 0; n_x < D; n_x++) {
     const float k_x = (n_x > middle) ? (n_x - D) * delta_k : n_x * delta_k;
     for (int n_y = 0; n_y < D; n_y++) {
@@ -529,7 +542,22 @@ void mxo_destroy(mxo_ctx* c)
   free(c->sum_lyn);
   free(c->freq_tables);
   free(c->margin);
+  for (int i = 0; i < 10; i++)
+    free(c->fhb_buf[i]);
+  free(c->ts_buf[0]);
+  free(c->ts_buf[1]);
+  free(c->smoothed);
+  free(c->contrib);
   free(c);
+}
+
+/* A buffer of the context, allocated on first use (the grid size of a
+ * context is fixed). */
+static void* ctx_buf(void** slot, size_t bytes)
+{
+  if (!*slot)
+    *slot = malloc(bytes);
+  return *slot;
 }
 
 /* set_sfr_history, ComputeTs.c:32-76 */
@@ -575,6 +603,13 @@ int mxo_set_redshifts(mxo_ctx* c, const double* zz, int n_snaps)
 
 int mxo_n_sfr_histories(const mxo_ctx* c) { return c->n_hist; }
 const float* mxo_last_margin(const mxo_ctx* c) { return c->margin; }
+void mxo_set_timing_sample(mxo_ctx* c, int max_radii, int max_shells, int cell_div)
+{
+  c->sample_radii = max_radii > 0 ? max_radii : 0;
+  c->sample_shells = max_shells > 0 ? max_shells : 0;
+  c->sample_cell_div = cell_div > 1 ? cell_div : 0;
+}
+const double* mxo_phase_times(const mxo_ctx* c) { return c->phase; }
 double mxo_dtdz(const mxo_ctx* c, float z) { return c_dtdz(c, z); }
 double mxo_recombination_rate_splined(mxo_ctx* c, double z_eff, double gamma12)
 {
@@ -625,8 +660,8 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
     g->xH[i] = 1.0f;
     g->r_bubble[i] = 0.0f;
   }
-  free(c->margin);
-  c->margin = (float*)malloc(sizeof(float) * 2 * nreal);
+  c->margin = (float*)ctx_buf((void**)&c->margin, sizeof(float) * 2 * nreal);
+#pragma omp parallel for schedule(static)
   for (size_t i = 0; i < 2 * nreal; i++)
     c->margin[i] = INFINITY;
 
@@ -636,13 +671,15 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
                             recomb ? g->N_rec : NULL };
   float* unf[F_N] = { 0 };
   float* fil[F_N] = { 0 };
+  double tp = omp_get_wtime();
   for (int f = 0; f < F_N; f++) {
     if (!src[f])
       continue;
-    unf[f] = (float*)malloc(sizeof(float) * 2 * nc);
-    fil[f] = (float*)malloc(sizeof(float) * 2 * nc);
+    unf[f] = (float*)ctx_buf((void**)&c->fhb_buf[2 * f], sizeof(float) * 2 * nc);
+    fil[f] = (float*)ctx_buf((void**)&c->fhb_buf[2 * f + 1], sizeof(float) * 2 * nc);
     mxo_r2c_3d(D, src[f], 1, unf[f]);
     /* ×1/N: float complex /= double (find_HII_bubbles.c:168-182) */
+#pragma omp parallel for schedule(static)
     for (size_t i = 0; i < 2 * nc; i++)
       unf[f][i] = (float)((double)unf[f][i] / total_n_cells);
   }
@@ -651,7 +688,12 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
   double R = fmin(Rmax, K_L_FACTOR * box_size);
   int last = 0;
   int n_radii = 0;
+  c->phase[MXO_PH_FORWARD] = omp_get_wtime() - tp;
+  double t_radii = 0.0;
   while (!last) {
+    tp = omp_get_wtime();
+    if (c->sample_radii > 0 && n_radii == c->sample_radii)
+      break; /* timing sample: the first sample_radii radii only */
     if (((R / p->delta_r_factor) <= (cell_length_factor * box_size / (double)D)) ||
         ((R / p->delta_r_factor) <= p->r_bubble_min)) {
       last = 1;
@@ -667,6 +709,7 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
       mxo_c2r_3d(D, fil[f], fil[f]);
     }
     /* aliasing clamps, find_HII_bubbles.c:271-311 */
+#pragma omp parallel for schedule(static)
     for (int ix = 0; ix < D; ix++)
       for (int iy = 0; iy < D; iy++)
         for (int iz = 0; iz < D; iz++) {
@@ -745,9 +788,30 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
           }
         }
     R /= p->delta_r_factor;
+    if (n_radii > 1) /* the first radius also first touches the buffers */
+      t_radii += omp_get_wtime() - tp;
   }
 
-  /* global means + N_rec, find_HII_bubbles.c:451-494 */
+  c->phase[MXO_PH_RADII] = t_radii;
+  c->phase[MXO_PH_N_RADII] = n_radii > 1 ? n_radii - 1 : 0;
+  c->phase[MXO_PH_N_RADII_RUN] = n_radii;
+  tp = omp_get_wtime();
+  /* global means + N_rec, find_HII_bubbles.c:451-494: the N_rec update of
+   * each cell in parallel, the sums in the reference's cell order */
+  if (recomb) {
+#pragma omp parallel for schedule(static)
+    for (int ix = 0; ix < D; ix++)
+      for (int iy = 0; iy < D; iy++)
+        for (int iz = 0; iz < D; iz++) {
+          const size_t ir = real_idx(D, ix, iy, iz);
+          const size_t ip = pad_idx(D, ix, iy, iz);
+          const double cell_xH = (double)g->xH[ir];
+          const double dom = 1.0 + (double)g->deltax[ip];
+          const float z_eff = (float)((1. + redshift) * pow(dom, 1.0 / 3.0) - 1);
+          const double dNrec = c_rr_splined(c, z_eff, g->Gamma12[ir]) * fabs_dtdz * zstep * (1. - cell_xH);
+          g->N_rec[ip] += dNrec;
+        }
+  }
   double vol_xH = 0.0, mass_xH = 0.0, mass_weight = 0.0, vol_J21 = 0.0;
   for (int ix = 0; ix < D; ix++)
     for (int iy = 0; iy < D; iy++)
@@ -761,20 +825,12 @@ int mxo_find_HII_bubbles(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals
         const double dom = 1.0 + (double)g->deltax[ip];
         mass_xH += cell_xH * dom;
         mass_weight += dom;
-        if (recomb) {
-          const float z_eff = (float)((1. + redshift) * pow(dom, 1.0 / 3.0) - 1);
-          const double dNrec = c_rr_splined(c, z_eff, g->Gamma12[ir]) * fabs_dtdz * zstep * (1. - cell_xH);
-          g->N_rec[ip] += dNrec;
-        }
       }
   vol_xH /= total_n_cells;
   if (uvb)
     vol_J21 /= total_n_cells;
   mass_xH /= mass_weight;
-  for (int f = 0; f < F_N; f++) {
-    free(unf[f]);
-    free(fil[f]);
-  }
+  c->phase[MXO_PH_FHB_POST] = omp_get_wtime() - tp;
   if (out) {
     out->volume_weighted_global_xH = vol_xH;
     out->volume_weighted_global_J_21 = vol_J21;
@@ -1286,12 +1342,19 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
     const double R_factor = pow(K_R_XLY_MAX / R, 1 / (float)S);
     double* R_values = (double*)malloc(sizeof(double) * (size_t)S);
     int* scb = (int*)malloc(sizeof(int) * (size_t)S);
-    double* smoothed = (double*)malloc(sizeof(double) * (size_t)S * D * D * D);
-    float* unf = (float*)malloc(sizeof(float) * 2 * nc);
-    float* fil = (float*)malloc(sizeof(float) * 2 * nc);
+    if (c->smoothed && c->ts_buf[0] && S > c->ts_shells) {
+      free(c->smoothed);
+      c->smoothed = NULL;
+    }
+    double* smoothed = (double*)ctx_buf((void**)&c->smoothed, sizeof(double) * (size_t)S * D * D * D);
+    c->ts_shells = S;
+    float* unf = (float*)ctx_buf((void**)&c->ts_buf[0], sizeof(float) * 2 * nc);
+    float* fil = (float*)ctx_buf((void**)&c->ts_buf[1], sizeof(float) * 2 * nc);
     const double* ZZ = c->zz;
     double weight = 1;
     scb[0] = 1;
+    double tp = omp_get_wtime(), t_shells = 0.0, t_copies = 0.0;
+    int n_shells_done = 0;
     for (int R_ct = 0; R_ct < S; R_ct++) {
       double prev_zpp, prev_R;
       R_values[R_ct] = R;
@@ -1356,8 +1419,25 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
         }
       }
 
+      if (c->sample_shells > 0 && R_ct >= c->sample_shells) {
+        /* timing sample: this shell repeats a smoothed one (the per-cell
+         * work below still reads every shell) */
+        const int from = R_ct % c->sample_shells;
+        const double t0 = omp_get_wtime();
+        /* only the cells that the sampled per-cell step reads */
+        const size_t n_read = (size_t)(c->sample_cell_div > 1 ? D / c->sample_cell_div : D) * D * D;
+#pragma omp parallel for schedule(static)
+        for (size_t ir = 0; ir < n_read; ir++)
+          smoothed[(size_t)R_ct + (size_t)S * ir] = smoothed[(size_t)from + (size_t)S * ir];
+        t_copies += omp_get_wtime() - t0;
+        R *= R_factor;
+        continue;
+      }
+      n_shells_done++;
+      const double t_shell0 = omp_get_wtime();
       /* R2C, ×1/N (float division), filter, C2R: ComputeTs.c:379-409 */
       mxo_r2c_3d(D, g->sfr, 1, unf);
+#pragma omp parallel for schedule(static)
       for (size_t i = 0; i < 2 * nc; i++)
         unf[i] = unf[i] / (float)total_n_cells;
       memcpy(fil, unf, sizeof(float) * 2 * nc);
@@ -1375,11 +1455,11 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
             fil[ip] = fmaxf(fil[ip], 0.0);
             smoothed[(size_t)R_ct + (size_t)S * ir] = ((fil[ip] / pixel_volume) * sfr_unit);
           }
-      for (int ix = 0; ix < D; ix++)
-        for (int iy = 0; iy < D; iy++)
-          for (int iz = 0; iz < D; iz++) {
-            const size_t ip = pad_idx(D, ix, iy, iz);
-            if (R_ct == 0) {
+      if (R_ct == 0)
+        for (int ix = 0; ix < D; ix++)
+          for (int iy = 0; iy < D; iy++)
+            for (int iz = 0; iz < D; iz++) {
+              const size_t ip = pad_idx(D, ix, iy, iz);
               const double dom = 1.0 + g->deltax[ip];
               double cf = g->stars[ip] / (c_RtoM(c, R) * p->hubble_h * p->hubble_h * dom) * (4.0 / 3.0) * M_PI *
                           pow(R, 3.0) / pixel_volume;
@@ -1388,15 +1468,22 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
               collapse_fraction += cf;
               c->x_e_ave += g->x_e_box_prev[ip];
             }
-          }
       if (R_ct == 0) {
         collapse_fraction = collapse_fraction / total_n_cells;
         c->x_e_ave = c->x_e_ave / total_n_cells;
         c->stored_fcoll[snapshot] = collapse_fraction;
+      } else { /* shell 0 also first touches the buffers */
+        t_shells += omp_get_wtime() - t_shell0;
       }
       R *= R_factor;
     }
     const int NO_LIGHT = (collapse_fraction > 0.0) ? 0 : 1;
+    c->phase[MXO_PH_SHELLS] = t_shells;
+    c->phase[MXO_PH_N_SHELLS] = n_shells_done > 1 ? n_shells_done - 1 : 0;
+    c->phase[MXO_PH_N_SHELLS_RUN] = n_shells_done;
+    c->phase[MXO_PH_SHELL_COPIES] = t_copies;
+    (void)tp;
+    tp = omp_get_wtime();
 
     /* frequency-integral tables and Ly-n sums, ComputeTs.c:517-663 */
     int first_radii = 1, first_zero = 1;
@@ -1460,6 +1547,8 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
       }
     }
 
+    c->phase[MXO_PH_TABLES] = omp_get_wtime() - tp;
+    tp = omp_get_wtime();
     c->growth_zp = c_dicke(c, zp);
     c->dgrowth_dzp = c_ddicke_dz(c, zp);
     c->dt_dzp = c_dtdz(c, (float)zp);
@@ -1479,7 +1568,9 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
 
     /* per-cell evolution, ComputeTs.c:743-900: cells in parallel, the
      * volume averages summed afterwards in the reference's cell order */
-    double* contrib = (double*)malloc(sizeof(double) * 4 * (size_t)D * D * D);
+    double* contrib = (double*)ctx_buf((void**)&c->contrib, sizeof(double) * 4 * (size_t)D * D * D);
+    /* timing sample: the first D / sample_cell_div x planes only */
+    const int nx_cells = c->sample_cell_div > 1 ? D / c->sample_cell_div : D;
 #pragma omp parallel
     {
     double* SFR = (double*)malloc(sizeof(double) * (size_t)S);
@@ -1487,7 +1578,7 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
     double* fi = (double*)malloc(sizeof(double) * (size_t)S);
     double* fl = (double*)malloc(sizeof(double) * (size_t)S);
 #pragma omp for schedule(static)
-    for (int ix = 0; ix < D; ix++)
+    for (int ix = 0; ix < nx_cells; ix++)
       for (int iy = 0; iy < D; iy++)
         for (int iz = 0; iz < D; iz++) {
           const size_t ir = real_idx(D, ix, iy, iz);
@@ -1535,19 +1626,19 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
     free(fi);
     free(fl);
     }
+    c->phase[MXO_PH_EVOLVE] = omp_get_wtime() - tp;
+    c->phase[MXO_PH_EVOLVE_FRAC] = (double)nx_cells / (double)D;
     for (size_t ir = 0; ir < (size_t)D * D * D; ir++) {
       J_alpha_ave += contrib[4 * ir + 0];
       xalpha_ave += contrib[4 * ir + 1];
       Xheat_ave += contrib[4 * ir + 2];
       Xion_ave += contrib[4 * ir + 3];
     }
-    free(contrib);
+
     i_padded = pad_idx(D, D - 1, D - 1, D - 1); /* last cell visited */
     free(R_values);
     free(scb);
-    free(smoothed);
-    free(unf);
-    free(fil);
+
     J_alpha_ave /= total_n_cells;
     xalpha_ave /= total_n_cells;
     Xheat_ave /= total_n_cells;
@@ -1555,6 +1646,7 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
   }
 
   /* ComputeTs.c:940-974 */
+  const double tpost = omp_get_wtime();
   memcpy(g->x_e_box, g->x_e_box_prev, sizeof(float) * 2 * nc);
   double Ave_Ts = 0.0, Ave_x_e = 0.0, Ave_Tk = 0.0;
   for (int ix = 0; ix < D; ix++)
@@ -1568,6 +1660,7 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
   Ave_Ts /= total_n_cells;
   Ave_Tk /= total_n_cells;
   Ave_x_e /= total_n_cells;
+  c->phase[MXO_PH_TS_POST] = omp_get_wtime() - tpost;
   if (out) {
     if ((zp - p->max_heating_redshift) < -0.0001) {
       out->volume_ave_J_alpha = J_alpha_ave;

@@ -55,6 +55,34 @@ int mxo_ps_length(int D, double box_size_mpc_h, double hubble_h);
 int mxo_power_spectrum(int D, double box_size_mpc_h, double hubble_h, const float* delta_T, float* ps_k, float* ps_data,
                        float* ps_error, int cap);
 const float* mxo_last_margin(const mxo_ctx* c);
+
+/* CPU timing of the benchmark (not used by the parity tests).  A timing
+ * sample bounds the work of one call: find_HII_bubbles stops after its first
+ * max_radii radii, ComputeTs smooths only its first max_shells shells (the
+ * others repeat them, so the per-cell step still reads every shell) and
+ * evolves only the first D / cell_div x planes.  The grids such a call leaves
+ * are not the step's results.  0 (or 1 for cell_div) switches a limit off.
+ * mxo_phase_times returns the wall seconds of the phases of the last calls,
+ * indexed by MXO_PH_*, so that the sampled parts can be scaled to the full
+ * counts.  The first radius and the first shell also touch freshly
+ * allocated buffers for the first time and are left out of the per-radius and
+ * per-shell times. */
+#define MXO_PH_FORWARD 0       /* find_HII_bubbles: forward transforms + 1/N */
+#define MXO_PH_RADII 1         /* the radius loop after its first radius */
+#define MXO_PH_N_RADII 2       /* radii in MXO_PH_RADII */
+#define MXO_PH_FHB_POST 3      /* global means and N_rec */
+#define MXO_PH_SHELLS 4        /* ComputeTs: SFR reweighting + smoothing of the shells after the first */
+#define MXO_PH_N_SHELLS 5      /* shells in MXO_PH_SHELLS */
+#define MXO_PH_TABLES 6        /* frequency-integral tables and Ly-n sums */
+#define MXO_PH_EVOLVE 7        /* per-cell evolution */
+#define MXO_PH_EVOLVE_FRAC 8   /* fraction of the cells evolved */
+#define MXO_PH_TS_POST 9       /* means */
+#define MXO_PH_N_RADII_RUN 10  /* radii run (all of them without a sample) */
+#define MXO_PH_N_SHELLS_RUN 11 /* shells smoothed */
+#define MXO_PH_SHELL_COPIES 12 /* the repeated shells of a sample */
+#define MXO_N_PHASES 13
+void mxo_set_timing_sample(mxo_ctx* c, int max_radii, int max_shells, int cell_div);
+const double* mxo_phase_times(const mxo_ctx* c);
 /* dv/dx (padded layout) of the last delta_T with peculiar velocities, or NULL. */
 const float* mxo_last_velocity_gradient(const mxo_ctx* c);
 

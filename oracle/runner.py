@@ -12,14 +12,18 @@ from meraxes_gb300.params import GRID_NAMES, MxGlobals, MxGrids, ReionParams
 
 ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libmxoracle.so")
+# single-precision transforms (the reference's fftwf precision), for CPU timing
+TIMING_LIB = os.path.join(ORACLE_DIR, "_build", "libmxoracle_f32.so")
 REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libmxref.so")
 REF_SRC = os.environ.get("MX_REFERENCE_SRC", "/root/reference/src")
 
 
-def build_oracle(force: bool = False) -> str:
-    if force or not os.path.exists(ORACLE_LIB) or _stale(ORACLE_LIB, ["mx_oracle.c", "mx_numerics.c", "mx_oracle.h"]):
-        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "oracle"], check=True)
-    return ORACLE_LIB
+def build_oracle(force: bool = False, timing: bool = False) -> str:
+    lib, target = (TIMING_LIB, "timing") if timing else (ORACLE_LIB, "oracle")
+    if force or not os.path.exists(lib) or _stale(lib, ["mx_oracle.c", "mx_numerics.c", "mx_oracle.h",
+                                                        "mx_numerics.h"]):
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, target], check=True)
+    return lib
 
 
 def ref_available() -> bool:
@@ -48,8 +52,8 @@ class OracleBackend:
 
     kind = "port"
 
-    def __init__(self, params: ReionParams, redshifts, tables_dir: str):
-        self.lib = ctypes.CDLL(build_oracle())
+    def __init__(self, params: ReionParams, redshifts, tables_dir: str, timing: bool = False):
+        self.lib = ctypes.CDLL(build_oracle(timing=timing))
         L = self.lib
         L.mxo_create.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
         L.mxo_destroy.argtypes = [ctypes.c_void_p]
@@ -76,6 +80,9 @@ class OracleBackend:
         L.mxo_last_velocity_gradient.restype = ctypes.POINTER(ctypes.c_float)
         L.mxo_power_spectrum.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.mxo_set_timing_sample.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.mxo_phase_times.argtypes = [ctypes.c_void_p]
+        L.mxo_phase_times.restype = ctypes.POINTER(ctypes.c_double)
         self.params = params
         self._pc = params.to_ctypes()
         self.ctx = ctypes.c_void_p()
@@ -170,6 +177,18 @@ class OracleBackend:
         n = self.lib.mxo_power_spectrum(p.grid_dim, p.box_size, p.hubble_h, _ptr(d), *(_ptr(a) for a in out), 64)
         assert n > 0
         return tuple(a[:n].copy() for a in out)
+
+    PHASES = ("forward", "radii", "n_radii", "fhb_post", "shells", "n_shells", "tables", "evolve", "evolve_frac",
+              "ts_post", "n_radii_run", "n_shells_run", "shell_copies")
+
+    def set_timing_sample(self, max_radii: int = 0, max_shells: int = 0, cell_div: int = 1):
+        """Bounds the work of the next calls for CPU timing (their grids are
+        then not the step's results); zeros switch the limits off."""
+        self.lib.mxo_set_timing_sample(self.ctx, max_radii, max_shells, cell_div)
+
+    def phase_times(self) -> Dict[str, float]:
+        p = self.lib.mxo_phase_times(self.ctx)
+        return {n: float(p[i]) for i, n in enumerate(self.PHASES)}
 
     def margin(self) -> np.ndarray:
         """[2, D, D, D]: first-crossing margin and all-radii margin."""

@@ -15,6 +15,10 @@ Tolerances, from the acceptance rule of the step:
     of first crossing (J_21, Gamma12, N_rec) are compared where that radius
     agrees.  N_rec, which is updated from Gamma12 through the recombination
     rate table, also passes on Gamma12's relative difference at the cell.
+
+The report gives, per grid, the largest relative difference, the cells
+outside tolerance and, as `<grid>_floor_only`, the cells that are inside it
+only through the absolute FFT floor (outside the relative rule alone).
 """
 from __future__ import annotations
 
@@ -111,6 +115,7 @@ def compare(ref: Dict[str, np.ndarray], test: Dict[str, np.ndarray], ref_globals
         scale = max(float(np.abs(a).max()), 1e-300)
         if k == "xH":
             bad = np.abs(a - b) > XH_ATOL + floor
+            rep[k + "_floor_only"] = int((sel & ~bad & (np.abs(a - b) > XH_ATOL)).sum())
         elif k == "z_at_ionization":
             bad = a != b
         else:
@@ -123,6 +128,8 @@ def compare(ref: Dict[str, np.ndarray], test: Dict[str, np.ndarray], ref_globals
                 gb = _real(test["Gamma12"], D).astype(np.float64)
                 tol = tol + np.abs(a) * np.abs(ga - gb) / np.maximum(np.abs(ga), 1e-300)
             bad = np.abs(a - b) > tol
+            # cells inside the tolerance only through the FFT floor
+            rep[k + "_floor_only"] = int((sel & ~bad & (np.abs(a - b) > tol - floor * scale)).sum())
         bad &= sel
         err = np.abs(a - b)[sel] / np.maximum(np.abs(a[sel]), floor * scale)
         rep[k] = float(err.max()) if err.size else 0.0
