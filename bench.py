@@ -68,7 +68,7 @@ def parse_args(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--grid", type=int, default=512)
-    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
@@ -397,7 +397,7 @@ def run_gb300(args, rank, world, local):
     # ------------------------------------------------------------------ e2e
     e2e = None
     if not args.no_e2e and args.e2e_steps > 0:
-        e2e = run_e2e(args, step, w, fields, used, n_hist, device, world)
+        e2e = run_e2e(args, step, w, fields, hist, smax, timed, n_hist, device, world)
     block_sizes = list(step.fft_block_sizes())
     step.close()
     plain = None
@@ -556,26 +556,29 @@ def run_batch_native():
             "first_run_s_with_context_creation": round(first, 3)}
 
 
-def run_e2e(args, step, w, fields, used, n_hist, device, world):
-    """Same metric through mx_step with pinned host buffers: every step copies
-    that step's inputs and state host->device and all outputs back."""
+def run_e2e(args, step, w, fields, hist, smax, timed, n_hist, device, world):
+    """Same metric through the host-pointer entry points, on the same
+    evolution as `value`: the timed snapshots from the initial state, every
+    snapshot's inputs, state and SFR-history slices in pinned host buffers.
+    Each timed call copies its inputs host->device and all outputs back;
+    filling the pinned buffers with the next snapshot's inputs is not timed.
+    Two legs: mx_step (one call per snapshot), and the reference's three
+    entry points called one after another as the C adapter calls them
+    (mx_ComputeTs, mx_find_HII_bubbles, mx_ComputeBrightnessTemperatureBox,
+    each copying the grids it reads and writes)."""
     import torch
-
-    from meraxes_gb300.params import PADDED_GRIDS
 
     p = w.params
     D = p.grid_dim
-    s = used[-1]
-    host = {}
-    for k, v in fields[s].items():
-        host[k] = v.cpu().pin_memory().numpy()
-    st = state_grids(p, w.redshifts[max(s - 1, 0)], "cpu")
-    for k, v in st.items():
+    snaps = timed[: max(1, min(args.e2e_steps, len(timed)))]
+    host = {k: v.cpu().pin_memory().numpy() for k, v in fields[snaps[0]].items()}
+    st0 = state_grids(p, w.redshifts[0], "cpu")
+    for k, v in st0.items():
         host[k] = v.pin_memory().numpy()
+    hbuf = None
     if n_hist > 0:
-        h = torch.zeros((n_hist, D * D * 2 * (D // 2 + 1)), dtype=torch.float32).pin_memory()
-        h[0] = fields[s]["sfr"].reshape(-1).cpu()
-        host["sfr_histories"] = h.numpy()
+        hbuf = torch.zeros((n_hist, D * D * 2 * (D // 2 + 1)), dtype=torch.float32).pin_memory()
+        host["sfr_histories"] = hbuf.numpy()
     # mx_step uploads each input once; x_e_box is not uploaded when ComputeTs
     # runs (it writes x_e_box on the device before find_HII_bubbles reads it)
     in_names = ["deltax", "stars", "weighted_sfr", "N_rec", "z_at_ionization", "J_21_at_ionization",
@@ -587,30 +590,45 @@ def run_e2e(args, step, w, fields, used, n_hist, device, world):
     nb = lambda n: host[n].nbytes  # noqa: E731
     h2d = sum(nb(n) for n in in_names if n in host) + (host["sfr_histories"].nbytes if n_hist > 0 else 0)
     d2h = sum(nb(n) for n in out_names if n in host)
-    step.step(s, host)  # first host call allocates the device mirror
-    torch.cuda.synchronize()
-    barrier(world)
-    t = 0.0
-    for _ in range(args.e2e_steps):
-        t0 = time.perf_counter()
-        step.step(s, host)
-        t += time.perf_counter() - t0
-    # the drop-in adapter's path: the reference's three entry points called
-    # one after another (ComputeTs, find_HII_bubbles, the 21cm box), each
-    # copying the grids it reads to the device and the grids it writes back
-    step.ComputeTs(s, host)
-    torch.cuda.synchronize()
-    t3 = 0.0
-    for _ in range(args.e2e_steps):
-        t0 = time.perf_counter()
+
+    def prepare(s):
+        for k, v in fields[s].items():
+            torch.from_numpy(host[k]).copy_(v.reshape(host[k].shape))
+        if hbuf is not None:
+            hbuf.copy_(hist[smax - s: smax - s + n_hist])
+        torch.cuda.synchronize()
+
+    def reset_state():
+        for k, v in st0.items():
+            np.copyto(host[k], v.numpy())
+
+    def leg(call):
+        reset_state()
+        prepare(snaps[0])
+        call(snaps[0])  # first host calls allocate the device mirror
+        reset_state()
+        torch.cuda.synchronize()
+        barrier(world)
+        t = 0.0
+        for s in snaps:
+            if s == 0:
+                reset_state()
+            prepare(s)
+            t0 = time.perf_counter()
+            call(s)
+            t += time.perf_counter() - t0
+        return replica_value(t * 1e3, len(snaps), world, device)
+
+    def three(s):
         step.ComputeTs(s, host)
         step.find_HII_bubbles(s, host)
         step.ComputeBrightnessTemperatureBox(s, host)
-        t3 += time.perf_counter() - t0
-    return {"value": round(replica_value(t * 1e3, args.e2e_steps, world, device), 3), "unit": UNIT,
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
-            "entry_point": "mx_step (host pointers)",
-            "three_calls": {"value": round(replica_value(t3 * 1e3, args.e2e_steps, world, device), 3), "unit": UNIT,
+
+    v1 = leg(lambda s: step.step(s, host))
+    v3 = leg(three)
+    return {"value": round(v1, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "steps": len(snaps), "snapshots": snaps, "entry_point": "mx_step (host pointers)",
+            "three_calls": {"value": round(v3, 3), "unit": UNIT,
                             "entry_points": "mx_ComputeTs, mx_find_HII_bubbles, "
                                             "mx_ComputeBrightnessTemperatureBox (host pointers, as the C "
                                             "adapter calls them)"}}
@@ -631,6 +649,8 @@ def run_e2e(args, step, w, fields, used, n_hist, device, world):
 # calls, as the reference allocates its grids once, so the first snapshot of
 # a process also pays the first touch of those buffers and is not timed.
 CPU_SAMPLE = {"radii": 3, "shells": 3, "cell_div": 16}
+# per step of the reference arm, which runs W + K sampled snapshots
+REF_SAMPLE = {"radii": 2, "shells": 2, "cell_div": 64}
 
 
 def cpu_run(grid: int, threads: int, radii: int, shells: int, cell_div: int, runs: int) -> dict:
@@ -720,12 +740,12 @@ def run_reference(args, rank, world):
     """The CPU implementation of the path on all host threads: the oracle
     port (the reference's own build needs FFTW/GSL/MPI/HDF5 and the reference
     tree, absent on the GPU host), each step one sampled snapshot at the
-    benchmark's grid size (CPU_SAMPLE), after W warm-up snapshots."""
+    benchmark's grid size (REF_SAMPLE), after W warm-up snapshots."""
     if rank != 0:
         return None, rank
     threads = os.cpu_count() or 1
     try:
-        res = cpu_runs(args.grid, threads, max(args.warmup, 1) + args.steps)
+        res = cpu_runs(args.grid, threads, max(args.warmup, 1) + args.steps, sample=REF_SAMPLE)
     except Exception as e:  # noqa: BLE001
         return {"impl": "reference", "unavailable": "oracle port failed: " + str(e)[-300:]}, rank
     timed = res["runs"][max(args.warmup, 1):]

@@ -244,6 +244,11 @@ struct Pitch
 template <int D>
 struct Split3;
 template <>
+struct Split3<16>
+{
+  static constexpr int R1 = 4, R2 = 2, R3 = 2;
+};
+template <>
 struct Split3<32>
 {
   static constexpr int R1 = 4, R2 = 4, R3 = 2;
@@ -411,7 +416,7 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
 // block computes the filter weights of its tile for its radius (shared by all
 // fields and by the rows ky and D - ky, which have the same |k|), then for
 // each of the two rows and every field loads the unfiltered columns (rows of
-// H), scales by 1/N, multiplies by W(|k| R), inverse-DFTs along x and stores
+// HP, the forward transform's layout; columns past H are not read), scales by 1/N, multiplies by W(|k| R), inverse-DFTs along x and stores
 // to out[(r*G + g) * C + (x*D + ky)*HP + kz], all HP columns (those past H
 // are zero in, zero out).
 //
@@ -421,7 +426,7 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
 // at 512^3 took 8.75 ms with tables, 5.90 ms without).
 // XTHREADS threads per block: 256 or 512 (the context's autotuner picks).
 template <int D, int XTHREADS>
-__global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) k_fft_x_filter(XPassArgs a)
+__global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) k_fft_x_filter(const __grid_constant__ XPassArgs a)
 {
   using P = TilePlan<D>;
   constexpr int H = D / 2 + 1;
@@ -443,9 +448,9 @@ __global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) 
   using T = TileSteps<D, XTHREADS>;
   float2 pts[T::NPTS];
   auto read_points = [&](int ky, int g) {
-    const float2* __restrict__ src = a.in[g] + (long long)ky * H + kz0 + t0;
+    const float2* __restrict__ src = a.in[g] + (long long)ky * Pitch<D>::HP + kz0 + t0;
     T::for_each_input([&](int kx, int i) {
-      pts[i] = live ? src[(long long)kx * (D * H)] : make_float2(0.f, 0.f);
+      pts[i] = live ? src[(long long)kx * (D * Pitch<D>::HP)] : make_float2(0.f, 0.f);
     });
   };
   // filter weights of the tile, wsm[|kx| * TXC + t] for |kx| = min(kx, D -
@@ -1081,6 +1086,115 @@ __global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_store(const float2* sp
   }
 }
 
+
+// ------------------------------------------------------- forward transform
+// Forward R2C of G padded real grids (the FFTW r2c of find_HII_bubbles.c:
+// 118-163 and ComputeTs.c:379-389: unnormalised, exp(-2 pi i jk / n)) in
+// three passes, written as spectra [kx][ky][kz] with rows of HP complex
+// values (kz >= D/2 + 1 zero), the layout the x-pass reads:
+//
+//   z-pass   16 rows of a grid per block, read with coalesced loads into
+//            shared memory; each row's D real points as D/2 complex points
+//            z_m = x_2m + i x_2m+1, transformed by the tile engine (forward
+//            as conj(backward(conj))), then X_k = E_k + w_D^-k O_k with
+//            E_k = (Z_k + conj Z_{D/2-k}) / 2 and O_k = (Z_k - conj Z_{D/2-k}) / 2i;
+//   y-pass, x-pass   forward DFT along y, then x, in place (tiles of 16 kz
+//            columns, as the inverse y-pass).
+namespace {
+constexpr int FWD_ROWS = TXC;  // rows per z-pass block, one per tile column
+}
+
+template <int D>
+struct FwdZPlan
+{
+  static constexpr int L = D / 2, H = D / 2 + 1, HP = Pitch<D>::HP;
+  // shared memory (float2): twiddles of the L-point engine, w_D^-k for
+  // k <= D/2, the engine's tile, and the 16 rows (H float2 each: the padded
+  // input row, later the row's Z_k); a row pitch of H = 1 mod 16 float2 puts
+  // the 16 rows of a column access on distinct banks
+  static constexpr int OFF_TW = 0, OFF_POST = L, OFF_TILE = OFF_POST + H, OFF_ROWS = OFF_TILE + L * TXC;
+  static constexpr size_t BYTES = sizeof(float2) * (size_t)(OFF_ROWS + FWD_ROWS * H);
+};
+
+template <int D>
+__global__ void __launch_bounds__(FFT_THREADS) k_fft_z_r2c(const __grid_constant__ FwdArgs a)
+{
+  using P = FwdZPlan<D>;
+  constexpr int L = P::L, H = P::H, HP = P::HP;
+  extern __shared__ float2 smem[];
+  float2* tw = smem + P::OFF_TW;
+  float2* post = smem + P::OFF_POST;
+  float2* tile = smem + P::OFF_TILE;
+  float2* rows = smem + P::OFF_ROWS;
+  constexpr long long GROUPS = (long long)D * D / FWD_ROWS;
+  const int g = (int)(blockIdx.x / GROUPS);
+  const long long r0 = (blockIdx.x % GROUPS) * FWD_ROWS;
+  // the 16 padded rows are contiguous: FWD_ROWS * H float2
+  const float2* __restrict__ src = reinterpret_cast<const float2*>(a.src[g]) + r0 * H;
+  for (int i = threadIdx.x; i < FWD_ROWS * H; i += FFT_THREADS)
+    rows[i] = __ldg(src + i);
+  fill_twiddles<L>(tw);
+  for (int k = threadIdx.x; k < H; k += FFT_THREADS) {
+    float sn, cs;
+    sincospif(2.0f * (float)k / (float)D, &sn, &cs);
+    post[k] = make_float2(cs, -sn);
+  }
+  __syncthreads();
+  // forward DFT of each row's L points: conj in, backward engine, conj out
+  tile_dft<L, FFT_THREADS>(
+    tile, tw,
+    [&](int n, int t, int) {
+      const float2 v = rows[t * H + n];
+      return make_float2(v.x, -v.y);
+    },
+    [&](int k, int t, float2 v) { rows[t * H + k] = make_float2(v.x, -v.y); });
+  __syncthreads();
+  float2* __restrict__ dst = a.out + (long long)g * a.C + r0 * HP;
+  for (int i = threadIdx.x; i < FWD_ROWS * HP; i += FFT_THREADS) {
+    const int t = i / HP, k = i - t * HP;
+    float2 X = make_float2(0.f, 0.f);
+    if (k < H) {
+      const float2 zk = rows[t * H + (k < L ? k : 0)];
+      const float2 zm = rows[t * H + (k > 0 ? L - k : 0)];
+      const float2 A = make_float2(zk.x + zm.x, zk.y - zm.y);  // Z_k + conj Z_{L-k}
+      const float2 B = make_float2(zk.x - zm.x, zk.y + zm.y);  // Z_k - conj Z_{L-k}
+      const float2 C = cmul(B, post[k]);                       // w_D^-k B
+      X = make_float2(0.5f * (A.x + C.y), 0.5f * (A.y - C.x)); // (A - i C) / 2
+    }
+    dst[i] = X;
+  }
+}
+
+// Forward DFT along y (AXIS 1) or x (AXIS 0) of n spectra [D][D][HP], in
+// place, tiles of 16 kz columns; the inverse y-pass's engine with conjugated
+// input and output.
+template <int D, int T, int AXIS>
+__global__ void __launch_bounds__(T, T == 256 ? 3 : 2) k_fft_fwd_cols(float2* data, long long C, int n_spectra)
+{
+  using P = TilePlan<D>;
+  constexpr int HP = Pitch<D>::HP;
+  constexpr long long LINE = AXIS == 1 ? HP : (long long)D * HP;   // between the points of a column
+  constexpr long long OUTER = AXIS == 1 ? (long long)D * HP : HP;  // between the columns' rows
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* buf = smem + D;
+  const long long blk = blockIdx.x;
+  const int tile = (int)(blk % P::NT);
+  const int o = (int)((blk / P::NT) % D);
+  const long long s = blk / ((long long)P::NT * D);
+  float2* col = data + s * C + (long long)o * OUTER + tile * TXC + threadIdx.x % TXC;
+  using TS = TileSteps<D, T>;
+  float2 pts[TS::NPTS];
+  TS::for_each_input([&](int n, int i) { pts[i] = col[n * LINE]; });
+  fill_twiddles<D>(tw);
+  __syncthreads();
+  TS::a(buf, tw, [&](int, int, int i) { return make_float2(pts[i].x, -pts[i].y); });
+  __syncthreads();
+  TS::b(buf, tw);
+  __syncthreads();
+  TS::c(buf, [&](int y, int, float2 v) { col[y * LINE] = make_float2(v.x, -v.y); });
+}
+
 // ------------------------------------------------- adjoint filter (k-space)
 // acc = (first ? 0 : acc) + W(|k| R) * scale * U over a half spectrum [D][D][D/2+1]
 // with the weights of the x-pass (the filtered shells are a real, symmetric
@@ -1235,6 +1349,45 @@ bool launch_fft_y(int D, float2* data, long long C, int n_spectra, int threads, 
 }
 
 int fft_z_rows_per_group(int D) { return 2048 / D; }
+
+template <int D, int T, int AXIS>
+static void launch_fwd_cols_t(float2* data, long long C, int n, cudaStream_t s)
+{
+  const long long blocks = (long long)n * D * TilePlan<D>::NT;
+  cudaFuncSetAttribute(k_fft_fwd_cols<D, T, AXIS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y<D>());
+  k_fft_fwd_cols<D, T, AXIS><<<(unsigned)blocks, T, smem_y<D>(), s>>>(data, C, n);
+}
+template <int D>
+static void launch_fwd(const FwdArgs& a, int threads, cudaStream_t s)
+{
+  const size_t bytes = FwdZPlan<D>::BYTES;
+  cudaFuncSetAttribute(k_fft_z_r2c<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  const long long blocks = (long long)a.G * D * D / FWD_ROWS;
+  k_fft_z_r2c<D><<<(unsigned)blocks, FFT_THREADS, bytes, s>>>(a);
+  if (threads == 512) {
+    launch_fwd_cols_t<D, 512, 1>(a.out, a.C, a.G, s);
+    launch_fwd_cols_t<D, 512, 0>(a.out, a.C, a.G, s);
+  } else {
+    launch_fwd_cols_t<D, 256, 1>(a.out, a.C, a.G, s);
+    launch_fwd_cols_t<D, 256, 0>(a.out, a.C, a.G, s);
+  }
+}
+
+bool launch_fft_forward(int D, const FwdArgs& a, int threads, cudaStream_t s)
+{
+  if (a.G < 1 || a.G > MAX_FIELDS)
+    return false;
+  switch (D) {
+    case 32: launch_fwd<32>(a, threads, s); break;
+    case 64: launch_fwd<64>(a, threads, s); break;
+    case 128: launch_fwd<128>(a, threads, s); break;
+    case 256: launch_fwd<256>(a, threads, s); break;
+    case 512: launch_fwd<512>(a, threads, s); break;
+    default: return false;
+  }
+  fft_launches += 3;
+  return true;
+}
 int fft_z_row_groups(int D) { return D * D / fft_z_rows_per_group(D); }
 
 bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s)

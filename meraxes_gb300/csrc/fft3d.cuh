@@ -10,7 +10,7 @@ namespace mx {
 // x-pass: filter + 1/N scale + inverse FFT along x for a batch of radii.
 struct XPassArgs
 {
-  const float2* in[MAX_FIELDS];  // unfiltered, unnormalised half spectra
+  const float2* in[MAX_FIELDS];  // unfiltered, unnormalised half spectra, rows of fft_pitch(D)
   int G;                          // fields
   int n;                          // radii in the batch
   float2* out;                    // spectrum (r*G + g) at out + (r*G + g)*C
@@ -21,6 +21,16 @@ struct XPassArgs
   float delta_k;
   float scale;       // 1/N (exact for power-of-two N)
   float sharpk_max;  // set by launch_fft_x_filter
+};
+
+// Forward R2C of G padded real grids into spectra [kx][ky][kz] with rows of
+// fft_pitch(D) complex values (the x-pass's input layout).
+struct FwdArgs
+{
+  const float* src[MAX_FIELDS];  // PADDED real grids (8-byte aligned)
+  int G;
+  float2* out;  // spectrum g at out + g * C
+  long long C;  // D * D * fft_pitch(D)
 };
 
 // z-pass fused with the find_HII_bubbles per-cell test.
@@ -60,6 +70,9 @@ void launch_filter_accumulate(int D, float2* acc, const float2* U, float R, int 
 // threads per block of the x- and y-pass: 256 or 512
 bool launch_fft_x_filter(int D, const XPassArgs& a, int threads, cudaStream_t s);
 bool launch_fft_y(int D, float2* data, long long C, int n_spectra, int threads, cudaStream_t s);
+// three launches: z (real rows -> half spectrum), y, x; threads of the y and
+// x passes 256 or 512
+bool launch_fft_forward(int D, const FwdArgs& a, int threads, cudaStream_t s);
 bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s);
 bool launch_fft_z_store(int D, const float2* spectra, long long C, int n, int r0, float* shells, long long N,
                         unsigned* err, cudaStream_t s);

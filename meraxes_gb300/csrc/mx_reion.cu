@@ -103,6 +103,7 @@ struct mx_ctx
   long long work_fields = 0;    // capacity in spectra
   size_t work_cap_bytes = 0;    // cap on d_work (0: 45% of free memory)
   long long work_C = 0;         // complex values per batch spectrum: D*D*fft_pitch(D) fused, C otherwise
+  long long unf_C = 0;          // complex values per unfiltered spectrum in d_unf (same rule)
   float2** d_in_ptrs = nullptr; // device array of MAX_FIELDS pointers
   // light cone (Initialise_ConstructLightcone / ConstructLightcone state)
   long long lc_length = -1, lc_pos = 0;
@@ -273,7 +274,11 @@ void mx_ctx::make_shell_map()
 void mx_ctx::alloc_scratch()
 {
   const int G = n_fields(p);
-  MX_CUDA(cudaMalloc(&d_unf, sizeof(float2) * gd.C * MAX_FIELDS));
+  // unfiltered spectra: rows of fft_pitch(D) on the fused path (its forward
+  // transform's layout), of D/2 + 1 (cuFFT's) otherwise; the other users of
+  // this scratch index it in slots of C
+  unf_C = fused_fft ? (long long)gd.D * gd.D * fft_pitch(gd.D) : gd.C;
+  MX_CUDA(cudaMalloc(&d_unf, sizeof(float2) * std::max(gd.C, unf_C) * MAX_FIELDS));
   // Radius batch: as many (radius, field) spectra as the memory plan allows,
   // up to all radii of the snapshot.
   const std::vector<double> radii = filter_radii(p);
@@ -427,11 +432,25 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
     src[G++] = g->N_rec;
   }
   float2* unf_ptrs[MAX_FIELDS];
-  for (int f = 0; f < G; f++) {
-    unf_ptrs[f] = c->d_unf + (long long)f * gd.C;
-    MX_CUFFT(cufftSetStream(c->r2c_plan, s));
-    Prof pr(c, "cufft_r2c", B4N + B8C, s);
-    MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)src[f], (cufftComplex*)unf_ptrs[f]));
+  for (int f = 0; f < G; f++)
+    unf_ptrs[f] = c->d_unf + (long long)f * c->unf_C;
+  if (c->fused_fft) {
+    // hand-written forward transform of all G fields (fft3d.cu)
+    FwdArgs fa;
+    for (int f = 0; f < MAX_FIELDS; f++)
+      fa.src[f] = f < G ? src[f] : nullptr;
+    fa.G = G;
+    fa.out = c->d_unf;
+    fa.C = c->unf_C;
+    const double BC = 8.0 * (double)c->unf_C;
+    Prof pr(c, "fft_forward", G * (B4N * (gd.D + 2) / gd.D + 5.0 * BC), s);
+    launch_fft_forward(gd.D, fa, c->y_threads, s);
+  } else {
+    for (int f = 0; f < G; f++) {
+      MX_CUFFT(cufftSetStream(c->r2c_plan, s));
+      Prof pr(c, "cufft_r2c", B4N + B8C, s);
+      MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)src[f], (cufftComplex*)unf_ptrs[f]));
+    }
   }
   MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, unf_ptrs, sizeof(float2*) * G, cudaMemcpyHostToDevice, s));
 
@@ -837,7 +856,16 @@ static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sf
       launch_shell_extract(sfr, gd.P, 1, 0, c->d_shells, gd, s);
       q_first = 1;
     }
-    if (q_first < r_end) {
+    if (q_first < r_end && c->fused_fft) {
+      FwdArgs fa;
+      for (int f = 0; f < MAX_FIELDS; f++)
+        fa.src[f] = f == 0 ? sfr : nullptr;
+      fa.G = 1;
+      fa.out = sfr_unf;
+      fa.C = c->unf_C;
+      Prof pr(c, "fft_forward", 4.0 * (double)gd.N * (gd.D + 2) / gd.D + 40.0 * (double)c->unf_C, s);
+      launch_fft_forward(gd.D, fa, c->y_threads, s);
+    } else if (q_first < r_end) {
       MX_CUFFT(cufftSetStream(c->r2c_plan, s));
       Prof pr(c, "cufft_r2c", 4.0 * (double)gd.N + 8.0 * (double)gd.C, s);
       MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)sfr, (cufftComplex*)sfr_unf));
@@ -2112,7 +2140,7 @@ static void tune_fft(mx_ctx* c)
     return;
   const GridDims& gd = c->gd;
   cudaStream_t s = c->stream;
-  MX_CUDA(cudaMemsetAsync(c->d_unf, 0, sizeof(float2) * gd.C, s));
+  MX_CUDA(cudaMemsetAsync(c->d_unf, 0, sizeof(float2) * c->unf_C, s));
   const int n = (int)std::min<long long>(std::min<long long>(c->work_fields, 4), MAX_RADII);
   XPassArgs xa;
   for (int f = 0; f < MAX_FIELDS; f++)
