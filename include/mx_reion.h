@@ -215,8 +215,8 @@ const char* mx_last_error(const mx_ctx* ctx); /* ctx may be NULL: last mx_create
 int mx_set_redshifts(mx_ctx* ctx, const double* zz, int32_t n_snaps);
 int32_t mx_n_sfr_histories(const mx_ctx* ctx);
 /* Threads per block that the context's autotuner chose for the x- and
- * y-pass of its fused inverse transforms (256 or 512; 0 and 0 when the grid
- * uses cuFFT).  No reference counterpart. */
+ * y-pass of its fused inverse transforms (x: 256, 512 or 1024; y: 256 or 512;
+ * 0 and 0 when the grid uses cuFFT).  No reference counterpart. */
 int mx_fft_block_sizes(const mx_ctx* ctx, int32_t* x_threads, int32_t* y_threads);
 /* Filter radii of find_HII_bubbles for this configuration (largest first). */
 int32_t mx_filter_radii(const mx_ctx* ctx, double* radii, int32_t cap);

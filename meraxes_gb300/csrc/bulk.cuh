@@ -103,8 +103,30 @@ static inline cudaError_t set_consumer_wait_polls(long long polls)
   return cudaMemcpyToSymbol(consumer_wait_polls, &polls, sizeof(polls));
 }
 
+// Non-blocking test of the phase (mbarrier.test_wait); mbar_test's try_wait
+// may suspend the thread for a while before it returns false.
+__device__ __forceinline__ bool mbar_test_now(uint64_t* bar, unsigned parity)
+{
+  uint32_t ok;
+  asm volatile(
+    "{\n\t.reg .pred p;\n\t"
+    "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+    "selp.u32 %0, 1, 0, p;\n\t}"
+    : "=r"(ok)
+    : "r"(smem_addr(bar)), "r"(parity)
+    : "memory");
+  return ok != 0;
+}
+
 __device__ __forceinline__ bool mbar_wait_polls(uint64_t* bar, unsigned parity, long long polls)
 {
+  if (polls < WAIT_LIMIT_ITERS) {
+    // a lowered limit (a test of the give-up path): polls that do not wait
+    for (long long it = 0; it < polls; it++)
+      if (mbar_test_now(bar, parity))
+        return true;
+    return false;
+  }
   if (mbar_test(bar, parity))
     return true;
   const unsigned long long t0 = global_ns();

@@ -2125,12 +2125,14 @@ int mx_create_limited(const mx_params* params, const char* tables_dir, size_t ma
 // choice; MX_AUTOTUNE=0 keeps the defaults (x 512, y 256).
 static void tune_fft(mx_ctx* c)
 {
-  auto env_threads = [](const char* name) {
+  auto env_threads = [](const char* name, bool allow_1024) {
     const char* v = std::getenv(name);
     const int t = v ? std::atoi(v) : 0;
-    return (t == 256 || t == 512) ? t : 0;
+    return (t == 256 || t == 512 || (allow_1024 && t == 1024)) ? t : 0;
   };
-  const int fx = env_threads("MX_XPASS_THREADS"), fy = env_threads("MX_YPASS_THREADS");
+  // 1024-thread x-pass blocks (8 points per thread) need D >= 64
+  const bool x1024 = c->gd.D >= 64;
+  const int fx = env_threads("MX_XPASS_THREADS", x1024), fy = env_threads("MX_YPASS_THREADS", false);
   if (fx)
     c->x_threads = fx;
   if (fy)
@@ -2173,12 +2175,12 @@ static void tune_fft(mx_ctx* c)
     }
     return best;
   };
-  const int cand[2] = { 256, 512 };
-  float tx[2] = { 0, 0 }, ty[2] = { 0, 0 };
-  for (int i = 0; i < 2; i++) {
-    if (!fx)
+  const int cand[3] = { 256, 512, 1024 };
+  float tx[3] = { 1e30f, 1e30f, 1e30f }, ty[2] = { 1e30f, 1e30f };
+  for (int i = 0; i < 3; i++) {
+    if (!fx && (i < 2 || x1024))
       tx[i] = best_ms([&] { launch_fft_x_filter(gd.D, xa, cand[i], s); });
-    if (!fy)
+    if (!fy && i < 2)
       ty[i] = best_ms([&] { launch_fft_y(gd.D, c->d_work, c->work_C, n, cand[i], s); });
   }
   cudaEventDestroy(e0);
@@ -2186,7 +2188,7 @@ static void tune_fft(mx_ctx* c)
   MX_CUDA(cudaGetLastError());
   MX_CUDA(cudaStreamSynchronize(s));
   if (!fx)
-    c->x_threads = tx[0] < tx[1] ? 256 : 512;
+    c->x_threads = cand[std::min_element(tx, tx + 3) - tx];
   if (!fy)
     c->y_threads = ty[0] < ty[1] ? 256 : 512;
 }

@@ -19,7 +19,8 @@ Tolerances, from the acceptance rule of the step:
     error of an FP32 FFT of N points (the reference's FFTW single-precision
     path carries an error of the same size); values that depend on the radius
     of first crossing (J_21, Gamma12, N_rec) are compared where that radius
-    agrees.  N_rec, which is updated from Gamma12 through the recombination
+    agrees: where the first-crossing margin is at least 1e-4, the decision
+    margin of r_bubble.  N_rec, which is updated from Gamma12 through the recombination
     rate table, also passes on Gamma12's relative difference at the cell.
 
 The report gives, per grid, the largest relative difference, the cells
@@ -66,6 +67,12 @@ def compare(ref: Dict[str, np.ndarray], test: Dict[str, np.ndarray], ref_globals
     assert dis.sum() <= FLAG_FRACTION * n, f"flags differ in {dis.sum()} of {n} cells"
     if margin is not None:
         m_first, m_all = margin[0].reshape(-1), margin[1].reshape(-1)
+        edges = (1e-6, 1e-5, 1e-4)
+        for name, sel_, m in (("flag", dis, m_first), ("rbubble", rb_dis, m_all)):
+            mm = m[sel_]
+            rep[name + "_margin_buckets"] = [int((mm < edges[0]).sum())] + \
+                [int(((mm >= lo) & (mm < hi)).sum()) for lo, hi in zip(edges[:-1], edges[1:])] + \
+                [int((mm >= edges[-1]).sum())]
         if dis.any():
             rep["flag_margin_max"] = float(m_first[dis].max())
             assert np.all(m_first[dis] < MARGIN), f"flag disagreement at margin {m_first[dis].max():.3e} ({rep})"
@@ -75,7 +82,7 @@ def compare(ref: Dict[str, np.ndarray], test: Dict[str, np.ndarray], ref_globals
             assert rb_dis.sum() <= FLAG_FRACTION * n, f"r_bubble differs in {rb_dis.sum()} of {n} cells"
             assert np.all(m_all[rb_dis] < RBUBBLE_MARGIN), \
                 f"r_bubble disagreement at margin {m_all[rb_dis].max():.3e} ({rep})"
-        near_first = m_first < MARGIN
+        near_first = m_first < RBUBBLE_MARGIN
     else:
         assert rb_dis.sum() <= FLAG_FRACTION * n, f"r_bubble differs in {rb_dis.sum()} of {n} cells"
         near_first = np.zeros(n, bool)

@@ -81,7 +81,12 @@ def _workload(name, D, snapshots=None):
 
 def _oracle_vs_gpu(w, tables_dir):
     """Runs w's snapshots on the oracle and through mx_step on the same
-    inputs; compares every snapshot with the oracle's margins."""
+    inputs; compares every snapshot with the oracle's margins.  Each snapshot
+    starts from the same state on both sides (the GPU's is replaced by the
+    oracle's after each comparison): a cell whose decision flips near
+    threshold changes its N_rec, z_at_ionization and x_e, and through the
+    filters its neighbours' margins in the next snapshot, so margins hold
+    only for a step on identical inputs."""
     from cases import initial
     from meraxes_gb300 import synthetic as syn
     from meraxes_gb300.api import ReionGridStep
@@ -106,6 +111,7 @@ def _oracle_vs_gpu(w, tables_dir):
         compare(sa, sb, ga, gb, margin=margin, report=rep)
         rep["means_rel"] = check_means(sb, gb, w.params.grid_dim, w.params)
         reps.append(rep)
+        sb = {k: v.copy() for k, v in sa.items()}
     gpu.close()
     orc.close()
     return reps
