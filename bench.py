@@ -74,6 +74,7 @@ def parse_args(argv=None):
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="time the device step uncaptured")
     ap.add_argument("--adjoint-grid", type=int, default=256)
     return ap.parse_args(argv)
 
@@ -356,9 +357,17 @@ def run_gb300(args, rank, world, local):
     step = ReionGridStep(p, w.redshifts)
     n_hist = step.n_sfr_histories
     hist, smax = history_buffer(fields, used, n_hist, D, device)
+    # the headline: every snapshot's step captured and launched as one CUDA
+    # graph; the same evolution uncaptured is timed beside it
+    ungraphed = None
+    if not args.no_graph:
+        ms0, _, _, _, _ = time_evolution(step, w, fields, hist, smax, warm, timed, device, world, local)
+        ungraphed = replica_value(ms0, args.steps, world, device)
+        step.set_graph(True)
     ms, launches, glob, clk, kstats = time_evolution(step, w, fields, hist, smax, warm, timed, device, world, local,
                                                      profile=True)
     value = replica_value(ms, args.steps, world, device)
+    step.set_graph(False)
 
     # per-kernel achieved bandwidth (algorithmic bytes / event time)
     peaks = {}
@@ -417,7 +426,9 @@ def run_gb300(args, rank, world, local):
                             "warm-up)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (each grid 0.54 GB at 512^3)",
-                   "fft_block_sizes": block_sizes},
+                   "fft_block_sizes": block_sizes,
+                   "step_graph": not args.no_graph},
+        "value_uncaptured": round(ungraphed, 3) if ungraphed is not None else None,
         "gpu_launches": launches, "clocks": clk, "roofline": roofline,
         "step_model_gbs": round(model_gbs, 1), "step_model_frac": round(model_gbs / hbm_peak, 4),
         "step_model_bytes": model_bytes, "step_pass_gbs": round(step_gbs, 1),

@@ -215,8 +215,8 @@ const char* mx_last_error(const mx_ctx* ctx); /* ctx may be NULL: last mx_create
 int mx_set_redshifts(mx_ctx* ctx, const double* zz, int32_t n_snaps);
 int32_t mx_n_sfr_histories(const mx_ctx* ctx);
 /* Threads per block that the context's autotuner chose for the x- and
- * y-pass of its fused inverse transforms (x: 256, 512 or 1024; y: 256 or 512;
- * 0 and 0 when the grid uses cuFFT).  No reference counterpart. */
+ * y-pass of its fused inverse transforms (256 or 512; 0 and 0 when the grid
+ * uses cuFFT).  No reference counterpart. */
 int mx_fft_block_sizes(const mx_ctx* ctx, int32_t* x_threads, int32_t* y_threads);
 /* Filter radii of find_HII_bubbles for this configuration (largest first). */
 int32_t mx_filter_radii(const mx_ctx* ctx, double* radii, int32_t cap);
@@ -240,6 +240,15 @@ int mx_ComputeBrightnessTemperatureBox_device(mx_ctx* ctx,
                                               mx_globals* out,
                                               void* stream);
 int mx_step_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream);
+/* With on != 0, each later mx_step_device call captures the whole step
+ * (ComputeTs, find_HII_bubbles, the 21cm box) into one CUDA graph on the
+ * context's stream and launches it on `stream`; ComputeTs's frequency tables
+ * are built by a host node of the graph while the shells are smoothed.  The
+ * grids and globals equal those of the uncaptured step bit for bit.  Each
+ * call captures anew (kernel arguments depend on the snapshot); per-kernel
+ * profiling records its events as event nodes of the graph.  No reference
+ * counterpart (the reference runs the three calls from the dracarys loop). */
+int mx_set_step_graph(mx_ctx* ctx, int32_t on);
 
 /* Per-kernel timing with CUDA events recorded on the launching stream around
  * every kernel and cuFFT execution of the context.  No reference counterpart

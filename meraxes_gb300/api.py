@@ -93,6 +93,11 @@ class ReionGridStep:
         n = self.lib.mx_filter_radii(self.ctx, buf, 1024)
         return list(buf[:n])
 
+    def set_graph(self, on: bool = True):
+        """Device steps (step() on CUDA tensors) captured and launched as one
+        CUDA graph each (mx_set_step_graph)."""
+        self._check(self.lib.mx_set_step_graph(self.ctx, 1 if on else 0))
+
     def fft_block_sizes(self):
         """Threads per block of the fused x- and y-pass chosen at creation."""
         x, y = ctypes.c_int32(), ctypes.c_int32()

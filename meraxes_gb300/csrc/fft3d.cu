@@ -424,14 +424,9 @@ __device__ __forceinline__ void tile_dft(float2* buf, const float2* tw, Load loa
 // sincosf) measured slower: the table read before the block's barrier is a
 // DRAM wait that the weights' arithmetic is not (a 28-radius one-field batch
 // at 512^3 took 8.75 ms with tables, 5.90 ms without).
-// XTHREADS threads per block: 256, 512 or 1024 (the context's autotuner
-// picks).  With 1024 threads a thread holds 8 points of an item, and the next
-// item's points are read right after step A, so that their loads are in
-// flight during steps B and C (with 16 or 32 points per thread that prefetch
-// spills registers).
+// XTHREADS threads per block: 256 or 512 (the context's autotuner picks).
 template <int D, int XTHREADS>
-__global__ void __launch_bounds__(XTHREADS, XTHREADS == 1024 ? 1 : (XTHREADS == 256 && D < 512 ? 3 : 2))
-  k_fft_x_filter(const __grid_constant__ XPassArgs a)
+__global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) k_fft_x_filter(const __grid_constant__ XPassArgs a)
 {
   using P = TilePlan<D>;
   constexpr int H = D / 2 + 1;
@@ -469,13 +464,9 @@ __global__ void __launch_bounds__(XTHREADS, XTHREADS == 1024 ? 1 : (XTHREADS == 
   }
   const float* wcol = wsm + t0;
   const int n_rows = (kyp == 0 || kyp == D / 2) ? 1 : 2;
-  constexpr bool PREFETCH = XTHREADS == 1024;
-  if constexpr (PREFETCH)
-    read_points(kyp, 0);
   for (int h = 0; h < n_rows; h++) {
     const int ky = h == 0 ? kyp : D - kyp;
-    if constexpr (!PREFETCH)
-      read_points(ky, 0);
+    read_points(ky, 0);
     if (h == 0)
       __syncthreads();
     // steps B and C of field g after its step A
@@ -497,18 +488,6 @@ __global__ void __launch_bounds__(XTHREADS, XTHREADS == 1024 ? 1 : (XTHREADS == 
         return x;
       });
     };
-    if constexpr (PREFETCH) {
-      // item (h, g): step A, then the next item's reads, then steps B and C
-      for (int g = 0; g < a.G; g++) {
-        step_a();
-        if (g + 1 < a.G)
-          read_points(ky, g + 1);
-        else if (h + 1 < n_rows)
-          read_points(D - kyp, 0);
-        finish(g);
-      }
-      continue;
-    }
     step_a();
     finish(0);
     for (int g = 1; g < a.G; g++) {
@@ -1287,8 +1266,6 @@ static void launch_x(const XPassArgs& a, int threads, cudaStream_t s)
 {
   if (threads == 256)
     launch_x_t<D, 256>(a, s);
-  else if (threads == 1024 && D >= 64)
-    launch_x_t<D, 1024>(a, s);
   else
     launch_x_t<D, 512>(a, s);
 }

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <future>
 #include <map>
 #include <mutex>
@@ -148,6 +149,20 @@ struct mx_ctx
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> prof_events;
 
+  // Whole-step CUDA graph (mx_set_step_graph): mx_step_device captures
+  // ComputeTs -> find_HII_bubbles -> 21cm box on the context stream and
+  // launches the step as one graph.  While capturing, values read back from
+  // the device land in pinned slots of h_stage and the code that uses them
+  // (`finishers`) runs after the graph has completed; host data uploaded by
+  // the step is staged in h_stage too, so that it outlives the capture.
+  // ComputeTs's frequency tables are built by a host node of the graph.
+  bool graph_on = false;
+  bool capturing = false;
+  unsigned char* h_stage = nullptr;  // pinned, STAGE_BYTES
+  size_t stage_used = 0;
+  std::vector<std::function<void()>> finishers;
+  std::vector<std::shared_ptr<void>> graph_keep;  // host-node payloads of the step being captured
+
   ~mx_ctx();
   void alloc_scratch();
   void make_shell_map();
@@ -172,13 +187,22 @@ class Prof
     }
     c->prof.push_back({ name, bytes, ev });
     idx_ = ev;
-    MX_CUDA(cudaEventRecord(c->prof_events[ev], s));
+    MX_CUDA(record(c->prof_events[ev]));
   }
   ~Prof()
   {
     if (idx_ >= 0)
-      cudaEventRecord(c_->prof_events[idx_ + 1], s_);
+      record(c_->prof_events[idx_ + 1]);
   }
+
+ private:
+  // inside a captured step the record is an event node of the graph
+  cudaError_t record(cudaEvent_t e)
+  {
+    return c_->capturing ? cudaEventRecordWithFlags(e, s_, cudaEventRecordExternal) : cudaEventRecord(e, s_);
+  }
+
+ public:
 
  private:
   mx_ctx* c_;
@@ -186,8 +210,58 @@ class Prof
   int idx_ = -1;
 };
 
+// pinned staging of a step: read-back slots and uploads (graph capture)
+constexpr size_t STAGE_BYTES = 1 << 20;
+
+static void* stage(mx_ctx* c, size_t bytes)
+{
+  const size_t b = (bytes + 255) & ~(size_t)255;
+  if (c->stage_used + b > STAGE_BYTES)
+    throw CudaError{ MX_ENOTSUP, "step staging area exhausted" };
+  void* q = c->h_stage + c->stage_used;
+  c->stage_used += b;
+  return q;
+}
+
+// n values of type T read back from device memory into a pinned slot; the
+// slot is valid in the code passed to after()
+template <class T>
+static const T* readback(mx_ctx* c, const T* dsrc, int n, cudaStream_t s)
+{
+  T* h = static_cast<T*>(stage(c, sizeof(T) * (size_t)n));
+  MX_CUDA(cudaMemcpyAsync(h, dsrc, sizeof(T) * (size_t)n, cudaMemcpyDeviceToHost, s));
+  return h;
+}
+
+// Runs f once the work queued on s so far has completed: now (after a
+// synchronize) outside a capture, after the graph's completion inside one.
+template <class F>
+static void after(mx_ctx* c, cudaStream_t s, F&& f)
+{
+  if (c->capturing) {
+    c->finishers.emplace_back(std::forward<F>(f));
+    return;
+  }
+  MX_CUDA(cudaStreamSynchronize(s));
+  c->stage_used = 0;
+  f();
+}
+
+// Host -> device copy of data that the caller may overwrite after the call
+// returns: staged in pinned memory while capturing.
+static void upload(mx_ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t s)
+{
+  if (c->capturing) {
+    void* q = stage(c, bytes);
+    std::memcpy(q, src, bytes);
+    src = q;
+  }
+  MX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+}
+
 mx_ctx::~mx_ctx()
 {
+  cudaFreeHost(h_stage);
   for (cudaEvent_t e : prof_events)
     cudaEventDestroy(e);
   for (auto& kv : c2r_plans)
@@ -305,6 +379,7 @@ void mx_ctx::alloc_scratch()
   MX_CUDA(cudaMallocHost(&h_ps_sums, sizeof(double) * (3 * PS_MAX_BINS + 1)));
   MX_CUDA(cudaMalloc(&d_sums, sizeof(double) * 16));
   MX_CUDA(cudaMallocHost(&h_sums, sizeof(double) * 16));
+  MX_CUDA(cudaMallocHost(&h_stage, STAGE_BYTES));
   MX_CUDA(cudaMalloc(&d_rp, sizeof(RadiusParams) * MAX_RADII));
   MX_CUDA(cudaMalloc(&d_err, sizeof(unsigned int)));
   MX_CUDA(cudaMemset(d_err, 0, sizeof(unsigned int)));
@@ -452,7 +527,8 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
       MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)src[f], (cufftComplex*)unf_ptrs[f]));
     }
   }
-  MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, unf_ptrs, sizeof(float2*) * G, cudaMemcpyHostToDevice, s));
+  if (!c->fused_fft)
+    upload(c, c->d_in_ptrs, unf_ptrs, sizeof(float2*) * G, s);
 
   // radius schedule (find_HII_bubbles.c:184-207)
   const std::vector<double> radii = filter_radii(p);
@@ -481,7 +557,7 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
     q.kj = (float)(q.J21_const / pixel_volume);
     q.kg = (float)(q.Gamma_pref / pixel_volume);
   }
-  MX_CUDA(cudaMemcpyAsync(c->d_rp, rps.data(), sizeof(RadiusParams) * nR, cudaMemcpyHostToDevice, s));
+  upload(c, c->d_rp, rps.data(), sizeof(RadiusParams) * nR, s);
 
   // batched filter -> C2R -> threshold over chunks of radii, largest first.
   // A host call (whose output copies overlap the last batch's threshold
@@ -650,22 +726,24 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
     launch_fhb_reduce(ra, gd, s);
   }
   launch_finalize(c->d_partials, 4, c->d_sums, s);
-  MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
-  unsigned int errw = 0;
-  MX_CUDA(cudaMemcpyAsync(&errw, c->d_err, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
-  MX_CUDA(cudaStreamSynchronize(s));
-  if (errw) {
-    MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
-    throw CudaError{ MX_ECUDA, "find_HII_bubbles: a transform pipeline wait timed out" };
-  }
+  const double* sums = readback(c, (const double*)c->d_sums, 4, s);
+  const unsigned int* errw = readback(c, (const unsigned int*)c->d_err, 1, s);
   const double total = std::pow((double)gd.D, 3);
   if (out) {
-    out->volume_weighted_global_xH = c->h_sums[0] / total;
-    out->volume_weighted_global_J_21 = uvb ? c->h_sums[1] / total : 0.0;
-    out->mass_weighted_global_xH = c->h_sums[2] / c->h_sums[3];
     out->n_radii = nR;
     out->gpu_launches = kernel_launch_count() - launches0;
   }
+  after(c, s, [c, s, sums, errw, out, total, uvb]() {
+    if (*errw) {
+      MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
+      throw CudaError{ MX_ECUDA, "find_HII_bubbles: a transform pipeline wait timed out" };
+    }
+    if (out) {
+      out->volume_weighted_global_xH = sums[0] / total;
+      out->volume_weighted_global_J_21 = uvb ? sums[1] / total : 0.0;
+      out->mass_weighted_global_xH = sums[2] / sums[3];
+    }
+  });
 }
 
 // ======================================================================
@@ -871,7 +949,8 @@ static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sf
       MX_CUFFT(cufftExecR2C(c->r2c_plan, (cufftReal*)sfr, (cufftComplex*)sfr_unf));
     }
     float2* in_ptr[1] = { sfr_unf };
-    MX_CUDA(cudaMemcpyAsync(c->d_in_ptrs, in_ptr, sizeof(float2*), cudaMemcpyHostToDevice, s));
+    if (!c->fused_fft)
+      upload(c, c->d_in_ptrs, in_ptr, sizeof(float2*), s);
     for (int q0 = q_first; q0 < r_end;) {
       const int nb = (int)std::min<long long>(std::min<long long>(c->work_fields, MAX_RADII), r_end - q0);
       if (c->fused_fft) {
@@ -933,6 +1012,41 @@ static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sf
   }
 }
 
+// ComputeTs's host work inside a captured step: a host node of the graph
+// reads the collapse fraction and <x_e> (copied to pinned slots by the node
+// before it), builds the frequency-integral tables and fills the evolve
+// kernels' constants into the pinned h_tsc, which the next node uploads.
+struct TsHostWork
+{
+  mx_ctx* c = nullptr;
+  int snapshot = 0;
+  ShellPlan sp;
+  double zp = 0, prev_z = 0, pixel_volume = 0, total = 1;
+  const double* cf = nullptr;  // pinned: sum of f_coll, sum of x_e
+  std::string err;
+};
+
+static void CUDART_CB ts_tables_host(void* arg)
+{
+  TsHostWork* w = static_cast<TsHostWork*>(arg);
+  mx_ctx* c = w->c;
+  try {
+    const double collapse_fraction = w->cf[0] / w->total, x_e_ave = w->cf[1] / w->total;
+    c->stored_fcoll[w->snapshot] = collapse_fraction;
+    FreqTables ft;
+    build_freq_tables(c->p, c->d, c->ht, c->zz, c->stored_fcoll, w->snapshot, w->sp, x_e_ave, w->sp.weight_after,
+                      c->nthreads, &ft);
+    TsDevConst* t = c->h_tsc;
+    std::memset(t, 0, sizeof(TsDevConst));
+    fill_common_ts(c, t, w->zp);
+    fill_ts_constants(c, t, w->sp, ft, w->zp, w->prev_z, collapse_fraction, w->pixel_volume);
+  } catch (const CudaError& e) {
+    w->err = e.msg;
+  } catch (const std::exception& e) {
+    w->err = e.what();
+  }
+}
+
 static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* out, cudaStream_t s,
                           const TsUploads* up = nullptr)
 {
@@ -959,6 +1073,9 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
   const double R0 = k::L_FACTOR * box / (float)gd.D;
   const double RtoM_h2 = RtoM(p, c->d, R0) * p.hubble_h * p.hubble_h;
   double collapse_fraction = 0.0, x_e_ave = 0.0;
+  const double* homog_cf = nullptr;      // read back: sum of f_coll (homogeneous branch)
+  const double* evolve_sums = nullptr;   // read back: J_alpha, xalpha, Xheat, Xion sums
+  std::shared_ptr<TsHostWork> hw;        // host node of a captured step
 
   if (up) {
     MX_CUDA(cudaStreamWaitEvent(s, up->first, 0));
@@ -969,7 +1086,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
   }
   if (sp.homogeneous) {
     // ComputeTs.c:189-262
-    MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
+    upload(c, c->d_tsc, t, sizeof(TsDevConst), s);
     HomogArgs ha;
     ha.deltax = g->deltax;
     ha.stars = g->stars;
@@ -987,9 +1104,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     Prof pr(c, "k_homog", 5.0 * 4.0 * (double)gd.N, s);
     launch_homog(ha, gd, s);
     launch_finalize(c->d_partials, 1, c->d_sums, s);
-    MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double), cudaMemcpyDeviceToHost, s));
-    MX_CUDA(cudaStreamSynchronize(s));
-    collapse_fraction = c->h_sums[0] / total;
+    homog_cf = readback(c, (const double*)c->d_sums, 1, s);
   } else {
     // collapse fraction and <x_e> of the unsmoothed fields (ComputeTs.c:413-475)
     CfArgs ca;
@@ -1005,33 +1120,56 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
       launch_cf_xe(ca, gd, s);
     }
     launch_finalize(c->d_partials, 2, c->d_sums, s);
-    MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
-    MX_CUDA(cudaStreamSynchronize(s));
-    collapse_fraction = c->h_sums[0] / total;
-    x_e_ave = c->h_sums[1] / total;
-    c->stored_fcoll[snapshot] = collapse_fraction;
-
-    // X-ray frequency tables on host threads while the shells are smoothed
-    FreqTables ft;
-    std::vector<double> zz = c->zz;
-    std::future<void> tables = std::async(std::launch::async, [&]() {
-      build_freq_tables(p, c->d, c->ht, zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads,
-                        &ft);
-    });
-
-    // shells (ComputeTs.c:276-503): apply the SFR-history operations, forward
-    // transform when the grid changed, then filter + inverse transform in
-    // batches of shells sharing a spectrum.
-    try {
+    if (c->capturing) {
+      // a captured step: the tables are built by a host node on a side
+      // branch of the graph while the shells are smoothed on s
+      hw = std::make_shared<TsHostWork>();
+      hw->c = c;
+      hw->snapshot = snapshot;
+      hw->sp = sp;
+      hw->zp = zp;
+      hw->prev_z = prev_z;
+      hw->pixel_volume = pixel_volume;
+      hw->total = total;
+      cudaStream_t hs = c->copy_stream;
+      MX_CUDA(cudaEventRecord(c->ev_a, s));
+      MX_CUDA(cudaStreamWaitEvent(hs, c->ev_a, 0));
+      hw->cf = readback(c, (const double*)c->d_sums, 2, hs);
+      MX_CUDA(cudaLaunchHostFunc(hs, ts_tables_host, hw.get()));
+      MX_CUDA(cudaMemcpyAsync(c->d_tsc, c->h_tsc, sizeof(TsDevConst), cudaMemcpyHostToDevice, hs));
+      MX_CUDA(cudaEventRecord(c->ev_b, hs));
+      c->graph_keep.push_back(hw);
       compute_shells(c, sp, g->sfr, g->sfr_histories, s, up);
-    } catch (...) {
-      tables.wait();
-      throw;
-    }
-    tables.get();
+      MX_CUDA(cudaStreamWaitEvent(s, c->ev_b, 0));
+    } else {
+      MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+      MX_CUDA(cudaStreamSynchronize(s));
+      collapse_fraction = c->h_sums[0] / total;
+      x_e_ave = c->h_sums[1] / total;
+      c->stored_fcoll[snapshot] = collapse_fraction;
 
-    fill_ts_constants(c, t, sp, ft, zp, prev_z, collapse_fraction, pixel_volume);
-    MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
+      // X-ray frequency tables on host threads while the shells are smoothed
+      FreqTables ft;
+      std::vector<double> zz = c->zz;
+      std::future<void> tables = std::async(std::launch::async, [&]() {
+        build_freq_tables(p, c->d, c->ht, zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads,
+                          &ft);
+      });
+
+      // shells (ComputeTs.c:276-503): apply the SFR-history operations, forward
+      // transform when the grid changed, then filter + inverse transform in
+      // batches of shells sharing a spectrum.
+      try {
+        compute_shells(c, sp, g->sfr, g->sfr_histories, s, up);
+      } catch (...) {
+        tables.wait();
+        throw;
+      }
+      tables.get();
+
+      fill_ts_constants(c, t, sp, ft, zp, prev_z, collapse_fraction, pixel_volume);
+      MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
+    }
     EvolveArgs ea;
     ea.shells = c->d_shells;
     ea.deltax = g->deltax;
@@ -1050,7 +1188,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
       ev_blocks = launch_evolve(ea, gd, c->has_shell_map ? &c->shell_map : nullptr, s);
     }
     launch_finalize(c->d_partials, 4, c->d_sums + 8, s, ev_blocks);
-    MX_CUDA(cudaMemcpyAsync(c->h_sums + 8, c->d_sums + 8, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+    evolve_sums = readback(c, (const double*)(c->d_sums + 8), 4, s);
   }
 
   // x_e_box <- x_e_box_prev (ComputeTs.c:940) and the means (:942-974)
@@ -1063,34 +1201,43 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     launch_ts_means(g->TS_box, g->Tk_box, c->d_partials, gd, s);
   }
   launch_finalize(c->d_partials, 2, c->d_sums, s);
-  MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+  const double* means = readback(c, (const double*)c->d_sums, 2, s);
   // the reference's <x_e> reads the last cell's x_e_box_prev (ComputeTs.c:957)
   const long long last_pad = (long long)(gd.D - 1) + 2LL * gd.H * ((long long)(gd.D - 1) + (long long)gd.D * (gd.D - 1));
-  float xe_last = 0.f;
-  MX_CUDA(cudaMemcpyAsync(c->d_xe_last, g->x_e_box_prev + last_pad, sizeof(float), cudaMemcpyDeviceToDevice, s));
-  unsigned int errw = 0;
-  MX_CUDA(cudaMemcpyAsync(&errw, c->d_err, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
-  MX_CUDA(cudaMemcpyAsync(&xe_last, c->d_xe_last, sizeof(float), cudaMemcpyDeviceToHost, s));
-  MX_CUDA(cudaStreamSynchronize(s));
-  if (errw) {
-    MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
-    throw CudaError{ MX_ECUDA, (errw & 2u) ? "ComputeTs: a pipeline wait (transform or shell copies) timed out"
-                                           : "ComputeTs: spin-temperature iteration did not converge" };
-  }
-  if (out) {
-    if (!sp.homogeneous) {
-      out->volume_ave_J_alpha = c->h_sums[8] / total;
-      out->volume_ave_xalpha = c->h_sums[9] / total;
-      out->volume_ave_Xheat = c->h_sums[10] / total;
-      out->volume_ave_Xion = c->h_sums[11] / total;
-    }
-    out->volume_ave_TS = c->h_sums[0] / total;
-    out->volume_ave_TK = c->h_sums[1] / total;
-    out->volume_ave_xe = (double)xe_last;
-    out->x_e_ave = x_e_ave;
-    out->collapse_fraction = collapse_fraction;
+  const float* xe_last = readback(c, (const float*)(g->x_e_box_prev + last_pad), 1, s);
+  const unsigned int* errw = readback(c, (const unsigned int*)c->d_err, 1, s);
+  if (out)
     out->gpu_launches = kernel_launch_count() - launches0;
-  }
+  const bool homog = sp.homogeneous;
+  after(c, s, [=]() {
+    if (*errw) {
+      MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
+      throw CudaError{ MX_ECUDA, (*errw & 2u) ? "ComputeTs: a pipeline wait (transform or shell copies) timed out"
+                                              : "ComputeTs: spin-temperature iteration did not converge" };
+    }
+    if (hw && !hw->err.empty())
+      throw CudaError{ MX_ETABLE, "ComputeTs tables: " + hw->err };
+    double cf = collapse_fraction, xe = x_e_ave;
+    if (homog_cf)
+      cf = homog_cf[0] / total;
+    if (hw) {
+      cf = hw->cf[0] / total;
+      xe = hw->cf[1] / total;
+    }
+    if (out) {
+      if (!homog) {
+        out->volume_ave_J_alpha = evolve_sums[0] / total;
+        out->volume_ave_xalpha = evolve_sums[1] / total;
+        out->volume_ave_Xheat = evolve_sums[2] / total;
+        out->volume_ave_Xion = evolve_sums[3] / total;
+      }
+      out->volume_ave_TS = means[0] / total;
+      out->volume_ave_TK = means[1] / total;
+      out->volume_ave_xe = (double)xe_last[0];
+      out->x_e_ave = xe;
+      out->collapse_fraction = cf;
+    }
+  });
 }
 
 // ======================================================================
@@ -1195,12 +1342,14 @@ static void run_delta_T(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals* 
   } else {
     launch_finalize(c->d_partials, 1, c->d_sums, s);
   }
-  MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double), cudaMemcpyDeviceToHost, s));
-  MX_CUDA(cudaStreamSynchronize(s));
-  if (out) {
-    out->volume_ave_Tb = c->h_sums[0] / std::pow((double)gd.D, 3);
+  const double* sum = readback(c, (const double*)c->d_sums, 1, s);
+  if (out)
     out->gpu_launches = kernel_launch_count() - launches0;
-  }
+  const double total = std::pow((double)gd.D, 3);
+  after(c, s, [sum, out, total]() {
+    if (out)
+      out->volume_ave_Tb = sum[0] / total;
+  });
 }
 
 // ======================================================================
@@ -1862,6 +2011,74 @@ static void check_snapshot(mx_ctx* c, int snapshot)
 
 static cudaStream_t pick(mx_ctx* c, void* stream) { return stream ? (cudaStream_t)stream : c->stream; }
 
+// The device step (ComputeTs -> find_HII_bubbles -> 21cm box) as one CUDA
+// graph: captured on the context stream (thread-local capture mode), then
+// instantiated and launched on `s`; the reads back of the step run after the
+// graph has completed.  Every call captures the step anew: its kernel
+// arguments, radius parameters and history operations depend on the
+// snapshot.
+static void step_graph(mx_ctx* c, int snapshot, const mx_grids* dev, mx_globals* out, cudaStream_t s)
+{
+  cudaStream_t cs = c->stream;
+  mx_globals scratch{};
+  mx_globals* o = out ? out : &scratch;
+  c->stage_used = 0;
+  c->finishers.clear();
+  c->graph_keep.clear();
+  cudaGraph_t graph = nullptr;
+  int launches = 0;
+  // cuFFT plans allocate their work areas when created, which a capture
+  // does not allow: create the ones the step uses first
+  if (!c->fused_fft) {
+    c->c2r_plan(n_fields(c->p));
+    if (c->p.flag_spin_temp)
+      c->c2r_plan(1);
+  }
+  if (c->p.flag_spin_temp && c->p.flag_pecvel > 0)
+    c->c2r_plan(1);
+  MX_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  c->capturing = true;
+  try {
+    if (c->p.flag_spin_temp) {
+      run_ComputeTs(c, snapshot, dev, o, cs);
+      launches += o->gpu_launches;
+    }
+    run_find_HII_bubbles(c, snapshot, dev, o, cs);
+    launches += o->gpu_launches;
+    if (c->p.flag_21cm) {
+      run_delta_T(c, snapshot, dev, o, cs);
+      launches += o->gpu_launches;
+    }
+  } catch (...) {
+    c->capturing = false;
+    if (cudaStreamEndCapture(cs, &graph) == cudaSuccess && graph)
+      cudaGraphDestroy(graph);
+    c->finishers.clear();
+    c->graph_keep.clear();
+    throw;
+  }
+  c->capturing = false;
+  MX_CUDA(cudaStreamEndCapture(cs, &graph));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess)
+    throw CudaError{ MX_ECUDA, std::string("step graph: ") + cudaGetErrorString(ei) };
+  const cudaError_t el = cudaGraphLaunch(exec, s);
+  const cudaError_t es = el == cudaSuccess ? cudaStreamSynchronize(s) : el;
+  cudaGraphExecDestroy(exec);
+  if (es != cudaSuccess)
+    throw CudaError{ MX_ECUDA, std::string("step graph: ") + cudaGetErrorString(es) };
+  std::vector<std::function<void()>> fin;
+  fin.swap(c->finishers);
+  c->graph_keep.clear();
+  for (auto& f : fin)
+    f();
+  c->stage_used = 0;
+  if (out)
+    out->gpu_launches = launches;
+}
+
 extern "C" {
 
 const char* mx_build_info(void) { return "meraxes_gb300 reion step, sm_103a, abi 1"; }
@@ -2125,14 +2342,12 @@ int mx_create_limited(const mx_params* params, const char* tables_dir, size_t ma
 // choice; MX_AUTOTUNE=0 keeps the defaults (x 512, y 256).
 static void tune_fft(mx_ctx* c)
 {
-  auto env_threads = [](const char* name, bool allow_1024) {
+  auto env_threads = [](const char* name) {
     const char* v = std::getenv(name);
     const int t = v ? std::atoi(v) : 0;
-    return (t == 256 || t == 512 || (allow_1024 && t == 1024)) ? t : 0;
+    return (t == 256 || t == 512) ? t : 0;
   };
-  // 1024-thread x-pass blocks (8 points per thread) need D >= 64
-  const bool x1024 = c->gd.D >= 64;
-  const int fx = env_threads("MX_XPASS_THREADS", x1024), fy = env_threads("MX_YPASS_THREADS", false);
+  const int fx = env_threads("MX_XPASS_THREADS"), fy = env_threads("MX_YPASS_THREADS");
   if (fx)
     c->x_threads = fx;
   if (fy)
@@ -2175,12 +2390,12 @@ static void tune_fft(mx_ctx* c)
     }
     return best;
   };
-  const int cand[3] = { 256, 512, 1024 };
-  float tx[3] = { 1e30f, 1e30f, 1e30f }, ty[2] = { 1e30f, 1e30f };
-  for (int i = 0; i < 3; i++) {
-    if (!fx && (i < 2 || x1024))
+  const int cand[2] = { 256, 512 };
+  float tx[2] = { 0, 0 }, ty[2] = { 0, 0 };
+  for (int i = 0; i < 2; i++) {
+    if (!fx)
       tx[i] = best_ms([&] { launch_fft_x_filter(gd.D, xa, cand[i], s); });
-    if (!fy && i < 2)
+    if (!fy)
       ty[i] = best_ms([&] { launch_fft_y(gd.D, c->d_work, c->work_C, n, cand[i], s); });
   }
   cudaEventDestroy(e0);
@@ -2188,7 +2403,7 @@ static void tune_fft(mx_ctx* c)
   MX_CUDA(cudaGetLastError());
   MX_CUDA(cudaStreamSynchronize(s));
   if (!fx)
-    c->x_threads = cand[std::min_element(tx, tx + 3) - tx];
+    c->x_threads = tx[0] < tx[1] ? 256 : 512;
   if (!fy)
     c->y_threads = ty[0] < ty[1] ? 256 : 512;
 }
@@ -2407,12 +2622,21 @@ int mx_ComputeBrightnessTemperatureBox_device(mx_ctx* ctx,
   });
 }
 
+int mx_set_step_graph(mx_ctx* ctx, int32_t on)
+{
+  return guarded(ctx, [&]() { ctx->graph_on = on != 0; });
+}
+
 int mx_step_device(mx_ctx* ctx, int32_t snapshot, const mx_grids* dev, mx_globals* out, void* stream)
 {
   return guarded(ctx, [&]() {
     check_snapshot(ctx, snapshot);
     check_device_grids(dev);
     cudaStream_t s = pick(ctx, stream);
+    if (ctx->graph_on) {
+      step_graph(ctx, snapshot, dev, out, s);
+      return;
+    }
     int launches = 0;
     if (ctx->p.flag_spin_temp) {
       run_ComputeTs(ctx, snapshot, dev, out, s);
