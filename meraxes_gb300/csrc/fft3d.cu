@@ -154,13 +154,11 @@ __device__ __forceinline__ void dft_bwd(float2 (&v)[M])
   dft_stage<M, 1, 0, 0>(v);
 }
 
-// k-space filter of reionization.c:2110-2170 in single precision only:
-//  * real-space top-hat 3 (sin kR / kR^3 - cos kR / kR^2) as
-//    3 (sin kR / kR - cos kR) / kR^2 from one sincosf and one fast reciprocal
-//    (a few ulp from the reference's float expression, far inside the
-//    tolerance of an FP32 transform).  The reference's test (double)kR > 1e-4
-//    is the same predicate as kR > 1e-4f (1e-4f is the largest float below
-//    1e-4);
+// k-space filter of reionization.c:2110-2170:
+//  * real-space top-hat: tophat_weight (kernels.cuh), the reference's float
+//    expression below kR = 1, where it cancels, and one sincosf and a
+//    reciprocal above.  The reference's test (double)kR > 1e-4 is the same
+//    predicate as kR > 1e-4f (1e-4f is the largest float below 1e-4);
 //  * k-space top-hat: a mode is zeroed when (float)((double)kR * 0.413566994)
 //    > 1, i.e. when kR exceeds the float threshold sharpk_max computed on the
 //    host from that expression;
@@ -169,15 +167,8 @@ __device__ __forceinline__ float filter_weight(int filter_type, float kmag, floa
 {
   float kR = __fmul_rn(kmag, R);
   *zero = false;
-  if (filter_type == 0) {
-    if (kR > 1e-4f) {
-      float s, c;
-      sincosf(kR, &s, &c);
-      const float inv = __fdividef(1.0f, kR);
-      return 3.0f * (s * inv - c) * inv * inv;
-    }
-    return 1.0f;
-  }
+  if (filter_type == 0)
+    return kR > 1e-4f ? tophat_weight(kR) : 1.0f;
   if (filter_type == 1) {
     *zero = kR > sharpk_max;
     return 1.0f;

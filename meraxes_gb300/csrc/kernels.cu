@@ -158,7 +158,7 @@ __global__ void k_filter(const float2* const* __restrict__ in,
         float kR = __fmul_rn(kmag, fb.R[r]);
         if (fb.filter_type == 0) {
           if ((double)kR > 1e-4)
-            w = (float)(3.0 * (double)(__fsub_rn(__fdiv_rn(sinf(kR), powf(kR, 3.0f)), __fdiv_rn(cosf(kR), powf(kR, 2.0f)))));
+            w = tophat_weight(kR);
         } else if (fb.filter_type == 1) {
           kR = (float)((double)kR * 0.413566994);
           zero = kR > 1.0f;

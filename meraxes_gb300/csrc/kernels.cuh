@@ -13,6 +13,31 @@ constexpr int RED_THREADS = 256;
 // ir / D for a non-negative cell index: a 32-bit division while the index
 // fits in 32 bits (every grid up to 1625^3), which costs a fraction of the
 // emulated 64-bit one
+// Real-space top-hat weight W(x) of the filter, x = kR > 1e-4 (reionization.c
+// :2130-2140): the reference's float expression
+// 3 (sinf(x) / powf(x, 3) - cosf(x) / powf(x, 2)).  Both terms are about
+// 1/x^2 and their difference about 1/3, so for small x an ulp of sin, cos or
+// a power becomes about 3/x^2 ulp of W (at the lowest modes of the smallest
+// radii, x ~ 0.01, a relative 1e-3 of W, enough to move near-threshold cells
+// by 1e-4 of their ratio).  Below x = 1 the expression is therefore evaluated
+// as written, with sin and cos computed in double and rounded once to float
+// (the correctly rounded values, which a host libm returns to within its last
+// bit) and x^2, x^3 rounded from double; above, where the amplification is
+// below 3, one sincosf and a reciprocal.
+__device__ __forceinline__ float tophat_weight(float x)
+{
+  if (x < 1.0f) {
+    const double xd = x;
+    const float s = (float)sin(xd), c = (float)cos(xd);
+    const float p3 = (float)(xd * xd * xd), p2 = (float)(xd * xd);
+    return (float)(3.0 * (double)__fsub_rn(__fdiv_rn(s, p3), __fdiv_rn(c, p2)));
+  }
+  float s, c;
+  sincosf(x, &s, &c);
+  const float inv = __fdividef(1.0f, x);
+  return 3.0f * (s * inv - c) * inv * inv;
+}
+
 __device__ __forceinline__ long long row_of(long long ir, int D)
 {
   return ir < 4294967296LL ? (long long)((unsigned)ir / (unsigned)D) : ir / D;
