@@ -7,21 +7,17 @@ Tolerances, from the acceptance rule of the step:
   * ionisation flags may disagree in at most 1e-4 of the cells, and only in
     cells whose threshold margin |f_coll*eff/(nf(1+rec)) - 1| (from the oracle)
     is below 1e-5;
-  * r_bubble, the smallest radius at which a cell passes the test, may
-    disagree in at most 1e-4 of the cells, and only where the smallest margin
-    over all radii is below 1e-4.  A flip at any radius moves it, also in cells
-    ionised at a larger radius whose flags agree, and at small radii the FP32
-    rounding of a 256^3 or larger transform reaches a few 1e-5 of the
-    filtered value in low-valued cells (the reference's FFTW float transforms
-    carry an error of the same size);
+  * r_bubble, the smallest radius at which a cell passes the test, likewise,
+    with the smallest margin over all radii (a flip at any radius moves it,
+    also in cells whose flags agree);
   * T_S, T_K, delta_T and the other grids within 1e-4 relative per cell, with
     an absolute floor of 10 * 2^-24 * log2(N) * max|x| that bounds the rounding
     error of an FP32 FFT of N points (the reference's FFTW single-precision
     path carries an error of the same size); values that depend on the radius
     of first crossing (J_21, Gamma12, N_rec) are compared where that radius
-    agrees: where the first-crossing margin is at least 1e-4, the decision
-    margin of r_bubble.  N_rec, which is updated from Gamma12 through the recombination
-    rate table, also passes on Gamma12's relative difference at the cell.
+    agrees: where the first-crossing margin is at least 1e-5.  N_rec, which
+    is updated from Gamma12 through the recombination rate table, also passes
+    on Gamma12's relative difference at the cell.
 
 The report gives, per grid, the largest relative difference, the cells
 outside tolerance and, as `<grid>_floor_only`, the cells that are inside it
@@ -36,7 +32,6 @@ import numpy as np
 REL_TOL = 1e-5          # REL_TOL of the reference: ionised means xH < 1e-5
 FLAG_FRACTION = 1e-4
 MARGIN = 1e-5
-RBUBBLE_MARGIN = 1e-4
 GRID_RTOL = 1e-4
 XH_ATOL = 1e-4
 
@@ -80,9 +75,9 @@ def compare(ref: Dict[str, np.ndarray], test: Dict[str, np.ndarray], ref_globals
             rep["rbubble_margin_max"] = float(m_all[rb_dis].max())
             rep["rbubble_disagree_above_1e-5"] = int((m_all[rb_dis] >= MARGIN).sum())
             assert rb_dis.sum() <= FLAG_FRACTION * n, f"r_bubble differs in {rb_dis.sum()} of {n} cells"
-            assert np.all(m_all[rb_dis] < RBUBBLE_MARGIN), \
+            assert np.all(m_all[rb_dis] < MARGIN), \
                 f"r_bubble disagreement at margin {m_all[rb_dis].max():.3e} ({rep})"
-        near_first = m_first < RBUBBLE_MARGIN
+        near_first = m_first < MARGIN
     else:
         assert rb_dis.sum() <= FLAG_FRACTION * n, f"r_bubble differs in {rb_dis.sum()} of {n} cells"
         near_first = np.zeros(n, bool)

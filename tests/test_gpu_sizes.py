@@ -4,8 +4,10 @@ The kernels of the fused inverse transforms are compiled per grid size:
 k_fft_x_filter<D, threads>, k_fft_y<D, threads>,
 k_fft_z_threshold<D, spin, recombinations> and k_fft_z_store<D>.  Here the
 <256> builds run against the oracle (the full step of the 256^3 workload, and
-two snapshots of the evolving workload at 256^3 with its own cell size), and
-the <512> builds run the 512^3 workload against the cuFFT path
+two snapshots of the evolving workload at 256^3 with its own cell size); the
+<512> builds run one snapshot of the 512^3 benchmark workload against the
+oracle, through the captured device step the benchmark times, and against the
+cuFFT path
 (MX_TRANSFORM=cufft: cuFFT C2R with filter and threshold kernels that do not
 depend on the grid size and are held to the oracle at small sizes).  At 512^3
 find_HII_bubbles takes two radius batches and mx_step's threshold pass runs in
@@ -133,6 +135,45 @@ def test_evolving_workload_at_256_matches_oracle(tables_dir):
     w = _workload("evolve_512", 256, snapshots=[9, 10])
     reps = _oracle_vs_gpu(w, tables_dir)
     print("evolve_512@256", reps)
+
+
+def test_evolving_workload_512_matches_oracle(tables_dir):
+    """One snapshot of the benchmark workload at its own size (512^3, z =
+    10.26, 41 radii x 5 fields, 40 shells, delta_T) through the path the
+    benchmark times: device grids, the step captured as one CUDA graph, the
+    fused <512> transforms; against the oracle with its margins.  The oracle
+    snapshot takes a few minutes on the host cores and about 60 GB of host
+    memory."""
+    import torch
+
+    from cases import initial
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+    from oracle import OracleBackend
+
+    w = _workload("evolve_512", 512, snapshots=[10])
+    D = w.params.grid_dim
+    orc = OracleBackend(w.params, w.redshifts, tables_dir)
+    s = w.snapshots[0]
+    sa = initial(w, orc.n_sfr_histories)
+    sa.update(syn.FieldGenerator(w).inputs(s, orc.n_sfr_histories))
+    sa.setdefault("delta_T", np.zeros((D, D, D), np.float32))
+    dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in sa.items()}
+    gpu = ReionGridStep(w.params, w.redshifts)
+    gpu.set_graph(True)
+    gb = gpu.step(s, dev)
+    torch.cuda.synchronize()
+    gpu.close()
+    sb = {k: v.cpu().numpy() for k, v in dev.items()}
+    del dev
+    torch.cuda.empty_cache()
+    ga = orc.step(s, sa)
+    margin = orc.margin()
+    orc.close()
+    rep = {}
+    compare(sa, sb, ga, gb, margin=margin, report=rep)
+    rep["means_rel"] = check_means(sb, gb, D, w.params)
+    print("evolve_512 vs oracle", rep)
 
 
 def _run_512(transform, device, inputs, w, monkeypatch):
