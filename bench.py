@@ -37,28 +37,32 @@ METRIC = "ms/snapshot at 512^3 (ComputeTs + find_HII_bubbles + 21cm box)"
 UNIT = "ms/snapshot"
 REION_EFF = 1.0 / 0.15714 * 4000.0 / (1.0 - 0.75 * 0.24)
 FESC = 0.01
-# DRAM bytes (read + write) per algorithmic byte of each kernel.  The x- and
-# y-pass ratios come from a single-pass ncu capture (dram__bytes_read/write)
-# of this workload at 512^3; the others from an `ncu --set full` capture of
-# the same kernels at 256^3 (`python bench.py --grid 256 --steps 1 --warmup 1
-# --no-cpu --no-e2e` with MX_MAX_BATCH_SPECTRA=10).  Each kernel's DRAM
-# traffic grows in proportion to the spectra (or cells) it processes, so
-# traffic per launch at 512^3 is this ratio times the launch's algorithmic
-# bytes.  The transforms also move the row padding of the batch spectra (rows
-# of 144 complex values for 129 at 256^3, 272 for 257 at 512^3):
-# PAD_512_OVER_256 rescales that share of the 256^3 ratios.
+# DRAM bytes (read + write) per algorithmic byte of each kernel, from one
+# `ncu --set full` capture of each kernel at 256^3 (profiles/*_256.md: `python
+# bench.py --grid 256 --steps 2 --warmup 1 --no-cpu --no-e2e --no-adjoint
+# --no-batch --no-plain --no-graph` with MX_MAX_BATCH_SPECTRA=20, one to two
+# launches per kernel).  A kernel's DRAM traffic grows with the spectra (or
+# cells) it processes, so the traffic of a 512^3 launch is the ratio times the
+# launch's algorithmic bytes.  The transforms also move the row padding of
+# the spectra (rows of 144 complex values for 129 at 256^3, 272 for 257 at
+# 512^3): PAD_512_OVER_256 rescales that share of their ratios.  The
+# threshold z-pass also reads the state (xH, z_at_ionization: 8 bytes per
+# cell) at the start of every launch; the algorithmic model counts it once per
+# call, so it is added per launch (THRESHOLD_STATE_BYTES_PER_CELL).
 _C256, _N256 = 256 * 256 * 129, 256 ** 3
 PAD_512_OVER_256 = (272 / 257) / (144 / 129)
-_C512 = 512 * 512 * 257
 DRAM_PER_ALGORITHMIC = {
-    # find_HII_bubbles launch: 5 fields x 2 radii (5 unfiltered spectra read, 10 written)
-    # measured at 512^3 on the 5-field, 40-radius launches
-    "fft_x_filter": (2.93e9 + 114.88e9) / (8 * _C512 * 5 * (1 + 40)),
-    "fft_y": (114.10e9 + 114.02e9) / (16 * _C512 * 200),
-    "fft_z_threshold": 892.79e6 / (8 * _C256 * 10 + 2 * 4 * _N256) * PAD_512_OVER_256,  # 10 spectra + xH, z_at_ion
-    "fft_z_store": 1236.80e6 / ((8 * _C256 + 4 * _N256) * 9),                       # 9 shells
-    "k_evolve": 3084.0e6 / (46 * 4 * _N256),
+    # 5 unfiltered spectra read, 20 written; algorithmic 8 C G (1 + n_radii)
+    "fft_x_filter": (0.377542e9 + 1.452510e9) / (8 * _C256 * 5 * 5) * PAD_512_OVER_256,
+    # 20 spectra read and written; algorithmic 16 C per spectrum
+    "fft_y": (1.509980e9 + 1.447947e9) / (16 * _C256 * 20) * PAD_512_OVER_256,
+    # 20 spectra read (the state read of 8 B per cell taken out)
+    "fft_z_threshold": (1.644234e9 + 3.307264e6 - 8 * _N256) / (8 * _C256 * 20) * PAD_512_OVER_256,
+    # 19 shells: spectra read, shells written
+    "fft_z_store": (1.434571e9 + 1.234466e9) / ((8 * _C256 + 4 * _N256) * 19),
+    "k_evolve": (2.887466e9 + 0.196168e9) / (46 * 4 * _N256),
 }
+THRESHOLD_STATE_BYTES_PER_CELL = 8
 
 
 def parse_args(argv=None):
@@ -387,9 +391,12 @@ def run_gb300(args, rank, world, local):
         name, (n, kms, b) = dom
         achieved = (b / n / 1e9) / (kms / n / 1e3)
         ratio = DRAM_PER_ALGORITHMIC.get(name)
+        traffic = ratio * b / n if ratio else None
+        if traffic and name == "fft_z_threshold":
+            traffic += THRESHOLD_STATE_BYTES_PER_CELL * float(D) ** 3
         roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": hbm_peak,
                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-                    "traffic": round(ratio * b / n) if ratio else None,
+                    "traffic": round(traffic) if traffic else None,
                     "peak_source": peak_src, "algorithmic_bytes_per_launch": b / n}
     # whole-step algorithmic bandwidth
     total_bytes = sum(v[2] for v in kstats.values())

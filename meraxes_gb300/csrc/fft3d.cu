@@ -154,6 +154,30 @@ __device__ __forceinline__ void dft_bwd(float2 (&v)[M])
   dft_stage<M, 1, 0, 0>(v);
 }
 
+// Backward DFT of 3 points, v_k <- sum_n v_n w^{nk} with w = exp(2 pi i / 3)
+// = -1/2 + i sqrt(3)/2: v_0 = a + (b + d), v_{1,2} = a - (b + d)/2 +- i
+// (sqrt(3)/2)(b - d).
+__device__ __forceinline__ void dft3_bwd(float2 (&v)[3])
+{
+  constexpr float s = 0.86602540378443864676f;
+  const float2 a = v[0], t = cadd(v[1], v[2]), u = csub(v[1], v[2]);
+  const float2 m = make_float2(a.x - 0.5f * t.x, a.y - 0.5f * t.y);
+  const float2 su = make_float2(-s * u.y, s * u.x);  // i s u
+  v[0] = cadd(a, t);
+  v[1] = cadd(m, su);
+  v[2] = csub(m, su);
+}
+
+// In-register backward DFT of M points, M a power of two or 3.
+template <int M>
+__device__ __forceinline__ void dft_any(float2 (&v)[M])
+{
+  if constexpr (M == 3)
+    dft3_bwd(v);
+  else
+    dft_bwd<M>(v);
+}
+
 // k-space filter of reionization.c:2110-2170:
 //  * real-space top-hat: tophat_weight (kernels.cuh), the reference's float
 //    expression below kR = 1, where it cancels, and one sincosf and a
@@ -235,9 +259,34 @@ struct Pitch
 template <int D>
 struct Split3;
 template <>
+struct Split3<12>
+{
+  static constexpr int R1 = 4, R2 = 3, R3 = 1;
+};
+template <>
 struct Split3<16>
 {
   static constexpr int R1 = 4, R2 = 2, R3 = 2;
+};
+template <>
+struct Split3<24>
+{
+  static constexpr int R1 = 4, R2 = 2, R3 = 3;
+};
+template <>
+struct Split3<48>
+{
+  static constexpr int R1 = 4, R2 = 4, R3 = 3;
+};
+template <>
+struct Split3<96>
+{
+  static constexpr int R1 = 8, R2 = 4, R3 = 3;
+};
+template <>
+struct Split3<192>
+{
+  static constexpr int R1 = 8, R2 = 8, R3 = 3;
 };
 template <>
 struct Split3<32>
@@ -264,6 +313,20 @@ struct Split3<512>
 {
   static constexpr int R1 = 8, R2 = 8, R3 = 8;
 };
+
+template <int D>
+__host__ __device__ constexpr bool is_pow2()
+{
+  return (D & (D - 1)) == 0;
+}
+// Threads per block of the tile engine for a grid with a factor 3: 24 slots
+// of 16 columns, a multiple of the radix-3 step and of the radix-2/4/8 steps.
+constexpr int TILE_THREADS_3 = 384;
+template <int D>
+constexpr int gen_threads()
+{
+  return is_pow2<D>() ? FFT_THREADS : TILE_THREADS_3;
+}
 
 template <int D>
 struct TilePlan
@@ -330,11 +393,11 @@ struct TileSteps
 #pragma unroll
         for (int n1 = 0; n1 < R1; n1++)
           v[n1] = load(np + M * n1, t, j * R1 + n1);
-        dft_bwd<R1>(v);
+        dft_any<R1>(v);
         col[np * TXC] = v[0];
 #pragma unroll
         for (int k1 = 1; k1 < R1; k1++)
-          col[(k1 * M + np) * TXC] = cmul(v[k1], tw[(np * k1) & (D - 1)]);
+          col[(k1 * M + np) * TXC] = cmul(v[k1], tw[(np * k1) % D]);
       }
     }
   }
@@ -354,11 +417,11 @@ struct TileSteps
 #pragma unroll
         for (int n2 = 0; n2 < R2; n2++)
           v[n2] = line[R3 * n2 * TXC];
-        dft_bwd<R2>(v);
+        dft_any<R2>(v);
         line[0] = v[0];
 #pragma unroll
         for (int k2 = 1; k2 < R2; k2++)
-          line[R3 * k2 * TXC] = cmul(v[k2], tw[(R1 * n3 * k2) & (D - 1)]);
+          line[R3 * k2 * TXC] = cmul(v[k2], tw[(R1 * n3 * k2) % D]);
       }
     }
   }
@@ -380,7 +443,7 @@ struct TileSteps
 #pragma unroll
         for (int n3 = 0; n3 < R3; n3++)
           v[n3] = line[n3 * TXC];
-        dft_bwd<R3>(v);
+        dft_any<R3>(v);
 #pragma unroll
         for (int k3 = 0; k3 < R3; k3++)
           store(k1 + R1 * (k2 + R2 * k3), t, v[k3]);
@@ -883,8 +946,10 @@ constexpr int ST_RB_SHIFT = 8;       // radius index of the last ionising radius
 // SPIN and RECOMB fix the fields at compile time: deltax, stars,
 // weighted_sfr, then x_e with the spin temperature, then N_rec with
 // recombinations (the order find_HII_bubbles transforms them in).
-template <int D, bool SPIN, bool RECOMB>
-__global__ void __launch_bounds__(FFT_THREADS, 2) k_fft_z_threshold(ZThresholdArgs a)
+// MINB: resident blocks per SM the registers are budgeted for (2: 128
+// registers; 3: 80, with a few spills); the context picks one.
+template <int D, bool SPIN, bool RECOMB, int MINB>
+__global__ void __launch_bounds__(FFT_THREADS, MINB) k_fft_z_threshold(ZThresholdArgs a)
 {
   using P = ZPlan<D>;
   constexpr int G = 3 + (SPIN ? 1 : 0) + (RECOMB ? 1 : 0);
@@ -1107,8 +1172,8 @@ struct FwdZPlan
   static constexpr size_t BYTES = sizeof(float2) * (size_t)(OFF_ROWS + FWD_ROWS * H);
 };
 
-template <int D>
-__global__ void __launch_bounds__(FFT_THREADS) k_fft_z_r2c(const __grid_constant__ FwdArgs a)
+template <int D, int T>
+__global__ void __launch_bounds__(T) k_fft_z_r2c(const __grid_constant__ FwdArgs a)
 {
   using P = FwdZPlan<D>;
   constexpr int L = P::L, H = P::H, HP = P::HP;
@@ -1123,29 +1188,29 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_z_r2c(const __grid_constant
   // the 16 padded rows are contiguous: FWD_ROWS * H float2, all of a
   // thread's loads in flight while the twiddle tables are filled
   const float2* __restrict__ src = reinterpret_cast<const float2*>(a.src[g]) + r0 * H;
-  constexpr int NV = (FWD_ROWS * H + FFT_THREADS - 1) / FFT_THREADS;
+  constexpr int NV = (FWD_ROWS * H + T - 1) / T;
   float2 v[NV];
 #pragma unroll
   for (int j = 0; j < NV; j++) {
-    const int i = threadIdx.x + j * FFT_THREADS;
+    const int i = threadIdx.x + j * T;
     if (i < FWD_ROWS * H)
       v[j] = __ldg(src + i);
   }
   fill_twiddles<L>(tw);
-  for (int k = threadIdx.x; k < H; k += FFT_THREADS) {
+  for (int k = threadIdx.x; k < H; k += T) {
     float sn, cs;
     sincospif(2.0f * (float)k / (float)D, &sn, &cs);
     post[k] = make_float2(cs, -sn);
   }
 #pragma unroll
   for (int j = 0; j < NV; j++) {
-    const int i = threadIdx.x + j * FFT_THREADS;
+    const int i = threadIdx.x + j * T;
     if (i < FWD_ROWS * H)
       rows[i] = v[j];
   }
   __syncthreads();
   // forward DFT of each row's L points: conj in, backward engine, conj out
-  tile_dft<L, FFT_THREADS>(
+  tile_dft<L, T>(
     tile, tw,
     [&](int n, int t, int) {
       const float2 v = rows[t * H + n];
@@ -1154,7 +1219,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_z_r2c(const __grid_constant
     [&](int k, int t, float2 v) { rows[t * H + k] = make_float2(v.x, -v.y); });
   __syncthreads();
   float2* __restrict__ dst = a.out + (long long)g * a.C + r0 * HP;
-  for (int i = threadIdx.x; i < FWD_ROWS * HP; i += FFT_THREADS) {
+  for (int i = threadIdx.x; i < FWD_ROWS * HP; i += T) {
     const int t = i / HP, k = i - t * HP;
     float2 X = make_float2(0.f, 0.f);
     if (k < H) {
@@ -1199,6 +1264,234 @@ __global__ void __launch_bounds__(T, T == 256 ? 3 : 2) k_fft_fwd_cols(float2* da
   TS::c(buf, [&](int y, int, float2 v) { col[y * LINE] = make_float2(v.x, -v.y); });
 }
 
+
+// ------------------------------------------ z-pass for grids with a factor 3
+// D = 24, 48, 96, 192.  A block of TILE_THREADS_3 threads owns 16 rows
+// (row = x * D + y) and, per spectrum, reads the rows (HP complex values each)
+// with coalesced loads into shared memory, forms the D/2-point complex
+// sequence Z_k = E_k + i O_k with E_k = X_k + conj X_{D/2-k} and O_k =
+// (X_k - conj X_{D/2-k}) w_D^k (the imaginary parts of X_0 and X_{D/2}
+// ignored, FFTW c2r), transforms it with the tile engine (16 rows = the 16
+// columns of a tile) and keeps x_2m = Re z_m, x_2m+1 = Im z_m of every row in
+// shared memory.  The consumer then reads the real rows in cell order.  Shared
+// rows are padded to an odd number of words, so that the 16 rows of one tile
+// column fall on distinct banks.
+namespace {
+constexpr int ZG_ROWS = TXC;
+}
+
+template <int D>
+struct ZGPlan
+{
+  static constexpr int L = D / 2, H = D / 2 + 1, HP = Pitch<D>::HP;
+  static constexpr int RP = HP + 1;  // float2 row pitch of the staged rows
+  static constexpr int RD = D + 1;   // float row pitch of the real rows
+  static constexpr int OFF_TW = 0, OFF_POST = L, OFF_TILE = OFF_POST + L, OFF_ROWS = OFF_TILE + L * TXC;
+  static constexpr int END2 = OFF_ROWS + ZG_ROWS * RP;  // float2
+  static constexpr int REAL = ZG_ROWS * RD;              // floats per field
+  static constexpr size_t bytes(int fields) { return sizeof(float2) * (size_t)END2 + sizeof(float) * (size_t)fields * REAL; }
+};
+
+// Twiddles of the engine (length L) and w_D^k, k < L.
+template <int D>
+__device__ __forceinline__ void zg_tables(float2* s2)
+{
+  using P = ZGPlan<D>;
+  fill_twiddles<P::L>(s2 + P::OFF_TW);
+  for (int k = threadIdx.x; k < P::L; k += TILE_THREADS_3) {
+    float sn, cs;
+    sincospif(2.0f * (float)k / (float)D, &sn, &cs);
+    s2[P::OFF_POST + k] = make_float2(cs, sn);
+  }
+}
+
+// C2R along z of the 16 rows starting at row0 of one spectrum into real
+// (16 rows of RD floats).  Starts and ends with a block barrier.
+template <int D>
+__device__ void zg_c2r(const float2* __restrict__ spectrum, long long row0, float2* s2, float* real)
+{
+  using P = ZGPlan<D>;
+  constexpr int L = P::L, HP = P::HP, RP = P::RP, RD = P::RD;
+  float2* rows = s2 + P::OFF_ROWS;
+  const float2* post = s2 + P::OFF_POST;
+  const float2* __restrict__ src = spectrum + row0 * HP;
+  __syncthreads();  // the previous consumer of rows / real is done
+  for (int i = threadIdx.x; i < ZG_ROWS * HP; i += TILE_THREADS_3) {
+    const int t = i / HP;
+    rows[t * RP + (i - t * HP)] = __ldg(src + i);
+  }
+  __syncthreads();
+  tile_dft<L, TILE_THREADS_3>(
+    s2 + P::OFF_TILE, s2 + P::OFF_TW,
+    [&](int k, int t, int) {
+      float2 A = rows[t * RP + k];
+      float2 B = rows[t * RP + (L - k)];
+      if (k == 0) {
+        A.y = 0.0f;
+        B.y = 0.0f;
+      }
+      B.y = -B.y;
+      const float2 E = cadd(A, B);
+      const float2 O = cmul(csub(A, B), post[k]);
+      return make_float2(E.x - O.y, E.y + O.x);
+    },
+    [&](int m, int t, float2 v) {
+      real[t * RD + 2 * m] = v.x;
+      real[t * RD + 2 * m + 1] = v.y;
+    });
+  __syncthreads();
+}
+
+// The per-cell test of find_HII_bubbles (find_HII_bubbles.c:342-428) on the
+// clamped values of one cell: FP32 with the FP64 decision within 4e-6 of
+// threshold, as in k_fft_z_threshold.
+template <bool SPIN, bool RECOMB>
+__device__ __forceinline__ bool zg_test(float dx, float stv, float nr, float xe, const RadiusParams& rp,
+                                        double pixel_volume, double eff, float* xpart)
+{
+  const float inv_dom = __fdividef(1.0f, 1.0f + dx);
+  const float lhs_f = stv * rp.kfc * inv_dom;
+  const float nf_f = 1.0f - xe;
+  const float rhs_f = nf_f * (1.0f + nr * inv_dom);
+  if (fabsf(lhs_f - rhs_f) > 4e-6f * fmaxf(lhs_f, rhs_f)) {
+    *xpart = nf_f - lhs_f;
+    return lhs_f > rhs_f;
+  }
+  return threshold_fp64(dx, stv, nr, xe, RECOMB, SPIN, rp.M_mean, rp.R_cubed, pixel_volume, eff, xpart);
+}
+
+// z-pass fused with the per-cell test for grids with a factor 3: every field
+// of a radius is transformed into shared memory, then each thread tests its
+// cells (cell c = threadIdx.x + j * TILE_THREADS_3 of the block's 16 rows).
+// Same state, bookkeeping and stores as k_fft_z_threshold.
+template <int D, bool SPIN, bool RECOMB>
+__global__ void __launch_bounds__(TILE_THREADS_3) k_fft_z_threshold_gen(const __grid_constant__ ZThresholdArgs a)
+{
+  using P = ZGPlan<D>;
+  constexpr int G = 3 + (SPIN ? 1 : 0) + (RECOMB ? 1 : 0);
+  constexpr int IXE = 3, INR = SPIN ? 4 : 3;
+  constexpr int CELLS = ZG_ROWS * D, CPT = (CELLS + TILE_THREADS_3 - 1) / TILE_THREADS_3;
+  extern __shared__ __align__(16) unsigned char zgsm[];
+  float2* s2 = reinterpret_cast<float2*>(zgsm);
+  float* real = reinterpret_cast<float*>(zgsm + sizeof(float2) * P::END2);
+  zg_tables<D>(s2);
+  const long long row0 = ((long long)blockIdx.x + a.group0) * ZG_ROWS;
+  unsigned st[CPT];
+#pragma unroll
+  for (int j = 0; j < CPT; j++) {
+    const int c = threadIdx.x + j * TILE_THREADS_3;
+    st[j] = 0;
+    if (c < CELLS) {
+      const long long ir = row0 * D + c;
+      const float x0 = a.xH[ir], z0 = a.z_at_ion[ir];
+      st[j] = (x0 > REL_TOL_F ? ST_XHIGH : 0u) | (x0 < REL_TOL_F ? ST_XLOW : 0u) | (z0 < 0 ? ST_ZUNSET : 0u);
+    }
+  }
+  for (int r = 0; r < a.n_r; r++) {
+    const RadiusParams rp = a.rp[r];
+    const bool direct = rp.last != 0;
+    if (!direct) {
+      for (int g = 0; g < G; g++)
+        zg_c2r<D>(a.spectra + (long long)(r * G + g) * a.C, row0, s2, real + g * P::REAL);
+    }
+#pragma unroll
+    for (int j = 0; j < CPT; j++) {
+      const int c = threadIdx.x + j * TILE_THREADS_3;
+      if (c >= CELLS)
+        continue;
+      const int t = c / D, z = c - t * D;
+      const long long ir = row0 * D + c;
+      float f[G];
+#pragma unroll
+      for (int g = 0; g < G; g++)
+        f[g] = direct ? a.direct[g][(row0 + t) * 2LL * P::H + z] : real[g * P::REAL + t * P::RD + z];
+      const float dx = fmaxf(f[0], -1 + REL_TOL_F);
+      float stv = fmaxf(f[1], 0.0f);
+      if (stv < ABS_TOL_F)
+        stv = 0;
+      float nr = 0.0f, xe = 0.0f;
+      if constexpr (RECOMB) {
+        nr = fmaxf(f[INR], 0.0f);
+        if (nr < ABS_TOL_F)
+          nr = 0;
+      }
+      if constexpr (SPIN) {
+        xe = fmaxf(f[IXE], 0.0f);
+        if (xe < ABS_TOL_F)
+          xe = 0;
+        xe = fminf(xe, 0.999f);
+      }
+      float xpart;
+      const bool ionised = zg_test<SPIN, RECOMB>(dx, stv, nr, xe, rp, a.pixel_volume, a.eff, &xpart);
+      unsigned s = st[j];
+      const bool xr_high = !(s & ST_ION) && (s & ST_XHIGH);
+      bool xr_low = (s & ST_ION) || (s & ST_XLOW);
+      bool first_ion = false, first_z = false;
+      if (ionised) {
+        first_ion = xr_high;
+        s = (s & ((1u << ST_RB_SHIFT) - 1)) | ST_ION | ((unsigned)r << ST_RB_SHIFT);
+        xr_low = true;
+      } else if (rp.last && xr_high) {
+        const float xn = fminf(fmaxf(xpart, 0.0f), 1.0f);
+        a.xH[ir] = xn;
+        xr_low = xn < REL_TOL_F;
+      }
+      if (xr_low && (s & ST_ZUNSET)) {
+        a.z_at_ion[ir] = (float)a.redshift;
+        first_z = true;
+        s &= ~ST_ZUNSET;
+      }
+      st[j] = s;
+      if ((a.uvb || RECOMB) && (first_ion || (a.uvb && first_z))) {
+        float ws = fmaxf(f[2], 0.0f);
+        if (ws < ABS_TOL_F)
+          ws = 0;
+        const float J21_aux = a.uvb ? ws * rp.kj : 0.0f;
+        if (first_ion) {
+          if (a.uvb)
+            a.J21[ir] = J21_aux;
+          if (RECOMB)
+            a.Gamma12[ir] = ws * rp.kg;
+        }
+        if (a.uvb && first_z)
+          a.J21_at_ion[ir] = J21_aux * a.gamma_halo_bias;
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < CPT; j++) {
+    const int c = threadIdx.x + j * TILE_THREADS_3;
+    if (c < CELLS && (st[j] & ST_ION)) {
+      const long long ir = row0 * D + c;
+      a.xH[ir] = 0.0f;
+      a.r_bubble[ir] = (float)a.rp[st[j] >> ST_RB_SHIFT].R;
+    }
+  }
+}
+
+// Clamped store of ComputeTs shells for grids with a factor 3 (as
+// k_fft_z_store): shells[(r0 + r) * N + cell] = max(value, 0).
+template <int D>
+__global__ void __launch_bounds__(TILE_THREADS_3) k_fft_z_store_gen(const float2* spectra, long long C, int n, int r0,
+                                                                     float* shells, long long N)
+{
+  using P = ZGPlan<D>;
+  constexpr int CELLS = ZG_ROWS * D;
+  extern __shared__ __align__(16) unsigned char zgsm[];
+  float2* s2 = reinterpret_cast<float2*>(zgsm);
+  float* real = reinterpret_cast<float*>(zgsm + sizeof(float2) * P::END2);
+  zg_tables<D>(s2);
+  const long long row0 = (long long)blockIdx.x * ZG_ROWS;
+  for (int r = 0; r < n; r++) {
+    zg_c2r<D>(spectra + (long long)r * C, row0, s2, real);
+    float* dst = shells + (long long)(r0 + r) * N + row0 * D;
+    for (int c = threadIdx.x; c < CELLS; c += TILE_THREADS_3) {
+      const int t = c / D;
+      dst[c] = fmaxf(real[t * P::RD + (c - t * D)], 0.0f);
+    }
+  }
+}
+
 // ------------------------------------------------- adjoint filter (k-space)
 // acc = (first ? 0 : acc) + W(|k| R) * scale * U over a half spectrum [D][D][D/2+1]
 // with the weights of the x-pass (the filtered shells are a real, symmetric
@@ -1229,7 +1522,13 @@ __global__ void k_filter_accumulate(float2* __restrict__ acc, const float2* __re
 }
 
 // ----------------------------------------------------------------- launch
-bool fft3d_supported(int D) { return D == 32 || D == 64 || D == 128 || D == 256 || D == 512; }
+// powers of two from 32 to 512, and 3 x 8, 3 x 16, 3 x 32, 3 x 64 (radix-3
+// tile steps, the 384-thread engine and the factor-3 z-pass)
+static bool fft3d_factor3(int D) { return D == 24 || D == 48 || D == 96 || D == 192; }
+bool fft3d_supported(int D)
+{
+  return D == 32 || D == 64 || D == 128 || D == 256 || D == 512 || fft3d_factor3(D);
+}
 
 int fft_pitch(int D) { return (D / 2 + 1 + TXC - 1) / TXC * TXC; }
 
@@ -1275,13 +1574,22 @@ static void launch_y(float2* data, long long C, int n_spectra, int threads, cuda
   else
     launch_y_t<D, 256>(data, C, n_spectra, s);
 }
+template <int D, bool SPIN, bool RECOMB, int MINB>
+static void launch_zt_minb(const ZThresholdArgs& a, cudaStream_t s)
+{
+  const size_t bytes = ZPlan<D>::BYTES;
+  cudaFuncSetAttribute(k_fft_z_threshold<D, SPIN, RECOMB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)bytes);
+  const int groups = a.n_groups > 0 ? a.n_groups : D * D / ZPlan<D>::TZ;
+  k_fft_z_threshold<D, SPIN, RECOMB, MINB><<<groups, FFT_THREADS, bytes, s>>>(a);
+}
 template <int D, bool SPIN, bool RECOMB>
 static void launch_zt_cfg(const ZThresholdArgs& a, cudaStream_t s)
 {
-  const size_t bytes = ZPlan<D>::BYTES;
-  cudaFuncSetAttribute(k_fft_z_threshold<D, SPIN, RECOMB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  const int groups = a.n_groups > 0 ? a.n_groups : D * D / ZPlan<D>::TZ;
-  k_fft_z_threshold<D, SPIN, RECOMB><<<groups, FFT_THREADS, bytes, s>>>(a);
+  if (a.blocks_per_sm == 3)
+    launch_zt_minb<D, SPIN, RECOMB, 3>(a, s);
+  else
+    launch_zt_minb<D, SPIN, RECOMB, 2>(a, s);
 }
 template <int D>
 static void launch_zt(const ZThresholdArgs& a, cudaStream_t s)
@@ -1332,6 +1640,10 @@ bool launch_fft_x_filter(int D, const XPassArgs& args, int threads, cudaStream_t
     case 128: launch_x<128>(a, threads, s); break;
     case 256: launch_x<256>(a, threads, s); break;
     case 512: launch_x<512>(a, threads, s); break;
+    case 24: launch_x_t<24, TILE_THREADS_3>(a, s); break;
+    case 48: launch_x_t<48, TILE_THREADS_3>(a, s); break;
+    case 96: launch_x_t<96, TILE_THREADS_3>(a, s); break;
+    case 192: launch_x_t<192, TILE_THREADS_3>(a, s); break;
     default: return false;
   }
   fft_launches++;
@@ -1346,13 +1658,17 @@ bool launch_fft_y(int D, float2* data, long long C, int n_spectra, int threads, 
     case 128: launch_y<128>(data, C, n_spectra, threads, s); break;
     case 256: launch_y<256>(data, C, n_spectra, threads, s); break;
     case 512: launch_y<512>(data, C, n_spectra, threads, s); break;
+    case 24: launch_y_t<24, TILE_THREADS_3>(data, C, n_spectra, s); break;
+    case 48: launch_y_t<48, TILE_THREADS_3>(data, C, n_spectra, s); break;
+    case 96: launch_y_t<96, TILE_THREADS_3>(data, C, n_spectra, s); break;
+    case 192: launch_y_t<192, TILE_THREADS_3>(data, C, n_spectra, s); break;
     default: return false;
   }
   fft_launches++;
   return true;
 }
 
-int fft_z_rows_per_group(int D) { return 2048 / D; }
+int fft_z_rows_per_group(int D) { return fft3d_factor3(D) ? ZG_ROWS : 2048 / D; }
 
 template <int D, int T, int AXIS>
 static void launch_fwd_cols_t(float2* data, long long C, int n, cudaStream_t s)
@@ -1365,10 +1681,13 @@ template <int D>
 static void launch_fwd(const FwdArgs& a, int threads, cudaStream_t s)
 {
   const size_t bytes = FwdZPlan<D>::BYTES;
-  cudaFuncSetAttribute(k_fft_z_r2c<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaFuncSetAttribute(k_fft_z_r2c<D, gen_threads<D>()>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   const long long blocks = (long long)a.G * D * D / FWD_ROWS;
-  k_fft_z_r2c<D><<<(unsigned)blocks, FFT_THREADS, bytes, s>>>(a);
-  if (threads == 512) {
+  k_fft_z_r2c<D, gen_threads<D>()><<<(unsigned)blocks, gen_threads<D>(), bytes, s>>>(a);
+  if constexpr (!is_pow2<D>()) {
+    launch_fwd_cols_t<D, TILE_THREADS_3, 1>(a.out, a.C, a.G, s);
+    launch_fwd_cols_t<D, TILE_THREADS_3, 0>(a.out, a.C, a.G, s);
+  } else if (threads == 512) {
     launch_fwd_cols_t<D, 512, 1>(a.out, a.C, a.G, s);
     launch_fwd_cols_t<D, 512, 0>(a.out, a.C, a.G, s);
   } else {
@@ -1387,12 +1706,41 @@ bool launch_fft_forward(int D, const FwdArgs& a, int threads, cudaStream_t s)
     case 128: launch_fwd<128>(a, threads, s); break;
     case 256: launch_fwd<256>(a, threads, s); break;
     case 512: launch_fwd<512>(a, threads, s); break;
+    case 24: launch_fwd<24>(a, threads, s); break;
+    case 48: launch_fwd<48>(a, threads, s); break;
+    case 96: launch_fwd<96>(a, threads, s); break;
+    case 192: launch_fwd<192>(a, threads, s); break;
     default: return false;
   }
   fft_launches += 3;
   return true;
 }
 int fft_z_row_groups(int D) { return D * D / fft_z_rows_per_group(D); }
+
+template <int D, bool SPIN, bool RECOMB>
+static void launch_ztg_cfg(const ZThresholdArgs& a, cudaStream_t s)
+{
+  const size_t bytes = ZGPlan<D>::bytes(3 + (SPIN ? 1 : 0) + (RECOMB ? 1 : 0));
+  cudaFuncSetAttribute(k_fft_z_threshold_gen<D, SPIN, RECOMB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)bytes);
+  const int groups = a.n_groups > 0 ? a.n_groups : D * D / ZG_ROWS;
+  k_fft_z_threshold_gen<D, SPIN, RECOMB><<<groups, TILE_THREADS_3, bytes, s>>>(a);
+}
+template <int D>
+static void launch_ztg(const ZThresholdArgs& a, cudaStream_t s)
+{
+  if (a.spin)
+    a.recomb ? launch_ztg_cfg<D, true, true>(a, s) : launch_ztg_cfg<D, true, false>(a, s);
+  else
+    a.recomb ? launch_ztg_cfg<D, false, true>(a, s) : launch_ztg_cfg<D, false, false>(a, s);
+}
+template <int D>
+static void launch_zsg(const float2* spectra, long long C, int n, int r0, float* shells, long long N, cudaStream_t s)
+{
+  const size_t bytes = ZGPlan<D>::bytes(1);
+  cudaFuncSetAttribute(k_fft_z_store_gen<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_fft_z_store_gen<D><<<D * D / ZG_ROWS, TILE_THREADS_3, bytes, s>>>(spectra, C, n, r0, shells, N);
+}
 
 bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s)
 {
@@ -1409,6 +1757,10 @@ bool launch_fft_z_threshold(int D, const ZThresholdArgs& a, cudaStream_t s)
     case 128: launch_zt<128>(a, s); break;
     case 256: launch_zt<256>(a, s); break;
     case 512: launch_zt<512>(a, s); break;
+    case 24: launch_ztg<24>(a, s); break;
+    case 48: launch_ztg<48>(a, s); break;
+    case 96: launch_ztg<96>(a, s); break;
+    case 192: launch_ztg<192>(a, s); break;
     default: return false;
   }
   fft_launches++;
@@ -1424,6 +1776,10 @@ bool launch_fft_z_store(int D, const float2* spectra, long long C, int n, int r0
     case 128: launch_zs<128>(spectra, C, n, r0, shells, N, err, s); break;
     case 256: launch_zs<256>(spectra, C, n, r0, shells, N, err, s); break;
     case 512: launch_zs<512>(spectra, C, n, r0, shells, N, err, s); break;
+    case 24: launch_zsg<24>(spectra, C, n, r0, shells, N, s); break;
+    case 48: launch_zsg<48>(spectra, C, n, r0, shells, N, s); break;
+    case 96: launch_zsg<96>(spectra, C, n, r0, shells, N, s); break;
+    case 192: launch_zsg<192>(spectra, C, n, r0, shells, N, s); break;
     default: return false;
   }
   fft_launches++;

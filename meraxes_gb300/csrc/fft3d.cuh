@@ -57,6 +57,8 @@ struct ZThresholdArgs
   // row groups [group0, group0 + n_groups) of fft_z_row_groups(D) (n_groups
   // 0: all), so that a launch can cover a slab of rows
   int group0 = 0, n_groups = 0;
+  // register budget of the launch: 2 or 3 resident blocks per SM
+  int blocks_per_sm = 2;
 };
 
 bool fft3d_supported(int D);

@@ -88,6 +88,8 @@ struct mx_ctx
   bool fused_fft = false;
   // threads per block of the fused x- and y-pass, chosen by tune_fft()
   int x_threads = 512, y_threads = 256;
+  // register budget of the threshold z-pass: 2 or 3 resident blocks per SM
+  int z_blocks = 2;
   // 2-D tensor map of d_shells (cells x shells) for the evolve kernel's tile
   // copies (make_shell_map), when one applies
   bulk::TensorMap shell_map{};
@@ -623,6 +625,7 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
       za.recomb = recomb;
       za.spin = spin;
       za.err = c->d_err;
+      za.blocks_per_sm = c->z_blocks;
       // spectra read once, unfiltered last step read once, and the per-call
       // state (xH, z_at_ionization read and written; r_bubble, J_21,
       // J_21_at_ionization, Gamma12 written) counted with the first batch
@@ -2347,6 +2350,12 @@ static void tune_fft(mx_ctx* c)
     const int t = v ? std::atoi(v) : 0;
     return (t == 256 || t == 512) ? t : 0;
   };
+  if (c->fused_fft && (c->gd.D & (c->gd.D - 1)) != 0) {
+    // grids with a factor 3 run one block size (384 threads: 24 slots of 16
+    // columns, a multiple of the radix-3 and radix-2/4/8 steps)
+    c->x_threads = c->y_threads = 384;
+    return;
+  }
   const int fx = env_threads("MX_XPASS_THREADS"), fy = env_threads("MX_YPASS_THREADS");
   if (fx)
     c->x_threads = fx;
@@ -2445,6 +2454,8 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
   c->nthreads = std::max(1, std::min(64, hw_threads()));
   if (const char* env = std::getenv("MX_HOST_THREADS"))
     c->nthreads = std::max(1, std::atoi(env));
+  if (const char* env = std::getenv("MX_ZPASS_BLOCKS"))
+    c->z_blocks = std::atoi(env) == 3 ? 3 : 2;
   c->fused_fft = fft3d_supported(p.grid_dim);
   if (const char* env = std::getenv("MX_TRANSFORM"))
     if (std::string(env) == "cufft")

@@ -79,11 +79,14 @@ def test_gpu_matches_oracle_with_margins(name, D, tables_dir):
     print(name, D, _run_against_oracle(name, D, tables_dir))
 
 
-# Power-of-two grids run the fused three-pass inverse transforms by default;
-# MX_TRANSFORM=cufft selects cuFFT C2R with separate filter and test passes.
-# Both must meet the same tolerances against the oracle.
+# Power-of-two grids from 32^3 and the grids 24^3, 48^3, 96^3 and 192^3 (a
+# factor 3: radix-3 tile steps and the factor-3 z-pass) run the fused
+# transforms by default; MX_TRANSFORM=cufft selects cuFFT C2R with separate
+# filter and test passes.  Both must meet the same tolerances against the
+# oracle.
 @pytest.mark.parametrize("transform", ["fused", "cufft"])
-@pytest.mark.parametrize("name,D", [("full24", 64), ("plain32_gauss", 64), ("evolve16", 32)])
+@pytest.mark.parametrize("name,D", [("full24", 64), ("plain32_gauss", 64), ("evolve16", 32),
+                                    ("full24", 96), ("plain32_sharpk", 48), ("evolve16", 24)])
 def test_both_transform_paths_match_oracle(name, D, transform, tables_dir, monkeypatch):
     monkeypatch.setenv("MX_TRANSFORM", transform)
     print(name, D, transform, _run_against_oracle(name, D, tables_dir))
@@ -163,7 +166,8 @@ def test_shell_map_gives_identical_results(name, D, monkeypatch):
 # the work buffer; at 512^3 find_HII_bubbles takes two.  Small batches
 # (MX_MAX_BATCH_SPECTRA) must give the same grids as one batch, bit for bit.
 @pytest.mark.parametrize("transform", ["fused", "cufft"])
-@pytest.mark.parametrize("name,D,spectra", [("full24", 64, 15), ("plain32_tophat", 64, 6), ("evolve16", 32, 10)])
+@pytest.mark.parametrize("name,D,spectra", [("full24", 64, 15), ("plain32_tophat", 64, 6), ("evolve16", 32, 10),
+                                            ("full24", 48, 15)])
 def test_radius_batches_give_identical_results(name, D, spectra, transform, monkeypatch):
     from cases import initial
     from meraxes_gb300 import synthetic as syn
