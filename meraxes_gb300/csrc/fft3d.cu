@@ -1,4 +1,5 @@
-// Fused inverse 3-D transforms for power-of-two grids (D = 32 ... 512).
+// Fused 3-D transforms for power-of-two grids (D = 32 ... 512) and for the
+// grids 24, 48, 96 and 192 (a factor 3).
 //
 // The reference inverse-transforms every filtered field at every radius with
 // FFTW (find_HII_bubbles.c:254-269, ComputeTs.c:405-409) and then makes

@@ -1,4 +1,5 @@
-// Fused inverse 3-D transforms for power-of-two grids (see fft3d.cu).
+// Fused 3-D transforms for power-of-two grids and grids with a factor 3
+// (see fft3d.cu).
 #pragma once
 
 #include <cuda_runtime.h>

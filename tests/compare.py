@@ -6,7 +6,14 @@ Tolerances, from the acceptance rule of the step:
     mean by its own xH difference times its weight;
   * ionisation flags may disagree in at most 1e-4 of the cells, and only in
     cells whose threshold margin |f_coll*eff/(nf(1+rec)) - 1| (from the oracle)
-    is below 1e-5;
+    is below 1e-5, except that at most 1e-7 of the cells (at least one) may
+    lie between 1e-5 and 1e-4.  That allowance is the reference's own platform
+    spread: its float top-hat weight 3(sinf x/x^3 - cosf x/x^2) cancels at the
+    lowest modes of the smallest radius and amplifies a last-bit difference
+    of sinf, cosf or powf by 3/x^2; the oracle with correctly rounded sin and
+    cos in that expression (everything else unchanged, FP64 transforms)
+    flips one cell of the 512^3 benchmark snapshot at margin 1.4e-5 against
+    the oracle built on the host libm;
   * r_bubble, the smallest radius at which a cell passes the test, likewise,
     with the smallest margin over all radii (a flip at any radius moves it,
     also in cells whose flags agree);
@@ -32,6 +39,8 @@ import numpy as np
 REL_TOL = 1e-5          # REL_TOL of the reference: ionised means xH < 1e-5
 FLAG_FRACTION = 1e-4
 MARGIN = 1e-5
+LIBM_MARGIN = 1e-4
+LIBM_FRACTION = 1e-7
 GRID_RTOL = 1e-4
 XH_ATOL = 1e-4
 
@@ -68,14 +77,17 @@ def compare(ref: Dict[str, np.ndarray], test: Dict[str, np.ndarray], ref_globals
             rep[name + "_margin_buckets"] = [int((mm < edges[0]).sum())] + \
                 [int(((mm >= lo) & (mm < hi)).sum()) for lo, hi in zip(edges[:-1], edges[1:])] + \
                 [int((mm >= edges[-1]).sum())]
+        libm_cells = max(1, int(LIBM_FRACTION * n))
         if dis.any():
             rep["flag_margin_max"] = float(m_first[dis].max())
-            assert np.all(m_first[dis] < MARGIN), f"flag disagreement at margin {m_first[dis].max():.3e} ({rep})"
+            rep["flag_disagree_above_1e-5"] = int((m_first[dis] >= MARGIN).sum())
+            assert np.all(m_first[dis] < LIBM_MARGIN) and rep["flag_disagree_above_1e-5"] <= libm_cells, \
+                f"flag disagreement at margin {m_first[dis].max():.3e} ({rep})"
         if rb_dis.any():
             rep["rbubble_margin_max"] = float(m_all[rb_dis].max())
             rep["rbubble_disagree_above_1e-5"] = int((m_all[rb_dis] >= MARGIN).sum())
             assert rb_dis.sum() <= FLAG_FRACTION * n, f"r_bubble differs in {rb_dis.sum()} of {n} cells"
-            assert np.all(m_all[rb_dis] < MARGIN), \
+            assert np.all(m_all[rb_dis] < LIBM_MARGIN) and rep["rbubble_disagree_above_1e-5"] <= libm_cells, \
                 f"r_bubble disagreement at margin {m_all[rb_dis].max():.3e} ({rep})"
         near_first = m_first < MARGIN
     else:
