@@ -206,6 +206,17 @@ typedef struct mx_batch_item
 typedef struct mx_batch mx_batch;
 int mx_batch_create(const char* tables_dir, int32_t max_workers, size_t max_work_bytes, mx_batch** out);
 int mx_batch_run(mx_batch* batch, mx_batch_item* items, int32_t n_items);
+/* The same items as ONE CUDA graph, launched once: every item has its own
+ * context (kept between runs while its position's configuration stays the
+ * same, with the per-box history cleared); one capture puts each item's
+ * host->device copies, its step (ComputeTs -> find_HII_bubbles -> 21cm box,
+ * with the frequency tables built by a host node) and its device->host copies
+ * on a branch of the graph, and a single cudaGraphLaunch runs every box.  The
+ * host grids must be page-locked (cudaHostAlloc / cudaHostRegister), as the
+ * graph's copy nodes need pinned memory; other grids return MX_EINVAL.
+ * Results equal those of mx_step per box.  No reference counterpart (the
+ * reference runs one box per MPI job). */
+int mx_batch_run_graph(mx_batch* batch, mx_batch_item* items, int32_t n_items);
 void mx_batch_destroy(mx_batch* batch);
 const char* mx_batch_last_error(const mx_batch* batch);
 const char* mx_last_error(const mx_ctx* ctx); /* ctx may be NULL: last mx_create error */

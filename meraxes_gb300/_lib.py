@@ -27,7 +27,8 @@ EXPORTS = [
     "mx_lightcone_init", "mx_ConstructLightcone", "mx_ConstructLightcone_device",
     "mx_construct_baryon_grids", "mx_construct_baryon_grids_device", "mx_calculate_Mvir_crit",
     "mx_calculate_Mvir_crit_device", "mx_set_xray_params", "mx_ps_loss_device", "mx_adjoint_device",
-    "mx_create_limited", "mx_fft_block_sizes", "mx_set_step_graph", "mx_batch_create", "mx_batch_run", "mx_batch_destroy",
+    "mx_create_limited", "mx_fft_block_sizes", "mx_set_step_graph", "mx_batch_create", "mx_batch_run",
+    "mx_batch_run_graph", "mx_batch_destroy",
     "mx_batch_last_error",
 ]
 
@@ -132,6 +133,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mx_batch_create.restype = ctypes.c_int
         L.mx_batch_run.argtypes = [P, ctypes.POINTER(MxBatchItem), ctypes.c_int32]
         L.mx_batch_run.restype = ctypes.c_int
+        L.mx_batch_run_graph.argtypes = [P, ctypes.POINTER(MxBatchItem), ctypes.c_int32]
+        L.mx_batch_run_graph.restype = ctypes.c_int
         L.mx_batch_destroy.argtypes = [P]
         L.mx_batch_destroy.restype = None
         L.mx_batch_last_error.argtypes = [P]

@@ -347,11 +347,13 @@ class Batch:
         if rc != 0:
             raise _lib.MxError(rc, "mx_batch_create")
 
-    def run(self, items):
+    def run(self, items, graph: bool = False):
         """items: dicts with "params" (ReionParams), "redshifts", "snapshot"
         and "grids" (name -> C-contiguous float32 numpy array, updated in place
         as by ReionGridStep.step).  Returns the globals of every item; raises
-        MxError if any item failed (the others still ran)."""
+        MxError if any item failed (the others still ran).  graph=True runs
+        every item in one CUDA graph launch (mx_batch_run_graph; the arrays
+        must be page-locked, e.g. torch.empty(..., pin_memory=True).numpy())."""
         n = len(items)
         arr = (_lib.MxBatchItem * n)()
         keep = []  # ctypes objects that must outlive the call
@@ -377,7 +379,8 @@ class Batch:
             arr[i].grids = ctypes.pointer(g)
             arr[i].out = ctypes.pointer(out)
             arr[i].status = -99
-        rc = self.lib.mx_batch_run(self.handle, arr, n)
+        run = self.lib.mx_batch_run_graph if graph else self.lib.mx_batch_run
+        rc = run(self.handle, arr, n)
         if rc != 0:
             raise _lib.MxError(rc, self.lib.mx_batch_last_error(self.handle).decode())
         return [o.as_dict() for o in outs]

@@ -2962,6 +2962,11 @@ struct mx_batch
   size_t max_work_bytes = 0;
   int device = 0;
   std::vector<BatchWorker> workers;
+  // mx_batch_run_graph: one context per item position, and the stream the
+  // batch graph is captured and launched on
+  std::vector<BatchWorker> gctx;
+  cudaStream_t gstream = nullptr;
+  cudaEvent_t gfork = nullptr;
   std::mutex mu;
   std::string err;
   int err_item = -1;
@@ -2975,7 +2980,10 @@ struct mx_batch
     }
   }
 
-  void run_item(BatchWorker& w, mx_batch_item& it, int index)
+  // The worker's context for the item's configuration: kept (with the
+  // previous box's history cleared and the item's X-ray parameters) or
+  // created.  False (status and error set) if creation failed.
+  bool prepare(BatchWorker& w, mx_batch_item& it, int index)
   {
     const mx_params key = batch_key(*it.params);
     if (w.ctx && std::memcmp(&key, &w.key, sizeof(key)) == 0) {
@@ -2998,10 +3006,17 @@ struct mx_batch
         it.status = rc;
         fail(index, g_create_error);
         w.ctx = nullptr;
-        return;
+        return false;
       }
       w.key = key;
     }
+    return true;
+  }
+
+  void run_item(BatchWorker& w, mx_batch_item& it, int index)
+  {
+    if (!prepare(w, it, index))
+      return;
     int rc = mx_set_redshifts(w.ctx, it.redshifts, it.n_snaps);
     mx_globals scratch{};
     if (rc == MX_OK)
@@ -3039,6 +3054,13 @@ void mx_batch_destroy(mx_batch* b)
   for (BatchWorker& w : b->workers)
     if (w.ctx)
       mx_destroy(w.ctx);
+  for (BatchWorker& w : b->gctx)
+    if (w.ctx)
+      mx_destroy(w.ctx);
+  if (b->gfork)
+    cudaEventDestroy(b->gfork);
+  if (b->gstream)
+    cudaStreamDestroy(b->gstream);
   delete b;
 }
 
@@ -3143,6 +3165,223 @@ int mx_batch_run(mx_batch* b, mx_batch_item* items, int32_t n_items)
       pool.emplace_back(work, w);
   for (std::thread& th : pool)
     th.join();
+  for (int i = 0; i < n_items; i++)
+    if (items[i].status != MX_OK)
+      return items[i].status;
+  return MX_OK;
+}
+
+namespace {
+bool host_pinned(const void* p)
+{
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// The grids a step reads from the host (inputs not written by an earlier
+// stage of the step) and writes back, in the order ComputeTs,
+// find_HII_bubbles, brightness temperature (as mx_step).
+void step_copy_lists(const mx_params& p, std::vector<FieldIO>* in, std::vector<FieldIO>* out)
+{
+  std::vector<const std::vector<FieldIO>*> lists;
+  if (p.flag_spin_temp)
+    lists.push_back(&ts_fields());
+  lists.push_back(&fhb_fields());
+  if (p.flag_21cm)
+    lists.push_back(&dt_fields());
+  auto has = [](const std::vector<FieldIO>& v, float* mx_grids::*m) {
+    for (const FieldIO& f : v)
+      if (f.member == m)
+        return true;
+    return false;
+  };
+  for (const std::vector<FieldIO>* l : lists)
+    for (const FieldIO& f : *l) {
+      if ((f.dir & IN) && !has(*out, f.member) && !has(*in, f.member))
+        in->push_back({ f.member, f.padded, IN });
+      if ((f.dir & OUT) && !has(*out, f.member))
+        out->push_back({ f.member, f.padded, OUT });
+    }
+}
+}  // namespace
+
+int mx_batch_run_graph(mx_batch* b, mx_batch_item* items, int32_t n_items)
+{
+  if (!b)
+    return MX_EINVAL;
+  b->err.clear();
+  b->err_item = -1;
+  if (n_items < 0 || (n_items > 0 && !items)) {
+    b->err = "mx_batch_run_graph: bad item list";
+    return MX_EINVAL;
+  }
+  for (int i = 0; i < n_items; i++) {
+    if (!items[i].params || !items[i].redshifts || !items[i].grids) {
+      b->err = "item " + std::to_string(i) + ": NULL params, redshifts or grids";
+      items[i].status = MX_EINVAL;
+      return MX_EINVAL;
+    }
+    items[i].status = MX_OK;
+  }
+  if (n_items == 0)
+    return MX_OK;
+  if (cudaSetDevice(b->device) != cudaSuccess) {
+    b->err = "mx_batch_run_graph: cudaSetDevice failed";
+    return MX_ECUDA;
+  }
+  if (!b->gstream) {
+    if (cudaStreamCreateWithFlags(&b->gstream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->gfork, cudaEventDisableTiming) != cudaSuccess) {
+      b->err = "mx_batch_run_graph: stream creation failed";
+      return MX_ECUDA;
+    }
+  }
+  // contexts, redshifts, device mirrors and cuFFT plans: everything that
+  // allocates, before the capture
+  if ((int)b->gctx.size() < n_items)
+    b->gctx.resize(n_items);
+  std::vector<std::vector<FieldIO>> ins(n_items), outs(n_items);
+  for (int i = 0; i < n_items; i++) {
+    mx_batch_item& it = items[i];
+    BatchWorker& w = b->gctx[i];
+    if (!b->prepare(w, it, i))
+      return it.status;
+    mx_ctx* c = w.ctx;
+    const int rc = guarded(c, [&]() {
+      if (mx_set_redshifts(c, it.redshifts, it.n_snaps) != MX_OK)
+        throw CudaError{ MX_EINVAL, c->err };
+      check_snapshot(c, it.snapshot);
+      c->ensure_mirror();
+      if (!c->fused_fft) {
+        c->c2r_plan(n_fields(c->p));
+        if (c->p.flag_spin_temp)
+          c->c2r_plan(1);
+      }
+      if (c->p.flag_spin_temp && c->p.flag_pecvel > 0)
+        c->c2r_plan(1);
+      step_copy_lists(c->p, &ins[i], &outs[i]);
+      const mx_grids* h = it.grids;
+      float* mx_grids::*all[] = { &mx_grids::deltax,   &mx_grids::stars,        &mx_grids::weighted_sfr,
+                                  &mx_grids::sfr,      &mx_grids::sfr_histories, &mx_grids::N_rec,
+                                  &mx_grids::x_e_box,  &mx_grids::x_e_box_prev, &mx_grids::Tk_box,
+                                  &mx_grids::TS_box,   &mx_grids::xH,           &mx_grids::z_at_ionization,
+                                  &mx_grids::r_bubble, &mx_grids::J_21,         &mx_grids::J_21_at_ionization,
+                                  &mx_grids::Gamma12,  &mx_grids::delta_T,      &mx_grids::vel };
+      for (auto m : all)
+        if (h->*m && !host_pinned(h->*m))
+          throw CudaError{ MX_EINVAL, "a host grid is not page-locked (the graph's copies need pinned memory)" };
+    });
+    if (rc != MX_OK) {
+      it.status = rc;
+      b->fail(i, c->err);
+      return rc;
+    }
+  }
+  // one capture: each item's copies in, step and copies out on its own
+  // context stream, forked from and joined to the batch stream
+  cudaGraph_t graph = nullptr;
+  std::vector<mx_globals> scratch(n_items);
+  std::vector<int> launches(n_items, 0);
+  int failed = -1;
+  std::string msg;
+  if (cudaStreamBeginCapture(b->gstream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    b->err = "mx_batch_run_graph: capture could not begin";
+    return MX_ECUDA;
+  }
+  try {
+    MX_CUDA(cudaEventRecord(b->gfork, b->gstream));
+    for (int i = 0; i < n_items; i++) {
+      failed = i;
+      mx_batch_item& it = items[i];
+      mx_ctx* c = b->gctx[i].ctx;
+      mx_globals* o = it.out ? it.out : &scratch[i];
+      cudaStream_t s = c->stream;
+      MX_CUDA(cudaStreamWaitEvent(s, b->gfork, 0));
+      c->capturing = true;
+      c->stage_used = 0;
+      c->finishers.clear();
+      c->graph_keep.clear();
+      copy_fields(c, it.grids, ins[i], IN, s);
+      if (c->p.flag_spin_temp)
+        copy_histories(c, it.grids, s);
+      mx_grids m = mirror_for(c, it.grids);
+      if (c->p.flag_spin_temp) {
+        run_ComputeTs(c, it.snapshot, &m, o, s);
+        launches[i] += o->gpu_launches;
+      }
+      run_find_HII_bubbles(c, it.snapshot, &m, o, s);
+      launches[i] += o->gpu_launches;
+      if (c->p.flag_21cm) {
+        run_delta_T(c, it.snapshot, &m, o, s);
+        launches[i] += o->gpu_launches;
+      }
+      copy_fields(c, it.grids, outs[i], OUT, s);
+      MX_CUDA(cudaEventRecord(c->ev_state, s));
+      MX_CUDA(cudaStreamWaitEvent(b->gstream, c->ev_state, 0));
+      c->capturing = false;
+    }
+    failed = -1;
+  } catch (const CudaError& e) {
+    msg = e.msg;
+  } catch (const std::exception& e) {
+    msg = e.what();
+  }
+  for (int i = 0; i < n_items; i++)
+    if (b->gctx[i].ctx)
+      b->gctx[i].ctx->capturing = false;
+  const cudaError_t ec = cudaStreamEndCapture(b->gstream, &graph);
+  if (failed >= 0 || ec != cudaSuccess) {
+    if (graph)
+      cudaGraphDestroy(graph);
+    if (failed < 0) {
+      failed = 0;
+      msg = std::string("batch graph capture: ") + cudaGetErrorString(ec);
+    }
+    for (int i = 0; i < n_items; i++) {
+      items[i].status = MX_ECUDA;
+      if (b->gctx[i].ctx) {
+        b->gctx[i].ctx->finishers.clear();
+        b->gctx[i].ctx->graph_keep.clear();
+      }
+    }
+    b->fail(failed, msg);
+    return MX_ECUDA;
+  }
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e == cudaSuccess)
+    e = cudaGraphLaunch(exec, b->gstream);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(b->gstream);
+  if (exec)
+    cudaGraphExecDestroy(exec);
+  // each item's reads back, error checks and globals
+  for (int i = 0; i < n_items; i++) {
+    mx_ctx* c = b->gctx[i].ctx;
+    std::vector<std::function<void()>> fin;
+    fin.swap(c->finishers);
+    c->graph_keep.clear();
+    if (e != cudaSuccess) {
+      items[i].status = MX_ECUDA;
+      b->fail(i, std::string("batch graph: ") + cudaGetErrorString(e));
+      continue;
+    }
+    const int rc = guarded(c, [&]() {
+      for (auto& f : fin)
+        f();
+    });
+    c->stage_used = 0;
+    items[i].status = rc;
+    if (rc != MX_OK)
+      b->fail(i, c->err);
+    else if (items[i].out)
+      items[i].out->gpu_launches = launches[i];
+  }
   for (int i = 0; i < n_items; i++)
     if (items[i].status != MX_OK)
       return items[i].status;

@@ -1,7 +1,7 @@
-"""The batch of independent boxes (meraxes_gb300/batch.py): boxes of two
-sizes (a power of two on the fused transforms, 48^3 on cuFFT) run by
-concurrent workers give the same losses and gradients, bit for bit, as each
-box run alone."""
+"""The batch of independent boxes (meraxes_gb300/batch.py) and the native
+executor (mx_batch_run, mx_batch_run_graph): boxes of several sizes (powers of
+two, and 24^3 / 48^3 on the factor-3 transforms) give the same results, bit
+for bit, as each box run alone."""
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -111,3 +111,58 @@ def test_native_batch_object_reuses_contexts_across_runs():
     for it, g in zip(items, grids_first):
         for k in g:
             assert np.array_equal(it["grids"][k], g[k]), k
+
+
+def _pinned(grids):
+    """Copies of the grids in page-locked host memory (what the batch graph's
+    copy nodes need)."""
+    import torch
+
+    return {k: torch.from_numpy(v).pin_memory().numpy() for k, v in grids.items()}
+
+
+def test_batch_graph_matches_single_box_runs():
+    """mx_batch_run_graph: boxes of three sizes (a power of two, and 24^3 and
+    48^3 on the factor-3 transforms) and two X-ray luminosities stepped in
+    one CUDA graph launch give each box's grids and globals bit for bit as
+    ReionGridStep.step of that box alone, on a first run (contexts created)
+    and a second (contexts reused)."""
+    import numpy as np
+
+    from meraxes_gb300.api import Batch, ReionGridStep
+
+    specs = [("full24", 32, 1e40), ("full24", 48, 1e40), ("full24", 24, 3e40), ("full24", 48, 3e40),
+             ("plain32_tophat", 64, None), ("evolve16", 32, None)]
+    items = _native_items(specs)
+    fresh = [{k: v.copy() for k, v in it["grids"].items()} for it in items]
+    alone = []
+    for it in items:
+        g = {k: v.copy() for k, v in it["grids"].items()}
+        step = ReionGridStep(it["params"], it["redshifts"])
+        glob = step.step(it["snapshot"], g)
+        step.close()
+        alone.append((g, glob))
+    b = Batch(max_workers=2)
+    for run in range(2):
+        for it, f in zip(items, fresh):
+            it["grids"] = _pinned(f)
+        outs = b.run(items, graph=True)
+        for it, out, (g, glob) in zip(items, outs, alone):
+            for k in g:
+                assert np.array_equal(it["grids"][k], g[k]), (run, k)
+            for k in ("volume_weighted_global_xH", "volume_ave_TS", "volume_ave_Tb", "x_e_ave"):
+                assert out[k] == glob[k], (run, k)
+            assert out["gpu_launches"] > 0
+    b.close()
+
+
+def test_batch_graph_rejects_pageable_grids():
+    from meraxes_gb300 import _lib
+    from meraxes_gb300.api import Batch
+
+    items = _native_items([("plain32_tophat", 32, None)])
+    b = Batch(max_workers=1)
+    with pytest.raises(_lib.MxError) as e:
+        b.run(items, graph=True)
+    b.close()
+    assert e.value.code == -1 and "page-locked" in str(e.value)
