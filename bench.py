@@ -415,6 +415,7 @@ def run_gb300(args, rank, world, local):
     if not args.no_e2e and args.e2e_steps > 0:
         e2e = run_e2e(args, step, w, fields, hist, smax, timed, n_hist, device, world)
     block_sizes = list(step.fft_block_sizes())
+    zpass_blocks = step.zpass_blocks()
     step.close()
     plain = None
     if not args.no_plain:
@@ -433,7 +434,7 @@ def run_gb300(args, rank, world, local):
                             "warm-up)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (each grid 0.54 GB at 512^3)",
-                   "fft_block_sizes": block_sizes,
+                   "fft_block_sizes": block_sizes, "zpass_blocks_per_sm": zpass_blocks,
                    "step_graph": not args.no_graph},
         "value_uncaptured": round(ungraphed, 3) if ungraphed is not None else None,
         "gpu_launches": launches, "clocks": clk, "roofline": roofline,

@@ -229,6 +229,10 @@ int32_t mx_n_sfr_histories(const mx_ctx* ctx);
  * y-pass of its fused inverse transforms (256 or 512; 0 and 0 when the grid
  * uses cuFFT).  No reference counterpart. */
 int mx_fft_block_sizes(const mx_ctx* ctx, int32_t* x_threads, int32_t* y_threads);
+/* Resident blocks per SM that the context's autotuner budgeted the threshold
+ * z-pass's registers for (2 or 3; 0 when the grid does not run that kernel).
+ * No reference counterpart. */
+int32_t mx_zpass_blocks_per_sm(const mx_ctx* ctx);
 /* Filter radii of find_HII_bubbles for this configuration (largest first). */
 int32_t mx_filter_radii(const mx_ctx* ctx, double* radii, int32_t cap);
 

@@ -93,6 +93,10 @@ class ReionGridStep:
         n = self.lib.mx_filter_radii(self.ctx, buf, 1024)
         return list(buf[:n])
 
+    def zpass_blocks(self) -> int:
+        """Resident blocks per SM the threshold z-pass was tuned for (0: not run)."""
+        return int(self.lib.mx_zpass_blocks_per_sm(self.ctx))
+
     def set_graph(self, on: bool = True):
         """Device steps (step() on CUDA tensors) captured and launched as one
         CUDA graph each (mx_set_step_graph)."""

@@ -90,6 +90,8 @@ struct mx_ctx
   int x_threads = 512, y_threads = 256;
   // register budget of the threshold z-pass: 2 or 3 resident blocks per SM
   int z_blocks = 2;
+  // x-pass: L1 prefetch of each next field's points (MX_XPASS_PREFETCH=1)
+  int x_prefetch = 0;
   // 2-D tensor map of d_shells (cells x shells) for the evolve kernel's tile
   // copies (make_shell_map), when one applies
   bulk::TensorMap shell_map{};
@@ -591,6 +593,7 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
         xa.filter_type = p.filter_type;
         xa.delta_k = (float)(2.0 * k::PI / (float)p.box_size);
         xa.scale = (float)(1.0 / (double)gd.N);
+        xa.prefetch = c->x_prefetch;
         {
           Prof pr(c, "fft_x_filter", (double)G * B8C * (1 + nf), s);
           launch_fft_x_filter(gd.D, xa, c->x_threads, s);
@@ -971,6 +974,7 @@ static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sf
         xa.filter_type = p.ts_heating_filter_type;
         xa.delta_k = (float)(2.0 * k::PI / (float)p.box_size);
         xa.scale = (float)(1.0 / (double)gd.N);
+        xa.prefetch = c->x_prefetch;
         {
           Prof pr(c, "fft_x_filter", 8.0 * (double)gd.C * (1 + nb), s);
           launch_fft_x_filter(gd.D, xa, c->x_threads, s);
@@ -2343,6 +2347,88 @@ int mx_create_limited(const mx_params* params, const char* tables_dir, size_t ma
 // creation (a zero spectrum, up to four radii, best of three launches) and
 // keeps the faster.  MX_XPASS_THREADS / MX_YPASS_THREADS (256 or 512) fix a
 // choice; MX_AUTOTUNE=0 keeps the defaults (x 512, y 256).
+// Register budget of the threshold z-pass (power-of-two grids): 2 resident
+// blocks per SM (128 registers) or 3 (80, with a few spills).  Timed at
+// context creation on scratch: up to 4 radii of zero spectra of the
+// context's fields and six zero state grids in the transform work buffer,
+// best of three launches after one warm-up; MX_ZPASS_BLOCKS fixes it.
+static void tune_zpass(mx_ctx* c)
+{
+  if (const char* env = std::getenv("MX_ZPASS_BLOCKS")) {
+    c->z_blocks = std::atoi(env) == 3 ? 3 : 2;
+    return;
+  }
+  const char* at = std::getenv("MX_AUTOTUNE");
+  if ((at && std::string(at) == "0") || !c->fused_fft || (c->gd.D & (c->gd.D - 1)) != 0)
+    return;
+  const GridDims& gd = c->gd;
+  const int G = n_fields(c->p);
+  const long long spectrum_bytes = (long long)sizeof(float2) * c->work_C;
+  const long long state_bytes = 6LL * gd.N * (long long)sizeof(float);
+  const long long state_spectra = (state_bytes + spectrum_bytes - 1) / spectrum_bytes;
+  const int nr = (int)std::min<long long>(4, (c->work_fields - state_spectra) / G);
+  if (nr < 1)
+    return;
+  cudaStream_t s = c->stream;
+  float* state = reinterpret_cast<float*>(c->d_work + (long long)nr * G * c->work_C);
+  MX_CUDA(cudaMemsetAsync(c->d_work, 0, (size_t)(spectrum_bytes * nr * G + state_bytes), s));
+  std::vector<RadiusParams> rps(nr);
+  for (RadiusParams& q : rps) {
+    q = RadiusParams{};
+    q.R = q.M_mean = q.R_cubed = 1.0;
+  }
+  MX_CUDA(cudaMemcpyAsync(c->d_rp, rps.data(), sizeof(RadiusParams) * nr, cudaMemcpyHostToDevice, s));
+  const bool spin = c->p.flag_spin_temp != 0, recomb = c->p.flag_recombinations != 0;
+  ZThresholdArgs za;
+  za.spectra = c->d_work;
+  za.C = c->work_C;
+  za.G = G;
+  za.idx_xe = spin ? 3 : -1;
+  za.idx_nr = recomb ? (spin ? 4 : 3) : -1;
+  za.n_r = nr;
+  za.n_f = nr;
+  za.rp = c->d_rp;
+  for (int f = 0; f < MAX_FIELDS; f++)
+    za.direct[f] = nullptr;
+  za.xH = state;
+  za.z_at_ion = state + gd.N;
+  za.r_bubble = state + 2 * gd.N;
+  za.J21 = state + 3 * gd.N;
+  za.J21_at_ion = state + 4 * gd.N;
+  za.Gamma12 = state + 5 * gd.N;
+  za.pixel_volume = 1.0;
+  za.eff = 1.0;
+  za.redshift = 10.0;
+  za.gamma_halo_bias = 1.0f;
+  za.uvb = c->p.uvb_flag;
+  za.recomb = recomb;
+  za.spin = spin;
+  za.err = c->d_err;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  MX_CUDA(cudaEventCreate(&e0));
+  MX_CUDA(cudaEventCreate(&e1));
+  float best[2] = { 1e30f, 1e30f };
+  for (int v = 0; v < 2; v++) {
+    za.blocks_per_sm = v + 2;
+    launch_fft_z_threshold(gd.D, za, s);  // warm-up
+    for (int i = 0; i < 3; i++) {
+      cudaEventRecord(e0, s);
+      launch_fft_z_threshold(gd.D, za, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best[v] = std::min(best[v], ms);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  MX_CUDA(cudaGetLastError());
+  MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
+  MX_CUDA(cudaStreamSynchronize(s));
+  c->z_blocks = best[1] < best[0] ? 3 : 2;
+}
+
 static void tune_fft(mx_ctx* c)
 {
   auto env_threads = [](const char* name) {
@@ -2454,8 +2540,9 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
   c->nthreads = std::max(1, std::min(64, hw_threads()));
   if (const char* env = std::getenv("MX_HOST_THREADS"))
     c->nthreads = std::max(1, std::atoi(env));
-  if (const char* env = std::getenv("MX_ZPASS_BLOCKS"))
-    c->z_blocks = std::atoi(env) == 3 ? 3 : 2;
+  if (const char* env = std::getenv("MX_XPASS_PREFETCH"))
+    c->x_prefetch = std::atoi(env) != 0;
+
   c->fused_fft = fft3d_supported(p.grid_dim);
   if (const char* env = std::getenv("MX_TRANSFORM"))
     if (std::string(env) == "cufft")
@@ -2514,6 +2601,7 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
     c->work_cap_bytes = work_cap_bytes;
     c->alloc_scratch();
     tune_fft(c.get());
+    tune_zpass(c.get());
   } catch (const CudaError& e) {
     g_create_error = e.msg;
     return e.code == MX_ECUDA && e.msg.find("memory") != std::string::npos ? MX_ENOMEM : e.code;
@@ -2543,6 +2631,13 @@ int mx_set_redshifts(mx_ctx* ctx, const double* zz, int32_t n_snaps)
 }
 
 int32_t mx_n_sfr_histories(const mx_ctx* ctx) { return ctx ? ctx->n_hist : -1; }
+
+int32_t mx_zpass_blocks_per_sm(const mx_ctx* ctx)
+{
+  if (!ctx)
+    return MX_EINVAL;
+  return ctx->fused_fft && (ctx->gd.D & (ctx->gd.D - 1)) == 0 ? ctx->z_blocks : 0;
+}
 
 int mx_fft_block_sizes(const mx_ctx* ctx, int32_t* x_threads, int32_t* y_threads)
 {

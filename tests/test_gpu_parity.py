@@ -535,3 +535,38 @@ def test_gpu_deposit_edge_cases():
           "fesc_gsm": np.ones(1), "gross_sm": np.ones(1)}
     out = _deposit_gpu(step, D, hist0, [ok], [(0, 0.0, 0.0)], False)[0]
     assert out["stars"].sum() == np.float32(1.0)
+
+
+# The autotuner budgets the threshold z-pass's registers for 2 or 3 resident
+# blocks per SM (MX_ZPASS_BLOCKS fixes it); both give the same grids.
+@pytest.mark.parametrize("name,D", [("full24", 64), ("evolve16", 32)])
+def test_zpass_register_budgets_give_identical_results(name, D, monkeypatch):
+    from cases import initial
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+
+    c = CASES[name]
+    w = Case(name, c.base, D, c.overrides, c.fesc, c.snapshots).workload()
+    runs = []
+    for b in ("2", "3"):
+        monkeypatch.setenv("MX_ZPASS_BLOCKS", b)
+        step = ReionGridStep(w.params, w.redshifts)
+        assert step.zpass_blocks() == int(b)
+        gen = syn.FieldGenerator(w)
+        st = initial(w, step.n_sfr_histories)
+        glob = []
+        for s in w.snapshots:
+            st.update(gen.inputs(s, step.n_sfr_histories))
+            glob.append(step.step(s, st))
+        runs.append((st, glob))
+        step.close()
+    (sa, ga), (sb, gb) = runs
+    for k in OUTPUT_GRIDS:
+        if k in sa:
+            assert np.array_equal(sa[k], sb[k]), k
+    for a, b in zip(ga, gb):
+        assert a["volume_weighted_global_xH"] == b["volume_weighted_global_xH"]
+    monkeypatch.delenv("MX_ZPASS_BLOCKS")
+    tuned = ReionGridStep(w.params, w.redshifts)
+    assert tuned.zpass_blocks() in (2, 3)
+    tuned.close()
