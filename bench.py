@@ -729,6 +729,7 @@ def cpu_runs(grid: int, threads: int, runs: int, sample=None, timeout: float = 3
     """cpu_run in a child process with OMP_NUM_THREADS = threads (the child
     keeps the oracle's OpenMP pool away from this process's CUDA context)."""
     smp = dict(CPU_SAMPLE if sample is None else sample)
+    smp["cell_div"] = min(smp["cell_div"], grid)  # at least one x plane of cells
     code = (f"import sys, json; sys.path.insert(0, {ROOT!r}); sys.path.insert(0, {os.path.join(ROOT, 'tests')!r});"
             f"import bench; print(json.dumps(bench.cpu_run({grid}, {threads}, {smp['radii']}, {smp['shells']}, "
             f"{smp['cell_div']}, {runs})))")

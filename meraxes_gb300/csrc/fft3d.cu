@@ -508,16 +508,6 @@ __global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) 
       pts[i] = live ? src[(long long)kx * (D * Pitch<D>::HP)] : make_float2(0.f, 0.f);
     });
   };
-  // with a.prefetch: the next field's points requested into L1 (no
-  // registers held) while the current field's steps B and C run
-  auto prefetch_points = [&](int ky, int g) {
-    if (!a.prefetch || !live)
-      return;
-    const float2* src = a.in[g] + (long long)ky * Pitch<D>::HP + kz0 + t0;
-    T::for_each_input([&](int kx, int) {
-      asm volatile("prefetch.global.L1 [%0];" ::"l"(src + (long long)kx * (D * Pitch<D>::HP)));
-    });
-  };
   // filter weights of the tile, wsm[|kx| * TXC + t] for |kx| = min(kx, D -
   // kx) <= D/2, then the first field's points (read after the weights, whose
   // sincosf would otherwise push them out of registers; the reads are in
@@ -554,18 +544,10 @@ __global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) 
       });
     };
     step_a();
-    if (a.G > 1)
-      prefetch_points(ky, 1);
-    else if (h + 1 < n_rows)
-      prefetch_points(D - kyp, 0);
     finish(0);
     for (int g = 1; g < a.G; g++) {
       read_points(ky, g);
       step_a();
-      if (g + 1 < a.G)
-        prefetch_points(ky, g + 1);
-      else if (h + 1 < n_rows)
-        prefetch_points(D - kyp, 0);
       finish(g);
     }
   }

@@ -22,7 +22,6 @@ struct XPassArgs
   float delta_k;
   float scale;       // 1/N (exact for power-of-two N)
   float sharpk_max;  // set by launch_fft_x_filter
-  int prefetch = 0;  // request each next field's points into L1 during steps B and C
 };
 
 // Forward R2C of G padded real grids into spectra [kx][ky][kz] with rows of

@@ -90,8 +90,6 @@ struct mx_ctx
   int x_threads = 512, y_threads = 256;
   // register budget of the threshold z-pass: 2 or 3 resident blocks per SM
   int z_blocks = 2;
-  // x-pass: L1 prefetch of each next field's points (MX_XPASS_PREFETCH=1)
-  int x_prefetch = 0;
   // 2-D tensor map of d_shells (cells x shells) for the evolve kernel's tile
   // copies (make_shell_map), when one applies
   bulk::TensorMap shell_map{};
@@ -593,7 +591,6 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
         xa.filter_type = p.filter_type;
         xa.delta_k = (float)(2.0 * k::PI / (float)p.box_size);
         xa.scale = (float)(1.0 / (double)gd.N);
-        xa.prefetch = c->x_prefetch;
         {
           Prof pr(c, "fft_x_filter", (double)G * B8C * (1 + nf), s);
           launch_fft_x_filter(gd.D, xa, c->x_threads, s);
@@ -974,7 +971,6 @@ static void compute_shells(mx_ctx* c, const ShellPlan& sp, float* sfr, float* sf
         xa.filter_type = p.ts_heating_filter_type;
         xa.delta_k = (float)(2.0 * k::PI / (float)p.box_size);
         xa.scale = (float)(1.0 / (double)gd.N);
-        xa.prefetch = c->x_prefetch;
         {
           Prof pr(c, "fft_x_filter", 8.0 * (double)gd.C * (1 + nb), s);
           launch_fft_x_filter(gd.D, xa, c->x_threads, s);
@@ -2540,8 +2536,6 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
   c->nthreads = std::max(1, std::min(64, hw_threads()));
   if (const char* env = std::getenv("MX_HOST_THREADS"))
     c->nthreads = std::max(1, std::atoi(env));
-  if (const char* env = std::getenv("MX_XPASS_PREFETCH"))
-    c->x_prefetch = std::atoi(env) != 0;
 
   c->fused_fft = fft3d_supported(p.grid_dim);
   if (const char* env = std::getenv("MX_TRANSFORM"))

@@ -1569,7 +1569,9 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
     /* per-cell evolution, ComputeTs.c:743-900: cells in parallel, the
      * volume averages summed afterwards in the reference's cell order */
     double* contrib = (double*)ctx_buf((void**)&c->contrib, sizeof(double) * 4 * (size_t)D * D * D);
-    /* timing sample: the first D / sample_cell_div x planes only */
+    /* timing sample: the first D / sample_cell_div x planes only; the x and
+     * y loops are shared out together, so that a sample of fewer x planes
+     * than threads still keeps every thread busy */
     const int nx_cells = c->sample_cell_div > 1 ? D / c->sample_cell_div : D;
 #pragma omp parallel
     {
@@ -1577,7 +1579,7 @@ int mxo_ComputeTs(mxo_ctx* c, int snapshot, const mx_grids* g, mx_globals* out)
     double* fh = (double*)malloc(sizeof(double) * (size_t)S);
     double* fi = (double*)malloc(sizeof(double) * (size_t)S);
     double* fl = (double*)malloc(sizeof(double) * (size_t)S);
-#pragma omp for schedule(static)
+#pragma omp for collapse(2) schedule(static)
     for (int ix = 0; ix < nx_cells; ix++)
       for (int iy = 0; iy < D; iy++)
         for (int iz = 0; iz < D; iz++) {

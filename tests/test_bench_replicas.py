@@ -28,7 +28,7 @@ def _rank_main(rank, world, port, out):
     ms_local = 100.0 * (rank + 1)  # rank 1 is the slower replica
     value = bench.replica_value(ms_local, 4, world)
     bench.barrier(world)
-    args = bench.parse_args(["--impl", "reference", "--steps", "1", "--warmup", "0"])
+    args = bench.parse_args(["--impl", "reference", "--steps", "1", "--warmup", "0", "--grid", "32"])
     ref, _ = bench.run_reference(args, rank, world)
     out.put((rank, value, ref is None))
     import torch.distributed as dist
