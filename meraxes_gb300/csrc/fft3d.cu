@@ -608,6 +608,15 @@ __global__ void __launch_bounds__(YTHREADS, YTHREADS == 256 ? 3 : 2) k_fft_y(flo
 // finish them.  The arithmetic of every item is that of the separate passes,
 // so the results are the same bit for bit.
 namespace {
+// Block-wide barrier that does not require the warps to be converged
+// (barrier.sync without .aligned).  k_fft_xy branches on the item index, a
+// value read from shared memory, so the compiler cannot prove its barriers
+// uniform; __syncthreads() (the .aligned form) there let the threads of a
+// block run into step B before step A's stores had landed (measured: wrong
+// and run-to-run different x items at 16 points per thread, exact with this
+// form).
+__device__ __forceinline__ void block_barrier() { asm volatile("barrier.sync 0;" ::: "memory"); }
+
 // Waits until *p >= target (acquire): false after the consumer wait limit
 // or 2 s.
 __device__ __forceinline__ bool counter_wait(const unsigned* p, unsigned target)
@@ -647,10 +656,10 @@ __global__ void __launch_bounds__(NTHR, NTHR == 256 && D < 512 ? 3 : 2) k_fft_xy
   const int t0 = threadIdx.x % TXC;
   float2 pts[T::NPTS];
   for (;;) {
-    __syncthreads();  // the previous item is done with buf, wsm and s_item
+    block_barrier();  // the previous item is done with buf, wsm and s_item
     if (threadIdx.x == 0)
       s_item = atomicAdd(a.sync, 1u);
-    __syncthreads();
+    block_barrier();
     const unsigned q = s_item;
     if (q >= total)
       return;
@@ -685,7 +694,7 @@ __global__ void __launch_bounds__(NTHR, NTHR == 256 && D < 512 ? 3 : 2) k_fft_xy
         const float2* __restrict__ src = x.in[g] + (long long)ky * HP + kz0 + t0;
         T::for_each_input(
           [&](int kx, int i) { pts[i] = live ? src[(long long)kx * (D * HP)] : make_float2(0.f, 0.f); });
-        __syncthreads();  // weights written; the previous row's step C done with buf
+        block_barrier();  // weights written; the previous row's step C done with buf
         T::a(buf, tw, [&](int kx, int, int i) {
           float2 v = pts[i];
           const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
@@ -693,15 +702,15 @@ __global__ void __launch_bounds__(NTHR, NTHR == 256 && D < 512 ? 3 : 2) k_fft_xy
           v.y *= wv;
           return v;
         });
-        __syncthreads();
+        block_barrier();
         T::b(buf, tw);
-        __syncthreads();
+        block_barrier();
         float2* __restrict__ dst = spec + (long long)ky * HP + kz0 + t0;
         T::c(buf, [&](int xo, int, float2 v) { dst[(long long)xo * (D * HP)] = v; });
       }
       // release: every thread's stores, then one count for the block
       __threadfence();
-      __syncthreads();
+      block_barrier();
       if (threadIdx.x == 0)
         atomicAdd(a.sync + 1 + c, 1u);
     } else {
@@ -709,7 +718,7 @@ __global__ void __launch_bounds__(NTHR, NTHR == 256 && D < 512 ? 3 : 2) k_fft_xy
         s_ok = counter_wait(a.sync + 1 + c, (unsigned)H);
         __threadfence();
       }
-      __syncthreads();
+      block_barrier();
       if (!s_ok) {
         if (threadIdx.x == 0)
           atomicOr(a.err, ERR_PIPELINE_TIMEOUT | ERR_XY_TIMEOUT);
@@ -719,9 +728,9 @@ __global__ void __launch_bounds__(NTHR, NTHR == 256 && D < 512 ? 3 : 2) k_fft_xy
       float2* col = spec + (long long)idx * D * HP + kz0 + t0;
       T::for_each_input([&](int ky, int i) { pts[i] = __ldcg(col + ky * HP); });
       T::a(buf, tw, [&](int, int, int i) { return pts[i]; });
-      __syncthreads();
+      block_barrier();
       T::b(buf, tw);
-      __syncthreads();
+      block_barrier();
       T::c(buf, [&](int y, int, float2 v) { col[y * HP] = v; });
     }
   }

@@ -2000,6 +2000,11 @@ static int guarded(mx_ctx* c, F&& f)
     if (cudaSetDevice(c->device) != cudaSuccess)
       throw CudaError{ MX_ECUDA, "cudaSetDevice failed" };
     f();
+    // a launch that never ran (resources, configuration) leaves no trace but
+    // this error
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess)
+      throw CudaError{ MX_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(le) };
     c->err.clear();
     return MX_OK;
   } catch (const CudaError& e) {
