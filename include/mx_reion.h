@@ -233,11 +233,6 @@ int mx_fft_block_sizes(const mx_ctx* ctx, int32_t* x_threads, int32_t* y_threads
  * z-pass's registers for (2 or 3; 0 when the grid does not run that kernel).
  * No reference counterpart. */
 int32_t mx_zpass_blocks_per_sm(const mx_ctx* ctx);
-/* 1 when the context runs the x- and y-pass of its inverse transforms as one
- * persistent kernel (the spectra between them kept in L2), 0 when it runs
- * them as two passes (MX_XY_PASS=split, or a grid size without that kernel).
- * No reference counterpart. */
-int32_t mx_xy_pass_fused(const mx_ctx* ctx);
 /* Filter radii of find_HII_bubbles for this configuration (largest first). */
 int32_t mx_filter_radii(const mx_ctx* ctx, double* radii, int32_t cap);
 

@@ -27,7 +27,7 @@ EXPORTS = [
     "mx_lightcone_init", "mx_ConstructLightcone", "mx_ConstructLightcone_device",
     "mx_construct_baryon_grids", "mx_construct_baryon_grids_device", "mx_calculate_Mvir_crit",
     "mx_calculate_Mvir_crit_device", "mx_set_xray_params", "mx_ps_loss_device", "mx_adjoint_device",
-    "mx_create_limited", "mx_fft_block_sizes", "mx_zpass_blocks_per_sm", "mx_xy_pass_fused", "mx_set_step_graph", "mx_batch_create", "mx_batch_run",
+    "mx_create_limited", "mx_fft_block_sizes", "mx_zpass_blocks_per_sm", "mx_set_step_graph", "mx_batch_create", "mx_batch_run",
     "mx_batch_run_graph", "mx_batch_destroy",
     "mx_batch_last_error",
 ]
@@ -86,8 +86,6 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mx_fft_block_sizes.restype = ctypes.c_int
         L.mx_zpass_blocks_per_sm.argtypes = [P]
         L.mx_zpass_blocks_per_sm.restype = ctypes.c_int32
-        L.mx_xy_pass_fused.argtypes = [P]
-        L.mx_xy_pass_fused.restype = ctypes.c_int32
         L.mx_set_step_graph.argtypes = [P, ctypes.c_int32]
         L.mx_set_step_graph.restype = ctypes.c_int
         L.mx_filter_radii.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int32]

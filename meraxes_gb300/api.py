@@ -97,10 +97,6 @@ class ReionGridStep:
         """Resident blocks per SM the threshold z-pass was tuned for (0: not run)."""
         return int(self.lib.mx_zpass_blocks_per_sm(self.ctx))
 
-    def xy_fused(self) -> bool:
-        """Whether the x- and y-pass run as one persistent kernel (k_fft_xy)."""
-        return bool(self.lib.mx_xy_pass_fused(self.ctx))
-
     def set_graph(self, on: bool = True):
         """Device steps (step() on CUDA tensors) captured and launched as one
         CUDA graph each (mx_set_step_graph)."""

@@ -584,158 +584,6 @@ __global__ void __launch_bounds__(YTHREADS, YTHREADS == 256 ? 3 : 2) k_fft_y(flo
   T::c(buf, [&](int y, int, float2 v) { col[y * HP] = v; });
 }
 
-// ---------------------------------------------------------------- x+y pass
-// The x- and y-passes of a batch in one persistent kernel, with the
-// spectra between them kept in L2.  The work is cut into chunks
-// c = (t * G + g) * n + r: tile t (TXC kz columns) of the spectrum of field
-// g at radius r.  A chunk's x items (one per |ky| <= D/2: rows ky and D - ky
-// of the tile filtered and transformed along x, as one x-pass block does for
-// one field) write D * D * TXC complex values, 32 MB at D = 512; its y items
-// (one per x: the column transformed along y in place, as one y-pass block)
-// read them back.  Blocks take items in a fixed order from a ticket counter:
-//   x items of chunk 0, then for c = 1 .. n_chunks - 1 the x items of chunk c
-//   followed by the y items of chunk c - 1, then the y items of the last chunk.
-// A y item therefore seldom waits, about two chunks are in flight, and the
-// y items overwrite the x items' stores while those are still in L2: the
-// spectrum crosses HBM once (the y items' stores leaving L2) instead of
-// three times (x stores, y loads, y stores).  Consecutive chunks of one
-// (t, g) differ only in the radius, so the tile's unfiltered columns come
-// from HBM once and from L2 for the other radii.
-//
-// A y item waits, bounded, until all x items of its chunk have finished.
-// x items wait for nothing and hold earlier tickets than every y item of
-// their chunk, so each wait ends once the blocks holding those x items
-// finish them.  The arithmetic of every item is that of the separate passes,
-// so the results are the same bit for bit.
-namespace {
-// Block-wide barrier that does not require the warps to be converged
-// (barrier.sync without .aligned).  k_fft_xy branches on the item index, a
-// value read from shared memory, so the compiler cannot prove its barriers
-// uniform; __syncthreads() (the .aligned form) there let the threads of a
-// block run into step B before step A's stores had landed (measured: wrong
-// and run-to-run different x items at 16 points per thread, exact with this
-// form).
-__device__ __forceinline__ void block_barrier() { asm volatile("barrier.sync 0;" ::: "memory"); }
-
-// Waits until *p >= target (acquire): false after the consumer wait limit
-// or 2 s.
-__device__ __forceinline__ bool counter_wait(const unsigned* p, unsigned target)
-{
-  const long long limit = consumer_wait_polls;
-  const unsigned long long t0 = global_ns();
-  for (long long i = 0;; i++) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    if (v >= target)
-      return true;
-    if (i >= limit || ((i & 255) == 255 && global_ns() - t0 > WAIT_LIMIT_NS))
-      return false;
-    __nanosleep(100);
-  }
-}
-}  // namespace
-
-template <int D, int NTHR>
-__global__ void __launch_bounds__(NTHR, NTHR == 256 && D < 512 ? 3 : 2) k_fft_xy(const __grid_constant__ XYArgs a)
-{
-  using P = TilePlan<D>;
-  using T = TileSteps<D, NTHR>;
-  constexpr int H = D / 2 + 1, HP = Pitch<D>::HP;
-  extern __shared__ float2 smem[];
-  float2* tw = smem;
-  float2* buf = smem + D;
-  float* wsm = reinterpret_cast<float*>(buf + P::BUF);
-  __shared__ unsigned s_item;
-  __shared__ int s_ok;
-  fill_twiddles<D>(tw);
-  const XPassArgs& x = a.x;
-  const int G = x.G, n = x.n;
-  const unsigned n_chunks = (unsigned)(P::NT * G * n);
-  constexpr unsigned PER = H + D;  // items of one chunk
-  const unsigned total = n_chunks * PER;
-  const int t0 = threadIdx.x % TXC;
-  float2 pts[T::NPTS];
-  for (;;) {
-    block_barrier();  // the previous item is done with buf, wsm and s_item
-    if (threadIdx.x == 0)
-      s_item = atomicAdd(a.sync, 1u);
-    block_barrier();
-    const unsigned q = s_item;
-    if (q >= total)
-      return;
-    // ticket -> (x item or y item, chunk, index within the chunk)
-    bool is_x;
-    unsigned c, idx;
-    if (q < (unsigned)H) {
-      is_x = true, c = 0, idx = q;
-    } else {
-      const unsigned k = (q - H) / PER + 1, rem = (q - H) % PER;
-      if (k < n_chunks)
-        is_x = rem < (unsigned)H, c = is_x ? k : k - 1, idx = is_x ? rem : rem - H;
-      else
-        is_x = false, c = n_chunks - 1, idx = rem;
-    }
-    const int r = (int)(c % (unsigned)n), g = (int)((c / (unsigned)n) % (unsigned)G);
-    const int kz0 = (int)(c / (unsigned)(n * G)) * TXC;
-    float2* spec = x.out + (long long)(r * G + g) * x.C;
-    if (is_x) {
-      const int kyp = (int)idx;
-      const float kyv = kcomp(kyp, D, x.delta_k);
-      const bool live = kz0 + t0 < H;
-      for (int i = threadIdx.x; i < H * TXC; i += NTHR) {
-        const int kx = i / TXC, tt = i % TXC;
-        wsm[i] = x.apply[r] ? x_weight(kx, kyv, kz0 + tt, D, x.delta_k, x.filter_type, x.R[r], x.sharpk_max, x.scale)
-                            : x.scale;
-      }
-      const float* wcol = wsm + t0;
-      const int n_rows = (kyp == 0 || kyp == D / 2) ? 1 : 2;
-      for (int h = 0; h < n_rows; h++) {
-        const int ky = h == 0 ? kyp : D - kyp;
-        const float2* __restrict__ src = x.in[g] + (long long)ky * HP + kz0 + t0;
-        T::for_each_input(
-          [&](int kx, int i) { pts[i] = live ? src[(long long)kx * (D * HP)] : make_float2(0.f, 0.f); });
-        block_barrier();  // weights written; the previous row's step C done with buf
-        T::a(buf, tw, [&](int kx, int, int i) {
-          float2 v = pts[i];
-          const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
-          v.x *= wv;
-          v.y *= wv;
-          return v;
-        });
-        block_barrier();
-        T::b(buf, tw);
-        block_barrier();
-        float2* __restrict__ dst = spec + (long long)ky * HP + kz0 + t0;
-        T::c(buf, [&](int xo, int, float2 v) { dst[(long long)xo * (D * HP)] = v; });
-      }
-      // release: every thread's stores, then one count for the block
-      __threadfence();
-      block_barrier();
-      if (threadIdx.x == 0)
-        atomicAdd(a.sync + 1 + c, 1u);
-    } else {
-      if (threadIdx.x == 0) {
-        s_ok = counter_wait(a.sync + 1 + c, (unsigned)H);
-        __threadfence();
-      }
-      block_barrier();
-      if (!s_ok) {
-        if (threadIdx.x == 0)
-          atomicOr(a.err, ERR_PIPELINE_TIMEOUT | ERR_XY_TIMEOUT);
-        return;
-      }
-      // the x items' stores, read from L2 (this SM's L1 never held them)
-      float2* col = spec + (long long)idx * D * HP + kz0 + t0;
-      T::for_each_input([&](int ky, int i) { pts[i] = __ldcg(col + ky * HP); });
-      T::a(buf, tw, [&](int, int, int i) { return pts[i]; });
-      block_barrier();
-      T::b(buf, tw);
-      block_barrier();
-      T::c(buf, [&](int y, int, float2 v) { col[y * HP] = v; });
-    }
-  }
-}
-
 // ------------------------------------------------------------------ z-pass
 // The z-pass reads, per block, TZ consecutive rows (row = x * D + y) of every
 // spectrum of the batch: TZ rows at the pitch HP, TZ*HP contiguous complex
@@ -1727,27 +1575,6 @@ static void launch_y(float2* data, long long C, int n_spectra, int threads, cuda
   else
     launch_y_t<D, 256>(data, C, n_spectra, s);
 }
-template <int D, int T>
-static void launch_xy_t(const XYArgs& a, cudaStream_t s)
-{
-  cudaFuncSetAttribute(k_fft_xy<D, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x<D>());
-  int dev = 0, sms = 1, per_sm = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_xy<D, T>, T, smem_x<D>());
-  const long long items = (long long)TilePlan<D>::NT * a.x.G * a.x.n * (D / 2 + 1 + D);
-  const long long blocks = std::min<long long>((long long)std::max(per_sm, 1) * sms, items);
-  cudaMemsetAsync(a.sync, 0, sizeof(unsigned) * (size_t)fft_xy_sync_words(D, a.x.G, a.x.n), s);
-  k_fft_xy<D, T><<<(unsigned)blocks, T, smem_x<D>(), s>>>(a);
-}
-template <int D>
-static void launch_xy(const XYArgs& a, int threads, cudaStream_t s)
-{
-  if (threads == 256)
-    launch_xy_t<D, 256>(a, s);
-  else
-    launch_xy_t<D, 512>(a, s);
-}
 template <int D, bool SPIN, bool RECOMB, int MINB>
 static void launch_zt_minb(const ZThresholdArgs& a, cudaStream_t s)
 {
@@ -1837,27 +1664,6 @@ bool launch_fft_y(int D, float2* data, long long C, int n_spectra, int threads, 
     case 96: launch_y_t<96, TILE_THREADS_3>(data, C, n_spectra, s); break;
     case 192: launch_y_t<192, TILE_THREADS_3>(data, C, n_spectra, s); break;
     default: return false;
-  }
-  fft_launches++;
-  return true;
-}
-
-bool fft_xy_supported(int D) { return D == 96 || D == 128 || D == 192 || D == 256 || D == 512; }
-
-long long fft_xy_sync_words(int D, int G, int n) { return 1 + (long long)(fft_pitch(D) / TXC) * G * n; }
-
-bool launch_fft_xy(int D, const XYArgs& args, int threads, cudaStream_t s)
-{
-  static const float kmax = sharpk_threshold();
-  XYArgs a = args;
-  a.x.sharpk_max = kmax;
-  switch (D) {
-    case 128: launch_xy<128>(a, threads, s); break;
-    case 256: launch_xy<256>(a, threads, s); break;
-    case 512: launch_xy<512>(a, threads, s); break;
-    case 96: launch_xy_t<96, TILE_THREADS_3>(a, s); break;
-    case 192: launch_xy_t<192, TILE_THREADS_3>(a, s); break;
-    default: return false;  // smaller grids: the separate passes (their spectra stay in L2 anyway)
   }
   fft_launches++;
   return true;

@@ -24,16 +24,6 @@ struct XPassArgs
   float sharpk_max;  // set by launch_fft_x_filter
 };
 
-// x- and y-pass of a batch in one persistent kernel (k_fft_xy): the same
-// transforms as launch_fft_x_filter followed by launch_fft_y, bit for bit.
-struct XYArgs
-{
-  XPassArgs x;
-  unsigned* sync;  // [0]: ticket; [1 + c]: finished x items of chunk c (fft_xy_sync_words)
-  unsigned* err;   // bits 2 and 8 (ERR_XY_TIMEOUT): a y item's wait for its chunk timed out
-};
-constexpr unsigned ERR_XY_TIMEOUT = 8u;
-
 // Forward R2C of G padded real grids into spectra [kx][ky][kz] with rows of
 // fft_pitch(D) complex values (the x-pass's input layout).
 struct FwdArgs
@@ -83,12 +73,6 @@ void launch_filter_accumulate(int D, float2* acc, const float2* U, float R, int 
 // threads per block of the x- and y-pass: 256 or 512
 bool launch_fft_x_filter(int D, const XPassArgs& a, int threads, cudaStream_t s);
 bool launch_fft_y(int D, float2* data, long long C, int n_spectra, int threads, cudaStream_t s);
-// k_fft_xy over a batch; the sync words are zeroed on the stream first.
-// Grids of 96, 128, 192, 256 and 512 (false for the others).
-bool fft_xy_supported(int D);
-bool launch_fft_xy(int D, const XYArgs& a, int threads, cudaStream_t s);
-// sync words launch_fft_xy needs for G fields and n radii
-long long fft_xy_sync_words(int D, int G, int n);
 // three launches: z (real rows -> half spectrum), y, x; threads of the y and
 // x passes 256 or 512
 bool launch_fft_forward(int D, const FwdArgs& a, int threads, cudaStream_t s);

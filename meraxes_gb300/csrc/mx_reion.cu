@@ -88,11 +88,6 @@ struct mx_ctx
   bool fused_fft = false;
   // threads per block of the fused x- and y-pass, chosen by tune_fft()
   int x_threads = 512, y_threads = 256;
-  // the x- and y-pass as one persistent kernel with the spectra between them
-  // kept in L2 (k_fft_xy) where the grid size has one; MX_XY_PASS=split
-  // launches the two passes
-  bool xy_fused = false;
-  unsigned* d_xy_sync = nullptr;  // its ticket and chunk counters
   // register budget of the threshold z-pass: 2 or 3 resident blocks per SM
   int z_blocks = 2;
   // 2-D tensor map of d_shells (cells x shells) for the evolve kernel's tile
@@ -297,7 +292,6 @@ mx_ctx::~mx_ctx()
   cudaFreeHost(h_tsc);
   cudaFree(d_shells);
   cudaFree(d_err);
-  cudaFree(d_xy_sync);
   cudaFree(d_xe_last);
   cudaFree(d_rr_x);
   cudaFree(d_rr_y);
@@ -380,8 +374,6 @@ void mx_ctx::alloc_scratch()
     cap = std::max<long long>(cap, 1);
   work_fields = cap;
   MX_CUDA(cudaMalloc(&d_work, spectrum * cap));
-  if (xy_fused)
-    MX_CUDA(cudaMalloc(&d_xy_sync, sizeof(unsigned) * fft_xy_sync_words(gd.D, MAX_FIELDS, MAX_RADII)));
   MX_CUDA(cudaMalloc(&d_in_ptrs, sizeof(float2*) * MAX_FIELDS));
   MX_CUDA(cudaMalloc(&d_partials, sizeof(double) * RED_BLOCKS * 8));
   MX_CUDA(cudaMalloc(&d_ps_partials, sizeof(double) * RED_BLOCKS * 3 * PS_MAX_BINS));
@@ -472,25 +464,13 @@ struct FhbDownloads
 float* mx_grids::* const SLAB_OUTPUTS[] = { &mx_grids::xH,   &mx_grids::z_at_ionization,    &mx_grids::r_bubble,
                                              &mx_grids::J_21, &mx_grids::J_21_at_ionization, &mx_grids::Gamma12 };
 
-// x- and y-pass of a batch of xa.n radii x xa.G fields into xa.out: one
-// persistent kernel (k_fft_xy) where the context has one, else the two
-// passes.  Algorithmic bytes of each pass: the unfiltered spectra read once
-// and the filtered ones written (x-pass), the filtered ones read and written
-// (y-pass); of the persistent kernel, which moves the spectra between the
-// passes through L2, those of the x-pass alone.
+// x- and y-pass of a batch of xa.n radii x xa.G fields into xa.out.
+// Algorithmic bytes: the unfiltered spectra read once and the filtered ones
+// written (x-pass), the filtered ones read and written (y-pass).
 static void run_xy(mx_ctx* c, const XPassArgs& xa, cudaStream_t s)
 {
   const double B8C = 8.0 * (double)c->gd.C;
   const double x_bytes = B8C * xa.G * (1 + xa.n), y_bytes = 2.0 * B8C * xa.G * xa.n;
-  if (c->xy_fused) {
-    XYArgs a;
-    a.x = xa;
-    a.sync = c->d_xy_sync;
-    a.err = c->d_err;
-    Prof pr(c, "fft_xy", x_bytes, s);
-    launch_fft_xy(c->gd.D, a, c->x_threads, s);
-    return;
-  }
   {
     Prof pr(c, "fft_x_filter", x_bytes, s);
     launch_fft_x_filter(c->gd.D, xa, c->x_threads, s);
@@ -769,8 +749,7 @@ static void run_find_HII_bubbles(mx_ctx* c, int snapshot, const mx_grids* g, mx_
   after(c, s, [c, s, sums, errw, out, total, uvb]() {
     if (*errw) {
       MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
-      throw CudaError{ MX_ECUDA, std::string("find_HII_bubbles: a transform pipeline wait timed out") +
-                                   ((*errw & ERR_XY_TIMEOUT) ? " (x+y pass)" : "") };
+      throw CudaError{ MX_ECUDA, "find_HII_bubbles: a transform pipeline wait timed out" };
     }
     if (out) {
       out->volume_weighted_global_xH = sums[0] / total;
@@ -1239,10 +1218,8 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
   after(c, s, [=]() {
     if (*errw) {
       MX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), s));
-      throw CudaError{ MX_ECUDA, (*errw & 2u) ? std::string("ComputeTs: a pipeline wait (transform or shell copies) "
-                                                            "timed out") +
-                                                  ((*errw & ERR_XY_TIMEOUT) ? " (x+y pass)" : "")
-                                              : std::string("ComputeTs: spin-temperature iteration did not converge") };
+      throw CudaError{ MX_ECUDA, (*errw & 2u) ? "ComputeTs: a pipeline wait (transform or shell copies) timed out"
+                                              : "ComputeTs: spin-temperature iteration did not converge" };
     }
     if (hw && !hw->err.empty())
       throw CudaError{ MX_ETABLE, "ComputeTs tables: " + hw->err };
@@ -2572,10 +2549,6 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
   if (const char* env = std::getenv("MX_TRANSFORM"))
     if (std::string(env) == "cufft")
       c->fused_fft = false;
-  c->xy_fused = c->fused_fft && fft_xy_supported(p.grid_dim);
-  if (const char* env = std::getenv("MX_XY_PASS"))
-    if (std::string(env) == "split")
-      c->xy_fused = false;
   try {
     if (cudaGetDevice(&c->device) != cudaSuccess)
       throw CudaError{ MX_ECUDA, "no CUDA device" };
@@ -2666,13 +2639,6 @@ int32_t mx_zpass_blocks_per_sm(const mx_ctx* ctx)
   if (!ctx)
     return MX_EINVAL;
   return ctx->fused_fft && (ctx->gd.D & (ctx->gd.D - 1)) == 0 ? ctx->z_blocks : 0;
-}
-
-int32_t mx_xy_pass_fused(const mx_ctx* ctx)
-{
-  if (!ctx)
-    return MX_EINVAL;
-  return ctx->xy_fused ? 1 : 0;
 }
 
 int mx_fft_block_sizes(const mx_ctx* ctx, int32_t* x_threads, int32_t* y_threads)
