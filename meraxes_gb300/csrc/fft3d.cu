@@ -518,31 +518,38 @@ __global__ void __launch_bounds__(XTHREADS, XTHREADS == 256 && D < 512 ? 3 : 2) 
                         : a.scale;
   }
   const float* wcol = wsm + t0;
-  // items k = (row, field): the fields of row ky = kyp, then those of row
-  // D - kyp.  The points of item k + 1 are loaded after step B of item k, so
-  // that the loads are in flight during its step C (the registers of pts are
-  // free from step A on; step C holds only its own R3 points).
-  const int n_items = ((kyp == 0 || kyp == D / 2) ? 1 : 2) * a.G;
-  auto item_ky = [&](int k) { return k < a.G ? kyp : D - kyp; };
-  read_points(item_ky(0), 0);
-  __syncthreads();
-  for (int k = 0; k < n_items; k++) {
-    const int ky = item_ky(k), g = k % a.G;
-    T::a(buf, tw, [&](int kx, int, int i) {
-      float2 x = pts[i];
-      const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
-      x.x *= wv;
-      x.y *= wv;
-      return x;
-    });
-    __syncthreads();
-    T::b(buf, tw);
-    __syncthreads();
-    if (k + 1 < n_items)
-      read_points(item_ky(k + 1), (k + 1) % a.G);
-    float2* __restrict__ dst = a.out + (long long)(r * a.G + g) * a.C + (long long)ky * Pitch<D>::HP + kz0 + t0;
-    T::c(buf, [&](int x, int, float2 v) { dst[(long long)x * (D * Pitch<D>::HP)] = v; });
-    __syncthreads();
+  const int n_rows = (kyp == 0 || kyp == D / 2) ? 1 : 2;
+  for (int h = 0; h < n_rows; h++) {
+    const int ky = h == 0 ? kyp : D - kyp;
+    read_points(ky, 0);
+    if (h == 0)
+      __syncthreads();
+    // steps B and C of field g after its step A
+    auto finish = [&](int g) {
+      __syncthreads();
+      T::b(buf, tw);
+      __syncthreads();
+      float2* __restrict__ dst =
+        a.out + (long long)(r * a.G + g) * a.C + (long long)ky * Pitch<D>::HP + kz0 + t0;
+      T::c(buf, [&](int x, int, float2 v) { dst[(long long)x * (D * Pitch<D>::HP)] = v; });
+      __syncthreads();
+    };
+    auto step_a = [&]() {
+      T::a(buf, tw, [&](int kx, int, int i) {
+        float2 x = pts[i];
+        const float wv = wcol[(kx <= D / 2 ? kx : D - kx) * TXC];
+        x.x *= wv;
+        x.y *= wv;
+        return x;
+      });
+    };
+    step_a();
+    finish(0);
+    for (int g = 1; g < a.G; g++) {
+      read_points(ky, g);
+      step_a();
+      finish(g);
+    }
   }
 }
 
