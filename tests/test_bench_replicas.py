@@ -30,7 +30,16 @@ def _rank_main(rank, world, port, out):
     bench.barrier(world)
     args = bench.parse_args(["--impl", "reference", "--steps", "1", "--warmup", "0", "--grid", "32"])
     ref, _ = bench.run_reference(args, rank, world)
-    out.put((rank, value, ref is None))
+    ok = ref is None
+    if ref is not None:
+        # the reference arm's line: the contract's keys, its own CPU baseline and an e2e with no copies
+        want = {"impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"}
+        ok = (want <= set(ref) and ref["impl"] == "reference" and ref["metric"] == bench.METRIC
+              and ref["higher_is_better"] is False and ref["value"] > 0
+              and ref["cpu_baseline"]["value"] == ref["value"] and ref["cpu_baseline"]["kind"] == "port"
+              and ref["e2e"]["h2d_bytes_per_step"] == 0 and ref["e2e"]["d2h_bytes_per_step"] == 0)
+    out.put((rank, value, ok))
     import torch.distributed as dist
 
     dist.destroy_process_group()
@@ -52,5 +61,5 @@ def test_two_replicas_report_slowest_rank_over_all_snapshots():
         assert p.exitcode == 0
     # max over ranks = 200 ms for 4 snapshots on each of 2 replicas
     assert [v for _, v, _ in res] == [25.0, 25.0]
-    # only rank 0 runs the reference arm
-    assert res[1][2] is True
+    # only rank 0 runs the reference arm, and its line keeps the contract
+    assert res[0][2] is True and res[1][2] is True
