@@ -149,9 +149,10 @@ __device__ float spline_f(const float* x, const float* y, const float* c, int n,
       lo = mid;
   }
   const float h = x[lo + 1] - x[lo];
+  const float ih = __fdividef(1.0f, h);
   const float dx = xv - x[lo];
-  const float b = (y[lo + 1] - y[lo]) / h - h * (c[lo + 1] + 2.0f * c[lo]) * (1.0f / 3.0f);
-  const float d = (c[lo + 1] - c[lo]) / (3.0f * h);
+  const float b = (y[lo + 1] - y[lo]) * ih - h * (c[lo + 1] + 2.0f * c[lo]) * (1.0f / 3.0f);
+  const float d = (c[lo + 1] - c[lo]) * ih * (1.0f / 3.0f);
   return y[lo] + dx * (b + dx * (c[lo] + dx * d));
 }
 
@@ -175,7 +176,7 @@ __device__ float kappa_f(const TsDevConst& c, int which, float T)
 // alpha_A (Abel et al. 1997 fit), XRayHeatingFunctions.c:1450-1458, in Horner form
 __device__ float alpha_A_f(float T)
 {
-  const float l = logf(T / 1.1604505e4f);
+  const float l = logf(T * (1.0f / 1.1604505e4f));
   float p = -3.07113524e-9f;
   p = p * l - 1.85676704e-8f;
   p = p * l + 5.75561414e-7f;
@@ -190,7 +191,10 @@ __device__ float alpha_A_f(float T)
 }
 
 // get_Ts in FP32; returns false when a stopping test is too close to the
-// reference's 1e-3 criterion for FP32 to decide it like FP64 would.
+// reference's 1e-3 criterion for FP32 to decide it like FP64 would.  Its
+// quotients are reciprocals or quotients of __fdividef (2 ulp), well inside
+// that 1e-5 band around the criterion; get_Ts_grad repeats the same
+// operations, so the adjoint runs the forward's iteration count.
 __device__ bool get_Ts_f(const TsDevConst& c, float delta, float TK, float xe, float Jalpha, float* TS_out,
                          float* xalpha)
 {
@@ -199,16 +203,19 @@ __device__ bool get_Ts_f(const TsDevConst& c, float delta, float TK, float xe, f
   const float xc = c.fxc[0] * ((1.0f - xe) * opd) * kappa_f(c, 0, TK) +
                    c.fxc[1] * (xe * opd) * kappa_f(c, 1, TK) + c.fxc[2] * (xe * opd) * kappa_f(c, 2, TK);
   float TS, xa = 0.0f;
+  const float iTK = __fdividef(1.0f, TK);
+  const float iTrad = __fdividef(1.0f, Trad);
   if (Jalpha > 1.0e-20f) {
     TS = Trad;
     float TSold = 0.0f;
     const float tgp = c.ftgp * opd * (1.0f - xe);
-    const float xi = cbrtf(1.0e-7f * tgp / TK / TK);
+    const float xi = cbrtf(1.0e-7f * tgp * iTK * iTK);
     const float den = 1.0f + 2.98394f * xi + 1.53583f * xi * xi + 3.85289f * xi * xi * xi;
-    const float iTK = 1.0f / TK;
+    const float iden = __fdividef(1.0f, den);
     int it = 0;
     for (;;) {
-      const float rel = fabsf(TS - TSold) / TS;
+      const float iTS = __fdividef(1.0f, TS);
+      const float rel = fabsf(TS - TSold) * iTS;
       if (fabsf(rel - 1.0e-3f) < 1.0e-5f)
         return false;
       if (!(rel > 1.0e-3f))
@@ -216,17 +223,16 @@ __device__ bool get_Ts_f(const TsDevConst& c, float delta, float TK, float xe, f
       if (++it > TS_MAX_ITER)
         return false;
       TSold = TS;
-      const float iTS = 1.0f / TS;
-      float St = 1.0f - 0.0631789f * iTK + 0.115995f * iTK * iTK - 0.401403f * iTS * iTK;
-      St += 0.336463f * iTS * iTK * iTK;
-      St /= den;
+      const float St =
+        (1.0f - 0.0631789f * iTK + 0.115995f * iTK * iTK - 0.401403f * iTS * iTK + 0.336463f * iTS * iTK * iTK) * iden;
       xa = c.fxa * St * Jalpha;
-      const float Tceff = 1.0f / (iTK + 0.405535f * iTK * (iTS - iTK));
-      TS = 1.0f / ((1.0f / Trad + xa / Tceff + xc * iTK) / (1.0f + xa + xc));
+      // 1 / Tceff = iTK + 0.405535 iTK (iTS - iTK)
+      const float iTceff = iTK + 0.405535f * iTK * (iTS - iTK);
+      TS = __fdividef(1.0f + xa + xc, iTrad + xa * iTceff + xc * iTK);
     }
     *xalpha = xa;
   } else {
-    TS = 1.0f / ((1.0f / Trad + xc / TK) / (1.0f + xc));
+    TS = __fdividef(1.0f + xc, iTrad + xc * iTK);
     *xalpha = 0.0f;
   }
   *TS_out = fabsf(TS);
@@ -341,7 +347,7 @@ __global__ void __launch_bounds__(RED_THREADS, 2)
     while (lo > 0 && xcall < c.xhii[lo])
       lo--;
     const int hi = lo + 1;
-    const float w = (xcall - c.xhii[lo]) / (c.xhii[hi] - c.xhii[lo]);
+    const float w = __fdividef(xcall - c.xhii[lo], c.xhii[hi] - c.xhii[lo]);
     float heat = 0.f, ion = 0.f, lya = 0.f, star = 0.f;
     if (light) {
       const bool arrived = bulk::mbar_wait(&bars[k % STAGES], (unsigned)(k / STAGES) & 1u);
@@ -381,14 +387,16 @@ __global__ void __launch_bounds__(RED_THREADS, 2)
     if (!valid)
       continue;
     const float opd = 1.0f + delta;
-    const float dxheat_dzp = heat / (1.0f + xe);
+    const float i1xe = __fdividef(1.0f, 1.0f + xe);
+    const float dxheat_dzp = heat * i1xe;
     const float dxe_dzp = ion - c.fksink * alpha_A_f(T) * xe * xe * opd;
     float dadia = c.fadia0;
+    // fdgrowth / (1/delta + fgrowth), as fdgrowth delta / (1 + fgrowth delta)
     if (fabsf(delta) > (float)FRACT_FLOAT_ERR)
-      dadia += c.fdgrowth / (1.0f / delta + c.fgrowth);
+      dadia += __fdividef(c.fdgrowth * delta, 1.0f + c.fgrowth * delta);
     dadia *= (2.0f / 3.0f) * T;
-    const float dspec = -dxe_dzp * T / (1.0f + xe);
-    const float dcomp = c.fccomp * (xe / (1.0f + xe + c.ff_he)) * (c.ftrad - T);
+    const float dspec = -dxe_dzp * T * i1xe;
+    const float dcomp = c.fccomp * __fdividef(xe, 1.0f + xe + c.ff_he) * (c.ftrad - T);
     const float d1 = dxheat_dzp + dcomp + dspec + dadia;
     const float Jalpha = lya * opd + star;
 
@@ -470,9 +478,10 @@ __device__ float dlnkappa_dlnT(const TsDevConst& c, int which, float T)
       lo = mid;
   }
   const float h = x[lo + 1] - x[lo];
+  const float ih = __fdividef(1.0f, h);
   const float dx = lt - x[lo];
-  const float b = (y[lo + 1] - y[lo]) / h - h * (cc[lo + 1] + 2.0f * cc[lo]) * (1.0f / 3.0f);
-  const float d = (cc[lo + 1] - cc[lo]) / (3.0f * h);
+  const float b = (y[lo + 1] - y[lo]) * ih - h * (cc[lo + 1] + 2.0f * cc[lo]) * (1.0f / 3.0f);
+  const float d = (cc[lo + 1] - cc[lo]) * ih * (1.0f / 3.0f);
   return b + dx * (2.0f * cc[lo] + 3.0f * d * dx);
 }
 
@@ -497,17 +506,19 @@ __device__ TsGrad get_Ts_grad(const TsDevConst& c, float delta, float TK, float 
   const float xc = c.fxc[0] * ((1.0f - xe) * opd) * k[0] + c.fxc[1] * (xe * opd) * k[1] + c.fxc[2] * (xe * opd) * k[2];
   const float xc_T = c.fxc[0] * ((1.0f - xe) * opd) * dk[0] + c.fxc[1] * (xe * opd) * dk[1] + c.fxc[2] * (xe * opd) * dk[2];
   const float xc_x = opd * (-c.fxc[0] * k[0] + c.fxc[1] * k[1] + c.fxc[2] * k[2]);
-  const float iTK = 1.0f / TK;
+  const float iTK = __fdividef(1.0f, TK);
+  const float iTrad = __fdividef(1.0f, Trad);
   TsGrad g;
   if (J > 1.0e-20f) {
     const float tgp = c.ftgp * opd * (1.0f - xe);
-    const float q = 1.0e-7f * tgp / TK / TK;
+    const float q = 1.0e-7f * tgp * iTK * iTK;
     const float xi = cbrtf(q);
     // d xi: xi = q^(1/3); dq/dTK = -2 q / TK, dq/dxe = -1e-7 ftgp opd / TK^2
     const float xi_q = q > 0.0f ? xi / (3.0f * q) : 0.0f;
     const float xi_T = xi_q * (-2.0f * q / TK);
     const float xi_x = xi_q * (-1.0e-7f * c.ftgp * opd / TK / TK);
     const float den = 1.0f + 2.98394f * xi + 1.53583f * xi * xi + 3.85289f * xi * xi * xi;
+    const float iden = __fdividef(1.0f, den);
     const float den_xi = 2.98394f + 2.0f * 1.53583f * xi + 3.0f * 3.85289f * xi * xi;
     const float den_T = den_xi * xi_T, den_x = den_xi * xi_x;
     const float iTK_T = -iTK * iTK;
@@ -515,34 +526,35 @@ __device__ TsGrad get_Ts_grad(const TsDevConst& c, float delta, float TK, float 
     float TS_T = 0.f, TS_x = 0.f, TS_J = 0.f;  // d TS
     int it = 0;
     for (;;) {
-      const float rel = fabsf(TS - TSold) / TS;
+      const float iTS = __fdividef(1.0f, TS);
+      const float rel = fabsf(TS - TSold) * iTS;
       if (!(rel > 1.0e-3f) || ++it > TS_MAX_ITER)
         break;
       TSold = TS;
-      const float iTS = 1.0f / TS;
       const float iTS_T = -iTS * iTS * TS_T, iTS_x = -iTS * iTS * TS_x, iTS_J = -iTS * iTS * TS_J;
       const float num = 1.0f - 0.0631789f * iTK + 0.115995f * iTK * iTK - 0.401403f * iTS * iTK + 0.336463f * iTS * iTK * iTK;
       const float num_iTK = -0.0631789f + 2.0f * 0.115995f * iTK - 0.401403f * iTS + 2.0f * 0.336463f * iTS * iTK;
       const float num_iTS = -0.401403f * iTK + 0.336463f * iTK * iTK;
       const float num_T = num_iTK * iTK_T + num_iTS * iTS_T;
       const float num_x = num_iTS * iTS_x, num_J = num_iTS * iTS_J;
-      const float St = num / den;
-      const float St_T = (num_T - St * den_T) / den, St_x = (num_x - St * den_x) / den, St_J = num_J / den;
+      const float St = num * iden;
+      const float St_T = (num_T - St * den_T) * iden, St_x = (num_x - St * den_x) * iden, St_J = num_J * iden;
       const float xa = c.fxa * St * J;
       const float xa_T = c.fxa * St_T * J, xa_x = c.fxa * St_x * J, xa_J = c.fxa * (St_J * J + St);
       // 1 / Tceff = iTK + 0.405535 iTK (iTS - iTK)
       const float E = iTK + 0.405535f * iTK * (iTS - iTK);
       const float E_T = iTK_T + 0.405535f * (iTK_T * (iTS - iTK) + iTK * (iTS_T - iTK_T));
       const float E_x = 0.405535f * iTK * iTS_x, E_J = 0.405535f * iTK * iTS_J;
-      const float A = 1.0f / Trad + xa * E + xc * iTK;
+      const float A = iTrad + xa * E + xc * iTK;
       const float A_T = xa_T * E + xa * E_T + xc_T * iTK + xc * iTK_T;
       const float A_x = xa_x * E + xa * E_x + xc_x * iTK, A_J = xa_J * E + xa * E_J;
       const float B = 1.0f + xa + xc;
       const float B_T = xa_T + xc_T, B_x = xa_x + xc_x, B_J = xa_J;
-      TS = 1.0f / (A / B);
-      TS_T = (B_T - TS * A_T) / A;
-      TS_x = (B_x - TS * A_x) / A;
-      TS_J = (B_J - TS * A_J) / A;
+      TS = __fdividef(B, A);
+      const float iA = __fdividef(1.0f, A);
+      TS_T = (B_T - TS * A_T) * iA;
+      TS_x = (B_x - TS * A_x) * iA;
+      TS_J = (B_J - TS * A_J) * iA;
     }
     g.TS = TS;
     g.dT = TS_T;
@@ -550,8 +562,8 @@ __device__ TsGrad get_Ts_grad(const TsDevConst& c, float delta, float TK, float 
     g.dJ = TS_J;
   } else {
     // TS = (1 + xc) / (1/Trad + xc/TK)
-    const float A = 1.0f / Trad + xc * iTK, B = 1.0f + xc;
-    g.TS = 1.0f / (A / B);
+    const float A = iTrad + xc * iTK, B = 1.0f + xc;
+    g.TS = __fdividef(B, A);
     const float A_T = xc_T * iTK - xc * iTK * iTK, A_x = xc_x * iTK;
     g.dT = (xc_T - g.TS * A_T) / A;
     g.dxe = (xc_x - g.TS * A_x) / A;
@@ -651,7 +663,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, i
     while (lo > 0 && xcall < c.xhii[lo])
       lo--;
     const int hi = lo + 1;
-    const float w = (xcall - c.xhii[lo]) / (c.xhii[hi] - c.xhii[lo]);
+    const float w = __fdividef(xcall - c.xhii[lo], c.xhii[hi] - c.xhii[lo]);
     float heat = 0.f, ion = 0.f, lya = 0.f, star = 0.f, dheat = 0.f, dion = 0.f, dlya = 0.f;
     const float* st = nullptr;
     if (light) {
@@ -692,15 +704,17 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, i
       dion = fmaf(w, dih - dil, dil);
       dlya = fmaf(w, dlh - dll, dll);
     }
-    // forward of the cell (k_evolve_f32), keeping the clamp states
+    // forward of the cell (k_evolve_f32, the same operations), keeping the
+    // clamp states
+    const float i1xe = __fdividef(1.0f, 1.0f + xe);
     const float dxe_dzp = ion - c.fksink * alpha_A_f(T) * xe * xe * opd;
     float dadia = c.fadia0;
     if (fabsf(delta) > (float)FRACT_FLOAT_ERR)
-      dadia += c.fdgrowth / (1.0f / delta + c.fgrowth);
+      dadia += __fdividef(c.fdgrowth * delta, 1.0f + c.fgrowth * delta);
     dadia *= (2.0f / 3.0f) * T;
-    const float dspec = -dxe_dzp * T / (1.0f + xe);
-    const float dcomp = c.fccomp * (xe / (1.0f + xe + c.ff_he)) * (c.ftrad - T);
-    const float d1 = heat / (1.0f + xe) + dcomp + dspec + dadia;
+    const float dspec = -dxe_dzp * T * i1xe;
+    const float dcomp = c.fccomp * __fdividef(xe, 1.0f + xe + c.ff_he) * (c.ftrad - T);
+    const float d1 = heat * i1xe + dcomp + dspec + dadia;
     const float Jalpha = lya * opd + star;
     float xn = xe + dxe_dzp * c.fdzp;
     bool xe_free = true;
@@ -725,8 +739,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_evolve_adjoint(AdjointArgs a, i
     xe_new_bar += TS_bar * tg.dxe;
     const float J_bar = TS_bar * tg.dJ;
     const float d1_bar = T_free ? Tn_bar * c.fdzp : 0.0f;
-    const float dxe_bar = (xe_free ? xe_new_bar * c.fdzp : 0.0f) + d1_bar * (-T / (1.0f + xe));
-    const float heat_bar = d1_bar / (1.0f + xe);
+    const float dxe_bar = (xe_free ? xe_new_bar * c.fdzp : 0.0f) + d1_bar * (-T * i1xe);
+    const float heat_bar = d1_bar * i1xe;
     const float ion_bar = dxe_bar;
     const float lya_bar = J_bar * opd;
     const float star_bar = J_bar;
