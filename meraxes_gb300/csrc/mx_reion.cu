@@ -75,6 +75,11 @@ struct mx_ctx
   double stored_fcoll[1000];
   cudaStream_t stream = nullptr;
   cudaStream_t copy_stream = nullptr;  // host-pointer mx_step: copies that overlap the compute
+  // host-pointer mx_step: ComputeTs's collapse fraction and <x_e> beside the
+  // shells (they wait for other uploads); ev_cf marks their sums on the host
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t ev_cf = nullptr;
+  bool early_shells = true;  // MX_TS_EARLY_SHELLS=0: the collapse fraction first
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
   // host-pointer mx_step: ComputeTs inputs arriving on the copy stream
   // (TsUploads)
@@ -302,13 +307,15 @@ mx_ctx::~mx_ctx()
     cudaEventDestroy(ev_a);
   if (ev_b)
     cudaEventDestroy(ev_b);
-  for (cudaEvent_t e : { ev_ts_first, ev_ts_sfr, ev_ts_tk, ev_state })
+  for (cudaEvent_t e : { ev_ts_first, ev_ts_sfr, ev_ts_tk, ev_state, ev_cf })
     if (e)
       cudaEventDestroy(e);
   for (cudaEvent_t e : ev_slices)
     cudaEventDestroy(e);
   if (copy_stream)
     cudaStreamDestroy(copy_stream);
+  if (aux_stream)
+    cudaStreamDestroy(aux_stream);
   if (stream)
     cudaStreamDestroy(stream);
 }
@@ -1083,7 +1090,11 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
   const double* evolve_sums = nullptr;   // read back: J_alpha, xalpha, Xheat, Xion sums
   std::shared_ptr<TsHostWork> hw;        // host node of a captured step
 
-  if (up) {
+  // host-pointer step, inhomogeneous: the shells start as soon as sfr has
+  // landed, and the collapse fraction waits for its three grids on the side
+  // stream (below)
+  const bool early_shells = up && !sp.homogeneous && !c->capturing && c->early_shells;
+  if (up && !early_shells) {
     MX_CUDA(cudaStreamWaitEvent(s, up->first, 0));
     if (sp.homogeneous) {
       MX_CUDA(cudaStreamWaitEvent(s, up->sfr, 0));
@@ -1121,6 +1132,31 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
     ca.R3 = std::pow(R0, 3.0);
     ca.pixel_volume = pixel_volume;
     ca.partials = c->d_partials;
+    if (early_shells) {
+      // the shells first on s; the sums on the side stream after the grids
+      // they read, copied to the host, where the tables wait for them
+      cudaStream_t as = c->aux_stream;
+      MX_CUDA(cudaStreamWaitEvent(as, up->first, 0));
+      {
+        Prof pr(c, "k_cf_xe", 3.0 * 4.0 * (double)gd.N, as);
+        launch_cf_xe(ca, gd, as);
+      }
+      launch_finalize(c->d_partials, 2, c->d_sums, as);
+      MX_CUDA(cudaMemcpyAsync(c->h_sums, c->d_sums, sizeof(double) * 2, cudaMemcpyDeviceToHost, as));
+      MX_CUDA(cudaEventRecord(c->ev_cf, as));
+      compute_shells(c, sp, g->sfr, g->sfr_histories, s, up);
+      MX_CUDA(cudaEventSynchronize(c->ev_cf));
+      collapse_fraction = c->h_sums[0] / total;
+      x_e_ave = c->h_sums[1] / total;
+      c->stored_fcoll[snapshot] = collapse_fraction;
+      FreqTables ft;
+      build_freq_tables(p, c->d, c->ht, c->zz, c->stored_fcoll, snapshot, sp, x_e_ave, sp.weight_after, c->nthreads,
+                        &ft);
+      fill_ts_constants(c, t, sp, ft, zp, prev_z, collapse_fraction, pixel_volume);
+      // the evolve kernel rewrites x_e_box_prev, which the side stream read
+      MX_CUDA(cudaStreamWaitEvent(s, c->ev_cf, 0));
+      MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
+    } else {
     {
       Prof pr(c, "k_cf_xe", 3.0 * 4.0 * (double)gd.N, s);
       launch_cf_xe(ca, gd, s);
@@ -1175,6 +1211,7 @@ static void run_ComputeTs(mx_ctx* c, int snapshot, const mx_grids* g, mx_globals
 
       fill_ts_constants(c, t, sp, ft, zp, prev_z, collapse_fraction, pixel_volume);
       MX_CUDA(cudaMemcpyAsync(c->d_tsc, t, sizeof(TsDevConst), cudaMemcpyHostToDevice, s));
+    }
     }
     EvolveArgs ea;
     ea.shells = c->d_shells;
@@ -2544,6 +2581,8 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
   c->nthreads = std::max(1, std::min(64, hw_threads()));
   if (const char* env = std::getenv("MX_HOST_THREADS"))
     c->nthreads = std::max(1, std::atoi(env));
+  if (const char* env = std::getenv("MX_TS_EARLY_SHELLS"))
+    c->early_shells = std::atoi(env) != 0;
 
   c->fused_fft = fft3d_supported(p.grid_dim);
   if (const char* env = std::getenv("MX_TRANSFORM"))
@@ -2563,6 +2602,8 @@ static int create_ctx(const mx_params* params, const char* tables_dir, size_t wo
     }
     MX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     MX_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    MX_CUDA(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
+    MX_CUDA(cudaEventCreateWithFlags(&c->ev_cf, cudaEventDisableTiming));
     MX_CUDA(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
     MX_CUDA(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
     MX_CUDA(cudaEventCreateWithFlags(&c->ev_ts_first, cudaEventDisableTiming));
@@ -2944,8 +2985,9 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
       late_out.push_back({ &mx_grids::delta_T, false, OUT });
     }
     // The copy stream starts after the compute stream's earlier work and
-    // carries every input: first what ComputeTs reads first (stars, deltax,
-    // x_e_box_prev), then sfr, the SFR-history slices in the order the shell
+    // carries every input: first sfr (the shells of the current SFR start on
+    // it), then what ComputeTs's collapse fraction reads (stars, deltax,
+    // x_e_box_prev), the SFR-history slices in the order the shell
     // operations first read them (slices no operation reads are not needed),
     // Tk_box, and the find_HII_bubbles inputs.  The compute stream waits for
     // each right before its first use (TsUploads), so most of the upload runs
@@ -2957,12 +2999,18 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
       auto upload = [&](float* mx_grids::*member, bool padded) {
         copy_fields(ctx, host, { { member, padded, IN } }, IN, cs);
       };
+      if (ctx->early_shells) {
+        upload(&mx_grids::sfr, true);
+        MX_CUDA(cudaEventRecord(ctx->ev_ts_sfr, cs));
+      }
       upload(&mx_grids::stars, true);
       upload(&mx_grids::deltax, true);
       upload(&mx_grids::x_e_box_prev, true);
       MX_CUDA(cudaEventRecord(ctx->ev_ts_first, cs));
-      upload(&mx_grids::sfr, true);
-      MX_CUDA(cudaEventRecord(ctx->ev_ts_sfr, cs));
+      if (!ctx->early_shells) {
+        upload(&mx_grids::sfr, true);
+        MX_CUDA(cudaEventRecord(ctx->ev_ts_sfr, cs));
+      }
       while ((int)ctx->ev_slices.size() < ctx->n_hist) {
         cudaEvent_t e = nullptr;
         MX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));

@@ -162,6 +162,39 @@ def test_shell_map_gives_identical_results(name, D, monkeypatch):
             assert a[k] == b[k], k
 
 
+# mx_step on host grids starts ComputeTs's shells as soon as sfr has landed
+# and computes the collapse fraction on a side stream (MX_TS_EARLY_SHELLS=0:
+# the collapse fraction first, on the compute stream): the same grids.
+@pytest.mark.parametrize("name,D", [("evolve16", 32), ("full24", 64)])
+def test_early_shells_give_identical_results(name, D, monkeypatch):
+    from cases import initial
+    from meraxes_gb300 import synthetic as syn
+    from meraxes_gb300.api import ReionGridStep
+
+    c = CASES[name]
+    w = Case(name, c.base, D, c.overrides, c.fesc, c.snapshots).workload()
+    runs = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("MX_TS_EARLY_SHELLS", flag)
+        step = ReionGridStep(w.params, w.redshifts)
+        gen = syn.FieldGenerator(w)
+        st = initial(w, step.n_sfr_histories)
+        glob = []
+        for s in w.snapshots:
+            st.update(gen.inputs(s, step.n_sfr_histories))
+            glob.append(step.step(s, st))
+        runs.append((st, glob))
+        step.close()
+    (sa, ga), (sb, gb) = runs
+    for k in OUTPUT_GRIDS:
+        if k in sa:
+            assert np.array_equal(sa[k], sb[k]), k
+    for a, b in zip(ga, gb):
+        for k in ("volume_weighted_global_xH", "volume_ave_TS", "volume_ave_Tb", "volume_ave_xe", "x_e_ave",
+                  "collapse_fraction"):
+            assert a[k] == b[k], k
+
+
 # Radii (and ComputeTs shells) go through the transforms in batches sized by
 # the work buffer; at 512^3 find_HII_bubbles takes two.  Small batches
 # (MX_MAX_BATCH_SPECTRA) must give the same grids as one batch, bit for bit.
