@@ -3055,7 +3055,11 @@ int mx_step(mx_ctx* ctx, int32_t snapshot, const mx_grids* host, mx_globals* out
       copy_fields(ctx, host, ts_out, OUT, cs);
     }
     MX_CUDA(cudaStreamWaitEvent(s, ctx->ev_b, 0));
-    FhbDownloads dl{ cs, ctx->ev_a, host, 4, false, ctx->ev_state };
+    // eight row slabs: the outputs of all but the last eighth go back while the
+    // threshold pass computes (at 512^3, two paired runs put eight 1.7 and 16 ms
+    // ahead of four, within the run-to-run spread of e2e on one host, and
+    // sixteen behind both)
+    FhbDownloads dl{ cs, ctx->ev_a, host, 8, false, ctx->ev_state };
     run_find_HII_bubbles(ctx, snapshot, &m, out, s, &dl);
     launches += out ? out->gpu_launches : 0;
     if (b21) {

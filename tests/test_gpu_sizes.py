@@ -11,7 +11,7 @@ cuFFT path
 (MX_TRANSFORM=cufft: cuFFT C2R with filter and threshold kernels that do not
 depend on the grid size and are held to the oracle at small sizes).  At 512^3
 find_HII_bubbles takes two radius batches and mx_step's threshold pass runs in
-four row slabs.  Every run's reported global means are also checked against
+eight row slabs.  Every run's reported global means are also checked against
 FP64 sums of the grids it returned (find_HII_bubbles.c:451-470,
 ComputeTs.c:942-974, BrightnessTemperature.c:530-545).
 """
@@ -204,7 +204,7 @@ def _run_512(transform, device, inputs, w, monkeypatch):
 def test_evolving_workload_512_fused_matches_cufft(monkeypatch):
     """One snapshot of the 512^3 workload (z = 10.26, 41 radii x 5 fields, 40
     shells) on the fused <512> transforms, through mx_step (host grids: the
-    remainder radius batch first, the last batch's threshold in four row
+    remainder radius batch first, the last batch's threshold in eight row
     slabs) and through mx_step_device (remainder last), against the cuFFT
     path on the same inputs.  The two fused runs must agree bit for bit; the
     fused and cuFFT runs within the parity tolerances (without oracle
