@@ -77,6 +77,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-adjoint", action="store_true",
+                    help="also time the 48-box batch with the adjoint of every box (Python workers)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="time the device step uncaptured")
     ap.add_argument("--adjoint-grid", type=int, default=256)
@@ -449,14 +451,32 @@ def run_gb300(args, rank, world, local):
     if plain:
         plain["ratio_to_value"] = round(plain["value"] / value, 3)
         out["plain_gpu"] = plain
+    # the legs beside the headline run in child processes of their own, each
+    # with a fresh CUDA context and the device memory to itself; a leg that
+    # fails is reported as such and the line is still printed
     if not args.no_adjoint and args.adjoint_grid > 0:
-        out["adjoint"] = run_adjoint_ratio(args)
+        out["adjoint"] = run_leg(f"bench.run_adjoint_ratio(bench.parse_args(['--adjoint-grid', '{args.adjoint_grid}']))")
     if not args.no_batch and world == 1:
-        out["batch"] = run_batch()
-        out["batch_native"] = run_batch_native()
+        if args.batch_adjoint:
+            out["batch"] = run_leg("bench.run_batch()")
+        out["batch_native"] = run_leg("bench.run_batch_native()")
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args)
     return out, rank
+
+
+def run_leg(call: str, timeout: float = 1800) -> dict:
+    """Runs `call` (an expression over this module) in a child process and
+    returns its JSON result, or {"error": ...} if the child failed."""
+    code = (f"import sys, json; sys.path.insert(0, {ROOT!r}); sys.path.insert(0, {os.path.join(ROOT, 'tests')!r});"
+            f"import bench; print(json.dumps({call}))")
+    try:
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=timeout)
+    except subprocess.TimeoutExpired:
+        return {"error": f"timed out after {timeout:.0f} s"}
+    if r.returncode != 0:
+        return {"error": (r.stderr.strip().splitlines() or ["exit code %d" % r.returncode])[-1][-300:]}
+    return json.loads(r.stdout.strip().splitlines()[-1])
 
 
 def run_adjoint_ratio(args, steps: int = 3):
